@@ -1,0 +1,333 @@
+"""Benchmark: validated edges/s of DiscreteMotionValidator::checkMotion on the planar 10-link
+kinematic-chain workload (32 world segments, segment fraction 0.005 of the extent, edges between
+valid states of a seeded 1M-state set), on one GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one batch of 100,000 edges checked by the batched form (persistent work-queue kernel,
+FP32 bulk with FP64 re-check, autotuned schedule). Twelve distinct batches (192 MB of endpoints,
+more than the 129 MB L2) rotate across steps, so no step re-reads L2-resident inputs. `e2e` is the
+same metric through the host-memory C-ABI call (gbo_check_motion_host: H2D of both endpoint
+arrays, kernel, D2H of results and lastValid fractions inside the timed region). Also reported:
+the plain one-launch-per-batch FP64 form on the same batches, state validity of the 1M states,
+and nearestK (k=16) over the 1M states.
+
+Under torchrun each rank runs an independent replica on its own GPU ("replicas only": the path
+has no exchange step); value = all ranks' edges / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_STATES = 1_000_000
+N_EDGES = 100_000
+N_BATCHES = 12
+KNN_QUERIES = 20_000
+METRIC = "validated edges/s (DiscreteMotionValidator, 10-link kinematic chain)"
+# algorithmic work of one checked state of the chain predicate: 20 sincos + 50 FMA-chain flops +
+# (55 + 352) segment tests x 21 flops, credited per checked state (states the reference's ordered
+# DiscreteMotionValidator evaluates)
+FLOP_PER_STATE = 50 + (55 + 352) * 21
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    return p.parse_args()
+
+
+def workload(seed=1):
+    from ompl_gb300 import workloads as W
+    return W.config1(seed=seed, n_states=N_STATES, n_edges=10, n_queries=10)
+
+
+def make_batches(valid_states, n_batches, seed=7):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_batches):
+        i = rng.integers(0, len(valid_states), N_EDGES)
+        j = rng.integers(0, len(valid_states), N_EDGES)
+        out.append((valid_states[i], valid_states[j]))
+    return out
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 8:
+                self.samples.append(p)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[4 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_edges_per_s(port, sd, cd, s1, s2, threads):
+    port.set_threads(threads)
+    t = time.perf_counter()
+    port.check_motion(sd, cd, s1, s2, want_state=False, want_bisect=False)
+    return len(s1) / (time.perf_counter() - t)
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle.oracle import CheckerDesc, Oracle, SpaceDesc
+    port = Oracle.port()
+    threads = os.cpu_count() or 1
+    port.set_threads(threads)
+    w = workload()
+    sd = SpaceDesc(w.space_kind, w.dim, link_length=w.link_length, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles)
+    valid = port.is_valid(sd, cd, w.states).astype(bool)
+    batches = make_batches(w.states[valid], N_BATCHES)
+    sample = 20_000
+    for i in range(args.warmup):
+        s1, s2 = batches[i % N_BATCHES]
+        port.check_motion(sd, cd, s1[:sample], s2[:sample], want_state=False, want_bisect=False)
+    t = time.perf_counter()
+    for i in range(args.steps):
+        s1, s2 = batches[i % N_BATCHES]
+        port.check_motion(sd, cd, s1[:sample], s2[:sample], want_state=True, want_bisect=False)
+    dt = time.perf_counter() - t
+    v = sample * args.steps / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "edges/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "kinematic_chain10: 1M states, 32 segments, edges between valid states, "
+                               "segment fraction 0.005", "edges_per_step": sample},
+        "cpu_baseline": {"value": v, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} edges per step of each 100k-edge batch, all host threads"},
+        "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def ours(args, rank, world, local_rank):
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import capi
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    w = workload()
+    space = B.KinematicChainSpace(w.dim, w.link_length)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.KinematicChainValidityChecker(space, w.obstacles)
+    checker.setPrecision("fp32_guarded")
+    mv = B.DiscreteMotionValidator(checker)
+    stream = torch.cuda.current_stream()
+
+    states_soa = torch.as_tensor(w.states.T.copy(), device=dev)
+    # validity of the 1M states (also yields the valid pool the edges are drawn from)
+    valid = checker.isValid(states_soa, soa=True)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(5):
+        valid = checker.isValid(states_soa, soa=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    states_per_s = 5 * N_STATES / (ev0.elapsed_time(ev1) * 1e-3)
+    vmask = valid.cpu().numpy().astype(bool)
+    host_batches = make_batches(w.states[vmask], N_BATCHES)
+    dev_batches = [(torch.as_tensor(a.T.copy(), device=dev), torch.as_tensor(b.T.copy(), device=dev))
+                   for a, b in host_batches]
+
+    def run(i, schedule):
+        s1, s2 = dev_batches[i % N_BATCHES]
+        return mv.checkMotions(s1, s2, schedule=schedule, soa=True)
+
+    for i in range(max(3, args.warmup)):
+        run(i, capi.SCHEDULE_AUTO)
+    torch.cuda.synchronize()
+    # checked states per batch (the reference's ordered DiscreteMotionValidator evaluates first_j
+    # states of an invalid motion and max(nd, 1) of a valid one)
+    checked = []
+    for i in range(N_BATCHES):
+        r = run(i, capi.SCHEDULE_AUTO)
+        fj, nd = r["first_j"].long(), r["nd"].long()
+        checked.append(int(torch.where(fj >= 0, fj, torch.clamp(nd, min=1)).sum().item()))
+    torch.cuda.synchronize()
+
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = B.launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local_rank) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            run(i, capi.SCHEDULE_AUTO)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = B.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = sum(step_ms) * 1e-3
+    t_local = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    dev_s, wall = t_local.tolist()
+    value = world * N_EDGES * args.steps / dev_s
+    mean_ms = statistics.mean(step_ms)
+    mean_checked = statistics.mean(checked[i % N_BATCHES] for i in range(args.steps))
+
+    # plain one-launch-per-batch FP64 form on the same batches
+    checker.setPrecision("fp64")
+    run(0, capi.SCHEDULE_PLAIN)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for i in range(N_BATCHES):
+        run(i, capi.SCHEDULE_PLAIN)
+    p1.record()
+    torch.cuda.synchronize()
+    plain_eps = N_BATCHES * N_EDGES / (p0.elapsed_time(p1) * 1e-3)
+    checker.setPrecision("fp32_guarded")
+    stats = checker.stats()
+
+    # end to end through the host-memory C-ABI call
+    mv.checkMotionHost(*host_batches[0])
+    t = time.perf_counter()
+    for i in range(args.steps):
+        mv.checkMotionHost(*host_batches[i % N_BATCHES])
+    e2e_s = time.perf_counter() - t
+    e2e = N_EDGES * args.steps / e2e_s
+
+    # nearestK k=16 over the 1M states
+    nn = B.NearestNeighborsGPU(space, capacity=N_STATES)
+    nn.add(states_soa, soa=True)
+    qi = np.random.default_rng(11).integers(0, N_STATES, KNN_QUERIES)
+    q = torch.as_tensor(w.states[qi].T.copy(), device=dev)
+    nn.nearestK(q[:, :256], 16, soa=True)
+    torch.cuda.synchronize()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record()
+    nn.nearestK(q, 16, soa=True, want_dist=False)
+    k1.record()
+    torch.cuda.synchronize()
+    knn_qps = KNN_QUERIES / (k0.elapsed_time(k1) * 1e-3)
+    knn_stats = nn.stats()
+
+    if rank != 0:
+        return
+    peak_fp32 = B.measure_fp32_peak()
+    achieved = mean_checked * FLOP_PER_STATE / (mean_ms * 1e-3)
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "motion_tile_chain10_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    # CPU baseline: the oracle port on all host threads, bounded sample of batch 0
+    from oracle.oracle import CheckerDesc, Oracle, SpaceDesc
+    port = Oracle.port()
+    sd = SpaceDesc(w.space_kind, w.dim, link_length=w.link_length, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles)
+    threads = os.cpu_count() or 1
+    sample = 20_000
+    cpu_v = cpu_edges_per_s(port, sd, cd, host_batches[0][0][:sample], host_batches[0][1][:sample], threads)
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic (seeded)",
+        "config": {"workload": "kinematic_chain10: 10 links x 0.1, 32 segments, 1M states, 100k edges/step between "
+                               "valid states, segment fraction 0.005, FP32 bulk + FP64 re-check, autotuned "
+                               "persistent schedule", "edges_per_step": N_EDGES, "batches_rotated": N_BATCHES,
+                   "l2": "inputs larger than L2 (12 x 16 MB batches rotate)", "parallelism": "replicas"},
+        "e2e": {"value": e2e, "unit": "edges/s", "h2d_bytes_per_step": 2 * N_EDGES * 10 * 8,
+                "d2h_bytes_per_step": N_EDGES * (1 + 8)},
+        "gpu_launches": launches,
+        "wall_s": wall,
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_fp32 / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak_fp32, "traffic": traffic,
+                     "peak_source": "FP32 FMA throughput measured in this run (gbo_measure_fp32_peak)",
+                     "work": f"{FLOP_PER_STATE} flop x checked states ({mean_checked:.0f} per step)"},
+        "cpu_baseline": {"value": cpu_v, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} edges of batch 0, oracle restatement, all host threads"},
+        "plain_fp64_edges_per_s": plain_eps,
+        "batched_vs_plain": value / world / plain_eps,
+        "states_per_s": states_per_s,
+        "knn_queries_per_s": knn_qps,
+        "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},
+        "recheck": stats,
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,172 @@
+/*
+ * gbompl — GB300 (sm_103a) implementation of OMPL's data-parallel inner loop behind a C ABI:
+ * state sampling, state validity, discrete motion checking and nearest-neighbour queries.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns a gbo_status and never
+ * throws. Device-pointer calls are asynchronous on the given stream (NULL = legacy default stream);
+ * `*_host` calls take host arrays and return when results are on the host.
+ *
+ * State layout. A batch of n states of dimension `dim` is passed as (ptr, n, ld, layout):
+ *   GBO_LAYOUT_SOA: value (i, d) at ptr[d * ld + i], ld >= n (coalesced; the native layout);
+ *   GBO_LAYOUT_AOS: value (i, d) at ptr[i * ld + d], ld >= dim (OMPL's per-state double arrays).
+ *
+ * Reference interfaces replaced (paths inside the OMPL source tree):
+ *   StateSampler::sampleUniform / sampleUniformNear        src/ompl/base/StateSampler.h:79-88
+ *     with RealVectorStateSampler / SO2StateSampler        src/ompl/base/spaces/src/RealVectorStateSpace.cpp:45-65,
+ *                                                           src/ompl/base/spaces/src/SO2StateSpace.cpp:46-56
+ *   StateValidityChecker::isValid                         src/ompl/base/StateValidityChecker.h:111
+ *   MotionValidator::checkMotion (both overloads), with    src/ompl/base/MotionValidator.h:83,99
+ *     DiscreteMotionValidator semantics                    src/ompl/base/src/DiscreteMotionValidator.cpp:48-145
+ *   StateSpace::validSegmentCount / distance / interpolate src/ompl/base/src/StateSpace.cpp:851-854
+ *   SpaceInformation::checkMotion(states, count, first)    src/ompl/base/src/SpaceInformation.cpp:288-341
+ *   NearestNeighbors<T>::add/remove/nearestK/nearestR/size/clear
+ *                                                          src/ompl/datastructures/NearestNeighbors.h:58-110
+ */
+#ifndef GBOMPL_H
+#define GBOMPL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gbo_status;
+enum {
+    GBO_OK = 0,
+    GBO_ERR_INVALID_ARGUMENT = 1, /* bad handle, size, kind or pointer (OMPL throws ompl::Exception here) */
+    GBO_ERR_CUDA = 2,             /* a CUDA runtime call failed; gbo_last_error() has the message */
+    GBO_ERR_NO_DEVICE = 3,        /* no CUDA device, or not an sm_103 device */
+    GBO_ERR_OUT_OF_MEMORY = 4,    /* device or pinned allocation failed / admission refused */
+    GBO_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out (kernel returned early) */
+    GBO_ERR_UNSUPPORTED = 6       /* combination not implemented (e.g. dim above 16) */
+};
+
+typedef struct gbo_space gbo_space;       /* a state space: metric, interpolation, bounds, segment length */
+typedef struct gbo_checker gbo_checker;   /* a validity checker bound to a space and a device-resident world */
+typedef struct gbo_sampler gbo_sampler;   /* a state sampler with its own mt19937 stream */
+typedef struct gbo_nn gbo_nn;             /* a device-resident nearest-neighbour index */
+typedef void *gbo_stream;                 /* a cudaStream_t */
+
+enum { GBO_LAYOUT_SOA = 0, GBO_LAYOUT_AOS = 1 };
+
+enum {
+    GBO_SPACE_REAL_VECTOR = 0,     /* RealVectorStateSpace: L2, linear interpolation, box bounds */
+    GBO_SPACE_SO2 = 1,             /* SO2StateSpace (dim 1) */
+    GBO_SPACE_KINEMATIC_CHAIN = 2, /* KinematicChainSpace of demos/KinematicChain.h (param = link length) */
+    GBO_SPACE_WRAP_L2 = 3          /* joint space on [-pi,pi]^dim, L2 over wrapped differences */
+};
+
+enum {
+    GBO_CHECK_ALL_VALID = 0,      /* AllValidStateValidityChecker */
+    GBO_CHECK_CIRCLES = 1,        /* point robot vs circles; world rows (x, y, r) */
+    GBO_CHECK_CHAIN_SEGMENTS = 2, /* KinematicChainValidityChecker; world rows (x0, y0, x1, y1) */
+    GBO_CHECK_DH_SPHERES = 3      /* DH serial arm covered by spheres vs world spheres (x, y, z, r) */
+};
+
+/* Arithmetic of validity / motion / kNN evaluation. */
+enum {
+    GBO_PRECISION_FP64 = 0,        /* FP64 throughout, reference operation order (the plain form) */
+    GBO_PRECISION_FP32_GUARDED = 1 /* FP32 bulk; anything within the guard band re-evaluated in FP64 */
+};
+
+/* Motion-batch schedules. */
+enum {
+    GBO_SCHEDULE_PLAIN = 0, /* one launch, one warp per edge, 32 steps per ballot, FP64 (drop-in) */
+    GBO_SCHEDULE_TILE = 1,  /* persistent: 32 edges per warp, lanes re-spread over live edges */
+    GBO_SCHEDULE_WARP = 2,  /* persistent: one warp per edge from the work queue */
+    GBO_SCHEDULE_AUTO = 3   /* autotuned between TILE and WARP (cached per checker) */
+};
+
+/* ---- errors / device ---- */
+const char *gbo_status_string(gbo_status s);
+const char *gbo_last_error(void); /* message of the last failure on this thread ("" if none) */
+gbo_status gbo_device_check(int *sm_count, int *cc_major, int *cc_minor);
+
+/* ---- state spaces ---- (StateSpace::setup, getLongestValidSegmentLength, validSegmentCount)
+ * low/high: dim bounds (REAL_VECTOR only; may be NULL otherwise). lvs and factor are the values the
+ * OMPL space reports (getLongestValidSegmentLength(), getValidSegmentCountFactor()); pass lvs <= 0 to
+ * have them computed as maximumExtent * lvs_fraction like StateSpace::setup. */
+gbo_status gbo_space_create(int kind, int dim, const double *low, const double *high, double param, double lvs,
+                            double lvs_fraction, unsigned factor, gbo_space **out);
+gbo_status gbo_space_destroy(gbo_space *s);
+gbo_status gbo_space_info(const gbo_space *s, double *max_extent, double *lvs);
+/* distance(a_i, b_i), interpolate(a_i, b_i, t_i), validSegmentCount(a_i, b_i) over batches (device). */
+gbo_status gbo_space_distance(const gbo_space *s, const double *a, const double *b, int64_t n, int64_t ld, int layout,
+                              double *out, gbo_stream stream);
+gbo_status gbo_space_interpolate(const gbo_space *s, const double *a, const double *b, const double *t, int64_t n,
+                                 int64_t ld, int layout, double *out, gbo_stream stream);
+
+/* ---- validity checkers ----
+ * world: n_world rows of 3 (circles) or 4 (segments, spheres) doubles, host memory, copied to the device.
+ * dh: n_joints rows (a, d, alpha_code), alpha_code in {0, +1, -1} = alpha 0, +pi/2, -pi/2 (DH_SPHERES). */
+gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *world, int64_t n_world,
+                              const double *dh, int n_joints, int spheres_per_link, double sphere_radius,
+                              gbo_checker **out);
+gbo_status gbo_checker_destroy(gbo_checker *c);
+gbo_status gbo_checker_set_precision(gbo_checker *c, int precision);
+/* Re-check statistics of the last FP32_GUARDED call: states evaluated, states re-checked in FP64. */
+gbo_status gbo_checker_stats(const gbo_checker *c, uint64_t *evaluated, uint64_t *rechecked);
+
+/* StateValidityChecker::isValid over a batch: out[i] = 1 valid, 0 invalid. */
+gbo_status gbo_is_valid(gbo_checker *c, const double *states, int64_t n, int64_t ld, int layout, uint8_t *out,
+                        gbo_stream stream);
+
+/* DiscreteMotionValidator::checkMotion over a batch of edges (s1_i -> s2_i):
+ *   ok[i]      1 when the motion is valid (both overloads agree on this);
+ *   first_j[i] ordered-variant index of the first invalid checked state: 1..nd-1 interpolated,
+ *              nd for s2 itself, -1 when valid [nullable];
+ *   nd[i]      validSegmentCount(s1, s2) [nullable].
+ * lastValid.second = (first_j - 1) / nd (FP64 division, as DiscreteMotionValidator.cpp:66,79) and
+ * lastValid.first = interpolate(s1, s2, lastValid.second) are produced by gbo_last_valid. */
+gbo_status gbo_check_motion(gbo_checker *c, const double *s1, const double *s2, int64_t n, int64_t ld, int layout,
+                            int schedule, uint8_t *ok, int32_t *first_j, int32_t *nd, gbo_stream stream);
+gbo_status gbo_last_valid(const gbo_space *s, const double *s1, const double *s2, const int32_t *first_j,
+                          const int32_t *nd, int64_t n, int64_t ld, int layout, double *last_t, double *last_state,
+                          gbo_stream stream);
+/* SpaceInformation::checkMotion(states, count, firstInvalidStateIndex): one ordered chain of states. */
+gbo_status gbo_check_motion_states(gbo_checker *c, const double *states, int64_t count, int64_t ld, int layout,
+                                   uint8_t *ok, int64_t *first_invalid, gbo_stream stream);
+
+/* Host-memory drop-ins (AoS rows like OMPL states); staging buffers are owned by the checker. */
+gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, uint8_t *out);
+gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double *s2, int64_t n, uint8_t *ok,
+                                 double *last_t, double *last_state);
+
+/* ---- samplers ---- RNG seeded like RNG::setLocalSeed(seed); one sampler = one sequential stream. */
+gbo_status gbo_sampler_create(const gbo_space *space, uint32_t local_seed, gbo_sampler **out);
+gbo_status gbo_sampler_destroy(gbo_sampler *s);
+gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream);
+gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double distance, int64_t n, int64_t ld,
+                                   int layout, double *out, gbo_stream stream);
+
+/* ---- nearest neighbours ---- (NearestNeighbors<T>; element key = insertion index) */
+gbo_status gbo_nn_create(const gbo_space *space, int64_t capacity, gbo_nn **out);
+gbo_status gbo_nn_destroy(gbo_nn *nn);
+gbo_status gbo_nn_set_precision(gbo_nn *nn, int precision);
+gbo_status gbo_nn_add(gbo_nn *nn, const double *states, int64_t n, int64_t ld, int layout, int64_t *first_key,
+                      gbo_stream stream);
+gbo_status gbo_nn_remove(gbo_nn *nn, const int64_t *keys, int64_t n, gbo_stream stream);
+gbo_status gbo_nn_clear(gbo_nn *nn);
+gbo_status gbo_nn_size(const gbo_nn *nn, int64_t *size);
+/* nearestK: idx/dist are nq x k row-major, sorted by (distance, key); -1 / +inf padding when fewer
+ * than k elements. prefix (nullable): query i only sees keys < prefix[i] (PRM insertion order).
+ * dist may be NULL. distance is evaluated as distance(element, query), like NearestNeighborsLinear. */
+gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
+                            const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream);
+/* nearestR (distance <= r): counts per query, then the CSR fill given the exclusive-scan offsets. */
+gbo_status gbo_nn_nearest_r_count(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
+                                  int64_t *counts, gbo_stream stream);
+gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
+                                 const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream);
+gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks);
+
+/* ---- measurement helper ---- FP32 FMA throughput of this GPU (FLOP/s), for roofline denominators. */
+gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
+/* Number of kernels this library launched since load (for launch accounting). */
+uint64_t gbo_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

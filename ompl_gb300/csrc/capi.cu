@@ -1,0 +1,1226 @@
+// C ABI of libgbompl (include/gbompl.h): object lifetimes, argument checking, guard-band bounds,
+// the uniform grid over world spheres, staging for host-memory calls, and kernel launches.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels_nn.cuh"
+
+using namespace gbo;
+
+namespace
+{
+thread_local std::string g_err;
+std::atomic<unsigned long long> g_launches{0};
+
+gbo_status fail(gbo_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+#define CUDA_TRY(expr)                                                                                               \
+    do                                                                                                               \
+    {                                                                                                                \
+        cudaError_t _e = (expr);                                                                                     \
+        if (_e != cudaSuccess)                                                                                       \
+            return fail(_e == cudaErrorMemoryAllocation ? GBO_ERR_OUT_OF_MEMORY : GBO_ERR_CUDA,                      \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));                                         \
+    } while (0)
+
+#define CHECK_LAUNCH()                                                                                               \
+    do                                                                                                               \
+    {                                                                                                                \
+        cudaError_t _e = cudaGetLastError();                                                                         \
+        if (_e != cudaSuccess)                                                                                       \
+            return fail(GBO_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(_e));                      \
+    } while (0)
+
+int g_sm_count = 0;
+int g_device_ok = -1;  // -1 unknown, 0 no, 1 yes
+
+gbo_status ensure_device()
+{
+    if (g_device_ok == 1)
+        return GBO_OK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    {
+        cudaGetLastError();
+        g_device_ok = 0;
+        return fail(GBO_ERR_NO_DEVICE, "no CUDA device");
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+        return fail(GBO_ERR_NO_DEVICE, "cudaGetDeviceProperties failed");
+    if (!(p.major == 10 && p.minor == 3))
+        return fail(GBO_ERR_NO_DEVICE, "libgbompl is built for sm_103a only; device is sm_" +
+                                           std::to_string(p.major) + std::to_string(p.minor));
+    g_sm_count = p.multiProcessorCount;
+    g_device_ok = 1;
+    return GBO_OK;
+}
+
+LaunchCfg lcfg(gbo_stream s)
+{
+    LaunchCfg lc;
+    lc.stream = (cudaStream_t)s;
+    lc.sm_count = g_sm_count;
+    return lc;
+}
+
+constexpr double kU32 = 5.9604644775390625e-08;  // 2^-24, FP32 unit roundoff
+constexpr double kPiH = 3.141592653589793238462643383279502884;
+
+bool valid_layout(int layout, int64_t n, int64_t ld, int dim)
+{
+    if (layout == GBO_LAYOUT_SOA)
+        return ld >= n;
+    if (layout == GBO_LAYOUT_AOS)
+        return ld >= dim;
+    return false;
+}
+
+// Ring of device counter slots so that calls in flight on different streams do not share one.
+struct CounterRing
+{
+    RunCounters *dev = nullptr;
+    std::atomic<unsigned> next{0};
+    unsigned last = 0;
+    static constexpr unsigned kSlots = 64;
+    gbo_status init()
+    {
+        CUDA_TRY(cudaMalloc(&dev, sizeof(RunCounters) * kSlots));
+        CUDA_TRY(cudaMemset(dev, 0, sizeof(RunCounters) * kSlots));
+        return GBO_OK;
+    }
+    RunCounters *take(cudaStream_t s)
+    {
+        unsigned i = next.fetch_add(1) % kSlots;
+        last = i;
+        cudaMemsetAsync(dev + i, 0, sizeof(RunCounters), s);
+        return dev + i;
+    }
+    ~CounterRing()
+    {
+        if (dev)
+            cudaFree(dev);
+    }
+};
+
+struct Pinned
+{
+    void *p = nullptr;
+    size_t bytes = 0;
+    gbo_status reserve(size_t b)
+    {
+        if (b <= bytes)
+            return GBO_OK;
+        if (p)
+            cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        CUDA_TRY(cudaMallocHost(&p, b));
+        bytes = b;
+        return GBO_OK;
+    }
+    ~Pinned()
+    {
+        if (p)
+            cudaFreeHost(p);
+    }
+};
+
+struct DevBuf
+{
+    void *p = nullptr;
+    size_t bytes = 0;
+    gbo_status reserve(size_t b)
+    {
+        if (b <= bytes)
+            return GBO_OK;
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        CUDA_TRY(cudaMalloc(&p, b));
+        bytes = b;
+        return GBO_OK;
+    }
+    ~DevBuf()
+    {
+        if (p)
+            cudaFree(p);
+    }
+};
+
+size_t pad16(size_t b)
+{
+    return (b + 15) & ~size_t(15);
+}
+}  // namespace
+
+struct gbo_space
+{
+    SpaceParams sp{};
+    double extent = 0.0;
+};
+
+struct gbo_checker
+{
+    SpaceParams sp{};
+    int kind = 0;
+    int precision = GBO_PRECISION_FP64;
+    WorldArgs wa{};
+    void *d64 = nullptr, *d32 = nullptr;
+    int *cell_start = nullptr, *cell_items = nullptr;
+    CounterRing ctr;
+    int tuned_schedule = -1;
+    std::mutex mu;
+    cudaStream_t host_stream = nullptr;
+    Pinned pin_in, pin_out;
+    DevBuf dev_in, dev_out;
+    ~gbo_checker()
+    {
+        if (d64)
+            cudaFree(d64);
+        if (d32)
+            cudaFree(d32);
+        if (cell_start)
+            cudaFree(cell_start);
+        if (cell_items)
+            cudaFree(cell_items);
+        if (host_stream)
+            cudaStreamDestroy(host_stream);
+    }
+};
+
+struct gbo_sampler
+{
+    SpaceParams sp{};
+    SamplerState *st = nullptr;
+    ~gbo_sampler()
+    {
+        if (st)
+            cudaFree(st);
+    }
+};
+
+struct gbo_nn
+{
+    SpaceParams sp{};
+    int precision = GBO_PRECISION_FP32_GUARDED;
+    int64_t cap = 0, size = 0, alive_count = 0;
+    int F = 0;
+    double *pts64 = nullptr;
+    float *feat32 = nullptr;
+    unsigned char *alive = nullptr;
+    float eps32 = 0.f;
+    DevBuf qfeat, fb_list;
+    CounterRing ctr;
+    unsigned long long queries = 0;
+    ~gbo_nn()
+    {
+        if (pts64)
+            cudaFree(pts64);
+        if (feat32)
+            cudaFree(feat32);
+        if (alive)
+            cudaFree(alive);
+    }
+};
+
+namespace gbo
+{
+void note_launch()
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+int persistent_grid(const void *kernel, int block, unsigned smem, const LaunchCfg &lc, int64_t max_blocks)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void *, unsigned>, int> occ;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto key = std::make_pair(kernel, smem);
+        auto it = occ.find(key);
+        if (it == occ.end())
+        {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+            if (per_sm < 1)
+                per_sm = 1;
+            occ[key] = per_sm;
+        }
+        else
+            per_sm = it->second;
+    }
+    int64_t g = (int64_t)per_sm * lc.sm_count;
+    if (max_blocks < g)
+        g = max_blocks;
+    return (int)(g < 1 ? 1 : g);
+}
+
+unsigned world_smem_bytes(const WorldArgs &wa, int precision)
+{
+    if (precision == GBO_PRECISION_FP32_GUARDED &&
+        (wa.kind == GBO_CHECK_CHAIN_SEGMENTS || wa.kind == GBO_CHECK_DH_SPHERES))
+        return wa.stage32 ? wa.bytes32 : 0;
+    return wa.stage64 ? wa.bytes64 : 0;
+}
+}  // namespace gbo
+
+namespace
+{
+// Guard-band bounds of the FP32 kinematic-chain test (see checkers.cuh). All bounds are
+// worst-case: eps_dir covers float conversion of the reduced angle (u*pi) plus the sincosf error
+// (2 ulp); link vectors VX = c*L have error L*(eps_dir + 2u); a position after k links has error
+// k*(L*(eps_dir + u) + u*R) with R the reach; a cross product a x b of vectors with component
+// magnitudes <= A, B and component errors da, db has error 2*(da*B + db*A + da*db) + 3u*A*B.
+// Each bound is inflated by a safety factor of 2.
+void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, std::vector<ChainSegF32> &segs,
+                  float &e_dist)
+{
+    const double u = kU32, L = sp.link, nl = sp.dim;
+    const double eps_dir = kU32 * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+    const double R = nl * L + 0.001;
+    const double dV = L * (eps_dir + 2 * u) + 1e-15;
+    const double dP = (nl + 1) * (L * (eps_dir + u) + u * R) + 1e-15;
+    auto cross = [&](double A, double B, double da, double db) {
+        return 2.0 * (da * B + db * A + da * db) + 3.0 * u * A * B + 1e-15;
+    };
+    const double safety = 2.0;
+    g.eps_dir = (float)eps_dir;
+    {
+        const double A = L, B = L, C = 2 * R, dC = 2 * dP + 2 * u * R;
+        const double eden = cross(A, B, dV, dV), es = cross(A, C, dV, dC), et = cross(B, C, dV, dC);
+        g.self_den = (float)(safety * eden + 1e-12);
+        g.self_s = (float)(safety * es);
+        g.self_t = (float)(safety * et);
+        g.self_u = (float)(safety * (es + eden + u * 2 * (A * C + A * B)));
+        g.self_v = (float)(safety * (et + eden + u * 2 * (B * C + A * B)));
+    }
+    segs.resize(n);
+    for (int j = 0; j < n; ++j)
+    {
+        const double x0 = w[4 * j], y0 = w[4 * j + 1], x1 = w[4 * j + 2], y1 = w[4 * j + 3];
+        const double sx = x1 - x0, sy = y1 - y0;
+        const double B = std::max(std::fabs(sx), std::fabs(sy));
+        const double W0 = std::max(std::fabs(x0), std::fabs(y0));
+        const double A = L, C = R + W0;
+        const double dB = u * B, dC = dP + u * W0 + u * C;
+        const double eden = cross(A, B, dV, dB), es = cross(A, C, dV, dC), et = cross(B, C, dB, dC);
+        ChainSegF32 s{};
+        s.x0 = (float)x0;
+        s.y0 = (float)y0;
+        s.sx = (float)sx;
+        s.sy = (float)sy;
+        s.e_den = (float)(safety * eden + 1e-12);
+        s.e_s = (float)(safety * es);
+        s.e_t = (float)(safety * et);
+        s.e_u = (float)(safety * (es + eden + u * 2 * (A * C + A * B)));
+        s.e_v = (float)(safety * (et + eden + u * 2 * (B * C + A * B)));
+        segs[j] = s;
+    }
+    // workspace distance (segment_count, FP32 form): dx_i accumulates 2i direction errors and i
+    // roundings of partial sums bounded by 2i; the norm adds |ddx| + |ddy| and a relative 2^-22.
+    double e = 0.0;
+    for (int i = 1; i <= sp.dim; ++i)
+    {
+        const double ddx = 2.0 * i * eps_dir + u * 2.0 * i * i;
+        e += 2.0 * ddx + std::ldexp(1.0, -21) * 2.0 * i;
+    }
+    e = L * (e + u * sp.dim * 2.0 * sp.dim) + u * L * 2.0 * sp.dim * sp.dim;
+    e_dist = (float)(safety * e);
+}
+
+// Chain kNN features X_i = sum_{m<=i} cos(theta_m) accumulate i direction errors and i roundings.
+float chain_knn_eps(const SpaceParams &sp)
+{
+    const double u = kU32, L = sp.link;
+    const double eps_dir = kU32 * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+    double e = 0.0;
+    for (int i = 1; i <= sp.dim; ++i)
+    {
+        const double dX = i * eps_dir + u * i * i;            // one feature
+        const double ddx = 2.0 * dX + u * 2.0 * i;            // difference of features
+        e += 2.0 * ddx + std::ldexp(1.0, -21) * 2.0 * i + u * 2.0 * i * sp.dim;
+    }
+    return (float)(2.0 * L * e * 1.01 + 1e-12);
+}
+
+// Box / wrapped spaces: features are coordinates rounded to FP32 (error u*|x|), squared distance
+// accumulated with FMA (relative error <= (dim + 2) u); bound on |sqrt(s32) - d64|.
+float box_knn_eps(const SpaceParams &sp)
+{
+    double m2 = 0.0, span2 = 0.0;
+    for (int d = 0; d < sp.dim; ++d)
+    {
+        const double lo = sp.kind == GBO_SPACE_REAL_VECTOR ? sp.low[d] : -kPiH;
+        const double hi = sp.kind == GBO_SPACE_REAL_VECTOR ? sp.high[d] : kPiH;
+        const double m = std::max(std::fabs(lo), std::fabs(hi));
+        m2 += m * m;
+        span2 += (hi - lo) * (hi - lo);
+    }
+    const double coord = 2.0 * kU32 * std::sqrt(m2) + (sp.kind == GBO_SPACE_REAL_VECTOR ? 0.0 : 4.0 * kU32 * 7.0);
+    const double rel = (sp.dim + 4) * kU32 * std::sqrt(span2);
+    return (float)(2.0 * (coord + rel) + 1e-12);
+}
+}  // namespace
+
+extern "C" {
+
+const char *gbo_status_string(gbo_status s)
+{
+    switch (s)
+    {
+        case GBO_OK:
+            return "ok";
+        case GBO_ERR_INVALID_ARGUMENT:
+            return "invalid argument";
+        case GBO_ERR_CUDA:
+            return "CUDA error";
+        case GBO_ERR_NO_DEVICE:
+            return "no usable device";
+        case GBO_ERR_OUT_OF_MEMORY:
+            return "out of memory";
+        case GBO_ERR_TIMEOUT:
+            return "device wait timed out";
+        case GBO_ERR_UNSUPPORTED:
+            return "unsupported";
+        default:
+            return "unknown status";
+    }
+}
+
+const char *gbo_last_error(void)
+{
+    return g_err.c_str();
+}
+
+uint64_t gbo_launch_count(void)
+{
+    return g_launches.load();
+}
+
+gbo_status gbo_device_check(int *sm_count, int *cc_major, int *cc_minor)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    {
+        cudaGetLastError();
+        return fail(GBO_ERR_NO_DEVICE, "no CUDA device");
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    if (sm_count)
+        *sm_count = p.multiProcessorCount;
+    if (cc_major)
+        *cc_major = p.major;
+    if (cc_minor)
+        *cc_minor = p.minor;
+    return ensure_device();
+}
+
+// ---------------------------------------------------------------- spaces
+gbo_status gbo_space_create(int kind, int dim, const double *low, const double *high, double param, double lvs,
+                            double lvs_fraction, unsigned factor, gbo_space **out)
+{
+    if (!out)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (kind < GBO_SPACE_REAL_VECTOR || kind > GBO_SPACE_WRAP_L2)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "unknown space kind");
+    if (dim < 1 || dim > GBO_MAXD)
+        return fail(dim > GBO_MAXD ? GBO_ERR_UNSUPPORTED : GBO_ERR_INVALID_ARGUMENT, "dimension must be 1..16");
+    if (kind == GBO_SPACE_SO2 && dim != 1)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "SO2 has dimension 1");
+    if (kind == GBO_SPACE_REAL_VECTOR && (!low || !high))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "RealVector bounds required");
+    if (factor < 1)
+        return fail(GBO_ERR_INVALID_ARGUMENT,
+                    "The multiplicative factor for the valid segment count between two states must be strictly positive");
+    auto *s = new gbo_space();
+    s->sp.kind = kind;
+    s->sp.dim = dim;
+    s->sp.factor = factor;
+    s->sp.link = param;
+    for (int d = 0; d < dim; ++d)
+    {
+        if (kind == GBO_SPACE_REAL_VECTOR)
+        {
+            if (!(low[d] <= high[d]))
+            {
+                delete s;
+                return fail(GBO_ERR_INVALID_ARGUMENT, "lower bound above upper bound");
+            }
+            s->sp.low[d] = low[d];
+            s->sp.high[d] = high[d];
+        }
+        else
+        {
+            s->sp.low[d] = -kPiH;
+            s->sp.high[d] = kPiH;
+        }
+    }
+    // StateSpace::setup (StateSpace.cpp:237-249) with the kind's getMaximumExtent
+    double e = 0.0;
+    if (kind == GBO_SPACE_SO2)
+        e = kPiH;
+    else
+    {
+        for (int d = 0; d < dim; ++d)
+        {
+            const double r = kind == GBO_SPACE_WRAP_L2 ? kPiH : s->sp.high[d] - s->sp.low[d];
+            e += r * r;
+        }
+        e = std::sqrt(e);
+    }
+    s->extent = e;
+    if (lvs <= 0.0)
+    {
+        const double eps = 2.220446049250313e-16;
+        if (lvs_fraction < eps || lvs_fraction > 1.0 - eps)
+        {
+            delete s;
+            return fail(GBO_ERR_INVALID_ARGUMENT, "The fraction of the extent must be larger than 0 and less than 1");
+        }
+        lvs = e * lvs_fraction;
+    }
+    if (!(lvs >= 2.220446049250313e-16))
+    {
+        delete s;
+        return fail(GBO_ERR_INVALID_ARGUMENT, "The longest valid segment must be positive.");
+    }
+    s->sp.lvs = lvs;
+    *out = s;
+    return GBO_OK;
+}
+
+gbo_status gbo_space_destroy(gbo_space *s)
+{
+    delete s;
+    return GBO_OK;
+}
+
+gbo_status gbo_space_info(const gbo_space *s, double *max_extent, double *lvs)
+{
+    if (!s)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "space is NULL");
+    if (max_extent)
+        *max_extent = s->extent;
+    if (lvs)
+        *lvs = s->sp.lvs;
+    return GBO_OK;
+}
+
+gbo_status gbo_space_distance(const gbo_space *s, const double *a, const double *b, int64_t n, int64_t ld, int layout,
+                              double *out, gbo_stream stream)
+{
+    if (!s || (n > 0 && (!a || !b || !out)) || n < 0 || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad distance arguments");
+    if (auto st = ensure_device())
+        return st;
+    launch_distance(lcfg(stream), s->sp, make_view(a, ld, layout), make_view(b, ld, layout), n, out);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_space_interpolate(const gbo_space *s, const double *a, const double *b, const double *t, int64_t n,
+                                 int64_t ld, int layout, double *out, gbo_stream stream)
+{
+    if (!s || (n > 0 && (!a || !b || !t || !out)) || n < 0 || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad interpolate arguments");
+    if (auto st = ensure_device())
+        return st;
+    StatesView ov = make_view(out, ld, layout);
+    launch_interpolate(lcfg(stream), s->sp, make_view(a, ld, layout), make_view(b, ld, layout), t, n,
+                       MutStatesView{out, ov.si, ov.sd});
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+// ---------------------------------------------------------------- checkers
+gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *world, int64_t n_world,
+                              const double *dh, int n_joints, int spheres_per_link, double sphere_radius,
+                              gbo_checker **out)
+{
+    if (!space || !out)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "space/out is NULL");
+    if (kind < GBO_CHECK_ALL_VALID || kind > GBO_CHECK_DH_SPHERES)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "unknown checker kind");
+    if (n_world < 0 || (n_world > 0 && !world) || n_world > (1 << 24))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad world");
+    const SpaceParams &sp = space->sp;
+    if (kind == GBO_CHECK_CIRCLES && sp.dim != 2)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "the circle checker needs a 2-D space");
+    if (kind == GBO_CHECK_CHAIN_SEGMENTS && sp.kind != GBO_SPACE_KINEMATIC_CHAIN)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "the chain checker needs a kinematic-chain space");
+    if (kind == GBO_CHECK_DH_SPHERES &&
+        (!dh || n_joints < 1 || n_joints > 8 || n_joints != sp.dim || spheres_per_link < 1 || sphere_radius < 0))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad DH arm (1..8 joints = space dimension)");
+    if (auto st = ensure_device())
+        return st;
+    auto *c = new gbo_checker();
+    c->sp = sp;
+    c->kind = kind;
+    WorldArgs &wa = c->wa;
+    wa.kind = kind;
+    wa.n = (int)n_world;
+    wa.inv_lvs32 = (float)(1.0 / sp.lvs);
+    auto cleanup = [&](gbo_status s) {
+        delete c;
+        return s;
+    };
+    if (c->ctr.init() != GBO_OK)
+        return cleanup(GBO_ERR_OUT_OF_MEMORY);
+    std::vector<double> w64;
+    if (kind == GBO_CHECK_CIRCLES)
+    {
+        for (int64_t i = 0; i < n_world; ++i)
+        {
+            w64.push_back(world[3 * i]);
+            w64.push_back(world[3 * i + 1]);
+            w64.push_back(world[3 * i + 2] * world[3 * i + 2]);  // circles2D.h:51 r2_ = r * r
+        }
+    }
+    else if (kind != GBO_CHECK_ALL_VALID)
+        w64.assign(world, world + 4 * n_world);
+    size_t b64 = pad16(w64.size() * sizeof(double));
+    if (b64)
+    {
+        if (cudaMalloc(&c->d64, b64) != cudaSuccess)
+            return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "world allocation failed"));
+        cudaMemset(c->d64, 0, b64);
+        cudaMemcpy(c->d64, w64.data(), w64.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    wa.data64 = c->d64;
+    wa.bytes64 = (unsigned)b64;
+    wa.stage64 = (b64 > 0 && b64 <= 96 * 1024 && kind != GBO_CHECK_DH_SPHERES) ? 1 : 0;
+    if (kind == GBO_CHECK_CHAIN_SEGMENTS)
+    {
+        std::vector<ChainSegF32> segs;
+        chain_bounds(sp, world, (int)n_world, wa.guard, segs, wa.e_dist);
+        size_t b32 = pad16(segs.size() * sizeof(ChainSegF32));
+        if (b32)
+        {
+            if (cudaMalloc(&c->d32, b32) != cudaSuccess)
+                return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "world allocation failed"));
+            cudaMemcpy(c->d32, segs.data(), segs.size() * sizeof(ChainSegF32), cudaMemcpyHostToDevice);
+        }
+        wa.data32 = c->d32;
+        wa.bytes32 = (unsigned)b32;
+        wa.stage32 = b32 > 0 && b32 <= 96 * 1024;
+        if (!wa.stage32 && b32)
+            return cleanup(fail(GBO_ERR_UNSUPPORTED, "segment world too large for shared memory"));
+    }
+    if (kind == GBO_CHECK_DH_SPHERES)
+    {
+        DHArm &arm = wa.arm;
+        arm.joints = n_joints;
+        arm.spl = spheres_per_link;
+        arm.rs = sphere_radius;
+        for (int i = 0; i < n_joints; ++i)
+        {
+            arm.a[i] = dh[3 * i];
+            arm.d[i] = dh[3 * i + 1];
+            const int code = (int)dh[3 * i + 2];
+            if (code < -1 || code > 1)
+                return cleanup(fail(GBO_ERR_INVALID_ARGUMENT, "alpha code must be -1, 0 or +1"));
+            arm.ca[i] = code == 0 ? 1.f : 0.f;
+            arm.sa[i] = code == 0 ? 0.f : (float)code;
+            arm.af[i] = (float)arm.a[i];
+            arm.dfl[i] = (float)arm.d[i];
+        }
+        // FP32 spheres
+        std::vector<float> s32(4 * n_world);
+        double rmax = 0.0;
+        for (int64_t i = 0; i < 4 * n_world; ++i)
+            s32[i] = (float)world[i];
+        for (int64_t i = 0; i < n_world; ++i)
+            rmax = std::max(rmax, world[4 * i + 3]);
+        size_t b32 = pad16(s32.size() * sizeof(float));
+        if (b32)
+        {
+            if (cudaMalloc(&c->d32, b32) != cudaSuccess)
+                return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "world allocation failed"));
+            cudaMemcpy(c->d32, s32.data(), s32.size() * sizeof(float), cudaMemcpyHostToDevice);
+        }
+        wa.data32 = c->d32;
+        wa.bytes32 = (unsigned)b32;
+        wa.stage32 = b32 > 0 && b32 <= 160 * 1024;
+        // FK error bound in FP32 (spectral-norm propagation): |dR_k| <= k (2 eps_t + 16u),
+        // |dp| <= sum_k (|dR_k| |pA| + |pA| (eps_t + u) + 4u (|p| + |pA|)); centres add 3u|p|.
+        const double u = kU32, eps_t = u * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+        double dR = 0.0, dp = 0.0, reach = 0.0;
+        for (int i = 0; i < n_joints; ++i)
+        {
+            const double pa = std::sqrt(arm.a[i] * arm.a[i] + arm.d[i] * arm.d[i]);
+            reach += pa;
+            dp += dR * pa + pa * (eps_t + u) * 2.0 + 4.0 * u * (reach + pa);
+            dR += 2.0 * eps_t + 16.0 * u;
+        }
+        const double dc = (dp + 3.0 * u * reach) * std::sqrt(3.0);  // Euclidean centre error
+        // near contact |d| <= 0.2 + rs + rmax: |d^2 - d_ref^2| <= 2|d| dc + dc^2 (+ rounding of d^2, rr^2)
+        const double D = 2.0 * (sphere_radius + rmax);
+        const double E = 2.0 * D * dc + dc * dc + 8.0 * u * D * D + 4.0 * u * (D * D);
+        wa.dh_e = (float)(2.0 * E);
+        // uniform grid: each sphere goes into every cell its box grown by rs + margin overlaps
+        const int G = 32;
+        const double margin = 1e-3;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int64_t i = 0; i < n_world; ++i)
+            for (int r = 0; r < 3; ++r)
+            {
+                const double ext = world[4 * i + 3] + sphere_radius + margin;
+                lo[r] = std::min(lo[r], world[4 * i + r] - ext);
+                hi[r] = std::max(hi[r], world[4 * i + r] + ext);
+            }
+        if (n_world == 0)
+            for (int r = 0; r < 3; ++r)
+            {
+                lo[r] = -1;
+                hi[r] = 1;
+            }
+        double inv[3];
+        for (int r = 0; r < 3; ++r)
+        {
+            lo[r] -= margin;
+            hi[r] += margin;
+            inv[r] = G / (hi[r] - lo[r]);
+            wa.glo64[r] = lo[r];
+            wa.ginv64[r] = inv[r];
+            wa.glo[r] = (float)lo[r];
+            wa.ginv[r] = (float)inv[r];
+        }
+        std::vector<std::vector<int>> cells((size_t)G * G * G);
+        for (int64_t i = 0; i < n_world; ++i)
+        {
+            int c0[3], c1[3];
+            for (int r = 0; r < 3; ++r)
+            {
+                const double ext = world[4 * i + 3] + sphere_radius + margin;
+                c0[r] = std::max(0, (int)std::floor((world[4 * i + r] - ext - lo[r]) * inv[r]) - 1);
+                c1[r] = std::min(G - 1, (int)std::floor((world[4 * i + r] + ext - lo[r]) * inv[r]) + 1);
+            }
+            for (int x = c0[0]; x <= c1[0]; ++x)
+                for (int y = c0[1]; y <= c1[1]; ++y)
+                    for (int z = c0[2]; z <= c1[2]; ++z)
+                        cells[((size_t)x * G + y) * G + z].push_back((int)i);
+        }
+        std::vector<int> start(cells.size() + 1, 0), items;
+        for (size_t k = 0; k < cells.size(); ++k)
+        {
+            start[k + 1] = start[k] + (int)cells[k].size();
+            items.insert(items.end(), cells[k].begin(), cells[k].end());
+        }
+        if (items.empty())
+            items.push_back(0);
+        if (cudaMalloc(&c->cell_start, start.size() * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&c->cell_items, items.size() * sizeof(int)) != cudaSuccess)
+            return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "grid allocation failed"));
+        cudaMemcpy(c->cell_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->cell_items, items.data(), items.size() * sizeof(int), cudaMemcpyHostToDevice);
+        wa.cell_start = c->cell_start;
+        wa.cell_items = c->cell_items;
+        wa.grid_n = G;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cleanup(fail(GBO_ERR_CUDA, cudaGetErrorString(e)));
+    if (cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(GBO_ERR_CUDA, "stream creation failed"));
+    *out = c;
+    return GBO_OK;
+}
+
+gbo_status gbo_checker_destroy(gbo_checker *c)
+{
+    if (c)
+        cudaDeviceSynchronize();
+    delete c;
+    return GBO_OK;
+}
+
+gbo_status gbo_checker_set_precision(gbo_checker *c, int precision)
+{
+    if (!c || (precision != GBO_PRECISION_FP64 && precision != GBO_PRECISION_FP32_GUARDED))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad precision");
+    c->precision = precision;
+    return GBO_OK;
+}
+
+gbo_status gbo_checker_stats(const gbo_checker *c, uint64_t *evaluated, uint64_t *rechecked)
+{
+    if (!c)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "checker is NULL");
+    RunCounters h{};
+    CUDA_TRY(cudaMemcpy(&h, c->ctr.dev + c->ctr.last, sizeof(h), cudaMemcpyDeviceToHost));
+    if (evaluated)
+        *evaluated = h.evaluated;
+    if (rechecked)
+        *rechecked = h.rechecked;
+    if (h.timeout)
+        return fail(GBO_ERR_TIMEOUT, "a device-side wait ran out in the last call");
+    return GBO_OK;
+}
+
+gbo_status gbo_is_valid(gbo_checker *c, const double *states, int64_t n, int64_t ld, int layout, uint8_t *out,
+                        gbo_stream stream)
+{
+    if (!c || n < 0 || (n > 0 && (!states || !out)) || !valid_layout(layout, n, ld, c->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad isValid arguments");
+    if (n == 0)
+        return GBO_OK;
+    LaunchCfg lc = lcfg(stream);
+    RunCounters *ctr = c->ctr.take(lc.stream);
+    launch_validity(lc, c->precision, c->sp, c->wa, make_view(states, ld, layout), n, out, ctr);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+static gbo_status motion_impl(gbo_checker *c, const double *s1, const double *s2, int64_t n, int64_t ld, int layout,
+                              int schedule, uint8_t *ok, int32_t *first_j, int32_t *nd, cudaStream_t stream)
+{
+    LaunchCfg lc = lcfg(stream);
+    RunCounters *ctr = c->ctr.take(lc.stream);
+    launch_motion(lc, c->precision, schedule, c->sp, c->wa, make_view(s1, ld, layout), make_view(s2, ld, layout), n,
+                  ok, first_j, nd, ctr);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_check_motion(gbo_checker *c, const double *s1, const double *s2, int64_t n, int64_t ld, int layout,
+                            int schedule, uint8_t *ok, int32_t *first_j, int32_t *nd, gbo_stream stream)
+{
+    if (!c || n < 0 || (n > 0 && (!s1 || !s2 || !ok)) || !valid_layout(layout, n, ld, c->sp.dim) ||
+        schedule < GBO_SCHEDULE_PLAIN || schedule > GBO_SCHEDULE_AUTO)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad checkMotion arguments");
+    if (n == 0)
+        return GBO_OK;
+    if (schedule == GBO_SCHEDULE_AUTO)
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if (c->tuned_schedule < 0)
+        {
+            // autotune: time both persistent schedules on (a prefix of) this batch
+            const int64_t m = std::min<int64_t>(n, 65536);
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            float best = 1e30f;
+            int pick = GBO_SCHEDULE_TILE;
+            for (int sch : {GBO_SCHEDULE_TILE, GBO_SCHEDULE_WARP})
+            {
+                for (int rep = 0; rep < 2; ++rep)
+                {
+                    cudaEventRecord(e0, (cudaStream_t)stream);
+                    if (auto st = motion_impl(c, s1, s2, m, ld, layout, sch, ok, first_j, nd, (cudaStream_t)stream))
+                        return st;
+                    cudaEventRecord(e1, (cudaStream_t)stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep == 1 && ms < best)
+                    {
+                        best = ms;
+                        pick = sch;
+                    }
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            c->tuned_schedule = pick;
+        }
+        schedule = c->tuned_schedule;
+    }
+    return motion_impl(c, s1, s2, n, ld, layout, schedule, ok, first_j, nd, (cudaStream_t)stream);
+}
+
+gbo_status gbo_last_valid(const gbo_space *s, const double *s1, const double *s2, const int32_t *first_j,
+                          const int32_t *nd, int64_t n, int64_t ld, int layout, double *last_t, double *last_state,
+                          gbo_stream stream)
+{
+    if (!s || n < 0 || (n > 0 && (!s1 || !s2 || !first_j || !nd)) || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad lastValid arguments");
+    StatesView ov = make_view(last_state, ld, layout);
+    launch_last_valid(lcfg(stream), s->sp, make_view(s1, ld, layout), make_view(s2, ld, layout), first_j, nd, n,
+                      last_t, MutStatesView{last_state, ov.si, ov.sd});
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+__global__ void finish_states_chain(const unsigned long long *first, int64_t count, uint8_t *ok, int64_t *fi)
+{
+    const unsigned long long f = *first;
+    const bool good = f >= (unsigned long long)count;
+    *ok = good ? 1 : 0;
+    if (fi)
+        *fi = good ? -1 : (int64_t)f;
+}
+
+gbo_status gbo_check_motion_states(gbo_checker *c, const double *states, int64_t count, int64_t ld, int layout,
+                                   uint8_t *ok, int64_t *first_invalid, gbo_stream stream)
+{
+    if (!c || count < 0 || (count > 0 && !states) || !ok || !valid_layout(layout, count, ld, c->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad checkMotion(states) arguments");
+    LaunchCfg lc = lcfg(stream);
+    RunCounters *ctr = c->ctr.take(lc.stream);
+    unsigned long long *first = &ctr->queue;  // slot's queue word doubles as the running minimum
+    CUDA_TRY(cudaMemsetAsync(first, 0xff, sizeof(unsigned long long), lc.stream));
+    if (count > 0)
+        launch_states_chain(lc, c->sp, c->wa, make_view(states, ld, layout), count, first, ctr);
+    finish_states_chain<<<1, 1, 0, lc.stream>>>(first, count, ok, first_invalid);
+    note_launch();
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, uint8_t *out)
+{
+    if (!c || n < 0 || (n > 0 && (!states || !out)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad isValid arguments");
+    if (n == 0)
+        return GBO_OK;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const size_t bin = (size_t)n * c->sp.dim * sizeof(double);
+    if (auto st = c->pin_in.reserve(bin))
+        return st;
+    if (auto st = c->dev_in.reserve(bin))
+        return st;
+    if (auto st = c->dev_out.reserve((size_t)n))
+        return st;
+    std::memcpy(c->pin_in.p, states, bin);
+    CUDA_TRY(cudaMemcpyAsync(c->dev_in.p, c->pin_in.p, bin, cudaMemcpyHostToDevice, c->host_stream));
+    if (auto st = gbo_is_valid(c, (const double *)c->dev_in.p, n, c->sp.dim, GBO_LAYOUT_AOS, (uint8_t *)c->dev_out.p,
+                               c->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(out, c->dev_out.p, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(c->host_stream));
+    return GBO_OK;
+}
+
+gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double *s2, int64_t n, uint8_t *ok,
+                                 double *last_t, double *last_state)
+{
+    if (!c || n < 0 || (n > 0 && (!s1 || !s2 || !ok)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad checkMotion arguments");
+    if (n == 0)
+        return GBO_OK;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const int dim = c->sp.dim;
+    const size_t bst = (size_t)n * dim * sizeof(double);
+    // device layout: s1 | s2 | first_j | nd | ok | last_t | last_state
+    const size_t off_fj = 2 * bst, off_nd = off_fj + 4 * (size_t)n, off_ok = off_nd + 4 * (size_t)n;
+    const size_t off_lt = pad16(off_ok + (size_t)n), off_ls = off_lt + 8 * (size_t)n, total = off_ls + bst;
+    if (auto st = c->pin_in.reserve(2 * bst))
+        return st;
+    if (auto st = c->dev_in.reserve(total))
+        return st;
+    const size_t out_bytes = (size_t)n + (last_t ? 8 * (size_t)n : 0) + (last_state ? bst : 0);
+    if (auto st = c->pin_out.reserve(out_bytes + 16))
+        return st;
+    std::memcpy(c->pin_in.p, s1, bst);
+    std::memcpy((char *)c->pin_in.p + bst, s2, bst);
+    char *d = (char *)c->dev_in.p;
+    CUDA_TRY(cudaMemcpyAsync(d, c->pin_in.p, 2 * bst, cudaMemcpyHostToDevice, c->host_stream));
+    const int sched = c->precision == GBO_PRECISION_FP64 ? GBO_SCHEDULE_PLAIN : GBO_SCHEDULE_TILE;
+    if (auto st = motion_impl(c, (const double *)d, (const double *)(d + bst), n, dim, GBO_LAYOUT_AOS, sched,
+                              (uint8_t *)(d + off_ok), (int32_t *)(d + off_fj), (int32_t *)(d + off_nd),
+                              c->host_stream))
+        return st;
+    char *po = (char *)c->pin_out.p;
+    CUDA_TRY(cudaMemcpyAsync(po, d + off_ok, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+    size_t pos = (size_t)n;
+    if (last_t || last_state)
+    {
+        StatesView v1 = make_view((const double *)d, dim, GBO_LAYOUT_AOS);
+        StatesView v2 = make_view((const double *)(d + bst), dim, GBO_LAYOUT_AOS);
+        launch_last_valid(lcfg(c->host_stream), c->sp, v1, v2, (const int32_t *)(d + off_fj),
+                          (const int32_t *)(d + off_nd), n, (double *)(d + off_lt),
+                          MutStatesView{last_state ? (double *)(d + off_ls) : nullptr, dim, 1});
+        CHECK_LAUNCH();
+        if (last_t)
+        {
+            CUDA_TRY(cudaMemcpyAsync(po + pos, d + off_lt, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+            pos += 8 * (size_t)n;
+        }
+        if (last_state)
+            CUDA_TRY(cudaMemcpyAsync(po + pos, d + off_ls, bst, cudaMemcpyDeviceToHost, c->host_stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->host_stream));
+    std::memcpy(ok, po, (size_t)n);
+    pos = (size_t)n;
+    if (last_t)
+    {
+        std::memcpy(last_t, po + pos, 8 * (size_t)n);
+        pos += 8 * (size_t)n;
+    }
+    if (last_state)
+        std::memcpy(last_state, po + pos, bst);
+    return GBO_OK;
+}
+
+// ---------------------------------------------------------------- samplers
+gbo_status gbo_sampler_create(const gbo_space *space, uint32_t local_seed, gbo_sampler **out)
+{
+    if (!space || !out)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "space/out is NULL");
+    if (auto st = ensure_device())
+        return st;
+    auto *s = new gbo_sampler();
+    s->sp = space->sp;
+    // mt19937 seeding (std::mersenne_twister_engine::seed): x0 = seed, x_i = f * (x_{i-1} ^ (x_{i-1} >> 30)) + i
+    SamplerState h{};
+    h.mt[0] = local_seed;
+    for (unsigned i = 1; i < 624; ++i)
+        h.mt[i] = 1812433253u * (h.mt[i - 1] ^ (h.mt[i - 1] >> 30)) + i;
+    h.pos = 624;
+    if (cudaMalloc(&s->st, sizeof(SamplerState)) != cudaSuccess)
+    {
+        delete s;
+        return fail(GBO_ERR_OUT_OF_MEMORY, "sampler allocation failed");
+    }
+    cudaMemcpy(s->st, &h, sizeof(h), cudaMemcpyHostToDevice);
+    *out = s;
+    return GBO_OK;
+}
+
+gbo_status gbo_sampler_destroy(gbo_sampler *s)
+{
+    delete s;
+    return GBO_OK;
+}
+
+gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream)
+{
+    if (!s || n < 0 || (n > 0 && !out) || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
+    StatesView ov = make_view(out, ld, layout);
+    launch_sample_uniform(lcfg(stream), s->st, s->sp, nullptr, StatesView{}, 0.0, n, MutStatesView{out, ov.si, ov.sd});
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double distance, int64_t n, int64_t ld,
+                                   int layout, double *out, gbo_stream stream)
+{
+    if (!s || n < 0 || (n > 0 && (!out || !near)) || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniformNear arguments");
+    StatesView ov = make_view(out, ld, layout);
+    launch_sample_uniform(lcfg(stream), s->st, s->sp, near, make_view(near, ld, layout), distance, n,
+                          MutStatesView{out, ov.si, ov.sd});
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+// ---------------------------------------------------------------- nearest neighbours
+gbo_status gbo_nn_create(const gbo_space *space, int64_t capacity, gbo_nn **out)
+{
+    if (!space || !out || capacity < 1)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nn arguments");
+    if (auto st = ensure_device())
+        return st;
+    auto *nn = new gbo_nn();
+    nn->sp = space->sp;
+    nn->cap = capacity;
+    nn->F = space->sp.kind == GBO_SPACE_KINEMATIC_CHAIN ? 2 * space->sp.dim : space->sp.dim;
+    nn->eps32 = space->sp.kind == GBO_SPACE_KINEMATIC_CHAIN ? chain_knn_eps(space->sp) : box_knn_eps(space->sp);
+    if (cudaMalloc(&nn->pts64, sizeof(double) * space->sp.dim * capacity) != cudaSuccess ||
+        cudaMalloc(&nn->feat32, sizeof(float) * nn->F * capacity) != cudaSuccess ||
+        cudaMalloc(&nn->alive, capacity) != cudaSuccess || nn->ctr.init() != GBO_OK)
+    {
+        delete nn;
+        return fail(GBO_ERR_OUT_OF_MEMORY, "nearest-neighbour index allocation failed");
+    }
+    cudaMemset(nn->alive, 0, capacity);
+    *out = nn;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_destroy(gbo_nn *nn)
+{
+    if (nn)
+        cudaDeviceSynchronize();
+    delete nn;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_set_precision(gbo_nn *nn, int precision)
+{
+    if (!nn || (precision != GBO_PRECISION_FP64 && precision != GBO_PRECISION_FP32_GUARDED))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad precision");
+    nn->precision = precision;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_add(gbo_nn *nn, const double *states, int64_t n, int64_t ld, int layout, int64_t *first_key,
+                      gbo_stream stream)
+{
+    if (!nn || n < 0 || (n > 0 && !states) || !valid_layout(layout, n, ld, nn->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad add arguments");
+    if (nn->size + n > nn->cap)
+        return fail(GBO_ERR_OUT_OF_MEMORY, "nearest-neighbour index capacity exceeded");
+    if (first_key)
+        *first_key = nn->size;
+    LaunchCfg lc = lcfg(stream);
+    StatesView v = make_view(states, ld, layout);
+    launch_store_points(lc, v, n, nn->sp.dim, nn->pts64, nn->cap, nn->size, nn->alive);
+    // features of the new elements, written at column offset `size` of the [F][cap] array
+    launch_features(lc, nn->sp, v, n, nn->feat32 + nn->size, nn->cap);
+    CHECK_LAUNCH();
+    nn->size += n;
+    nn->alive_count += n;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_remove(gbo_nn *nn, const int64_t *keys, int64_t n, gbo_stream stream)
+{
+    if (!nn || n < 0 || (n > 0 && !keys))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad remove arguments");
+    launch_remove(lcfg(stream), keys, n, nn->size, nn->alive);
+    CHECK_LAUNCH();
+    nn->alive_count = -1;  // recounted on demand
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_clear(gbo_nn *nn)
+{
+    if (!nn)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "nn is NULL");
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemset(nn->alive, 0, nn->cap));
+    nn->size = 0;
+    nn->alive_count = 0;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_size(const gbo_nn *nn, int64_t *size)
+{
+    if (!nn || !size)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad size arguments");
+    auto *m = const_cast<gbo_nn *>(nn);
+    if (m->alive_count < 0)
+    {
+        std::vector<unsigned char> h(m->size);
+        CUDA_TRY(cudaDeviceSynchronize());
+        if (m->size)
+            CUDA_TRY(cudaMemcpy(h.data(), m->alive, m->size, cudaMemcpyDeviceToHost));
+        int64_t c = 0;
+        for (auto x : h)
+            c += x;
+        m->alive_count = c;
+    }
+    *size = m->alive_count;
+    return GBO_OK;
+}
+
+static NNArgs nn_args(const gbo_nn *nn)
+{
+    NNArgs a;
+    a.pts64 = nn->pts64;
+    a.feat32 = nn->feat32;
+    a.alive = nn->alive;
+    a.cap = nn->cap;
+    a.size = nn->size;
+    a.eps32 = nn->eps32;
+    return a;
+}
+
+gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
+                            const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream)
+{
+    if (!nn || nq < 0 || k < 1 || (nq > 0 && (!q || !idx)) || !valid_layout(layout, nq, ld, nn->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestK arguments");
+    if (k > 64)
+        return fail(GBO_ERR_UNSUPPORTED, "nearestK supports k <= 64");
+    if (nq == 0)
+        return GBO_OK;
+    LaunchCfg lc = lcfg(stream);
+    NNArgs a = nn_args(nn);
+    StatesView qv = make_view(q, ld, layout);
+    RunCounters *ctr = nn->ctr.take(lc.stream);
+    nn->queries += nq;
+    if (nn->precision == GBO_PRECISION_FP32_GUARDED && k <= 20)
+    {
+        if (auto st = nn->qfeat.reserve(sizeof(float) * nn->F * nq))
+            return st;
+        if (auto st = nn->fb_list.reserve(sizeof(unsigned long long) * nq))
+            return st;
+        unsigned long long *fb_n = &ctr->queue;
+        launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
+        if (launch_knn_fp32(lc, a, nn->sp, qv, (const float *)nn->qfeat.p, nq, k, prefix, idx, dist,
+                            (unsigned long long *)nn->fb_list.p, fb_n, ctr))
+        {
+            // queries whose FP32 band overflowed: exact FP64 scan (count read on the device)
+            launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist, (const unsigned long long *)nn->fb_list.p,
+                             fb_n, std::min<int64_t>(nq, 4096));
+            CHECK_LAUNCH();
+            return GBO_OK;
+        }
+    }
+    launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist, nullptr, nullptr, nq);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_nearest_r_count(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
+                                  int64_t *counts, gbo_stream stream)
+{
+    if (!nn || nq < 0 || (nq > 0 && (!q || !counts)) || !valid_layout(layout, nq, ld, nn->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestR arguments");
+    launch_radius(lcfg(stream), nn_args(nn), nn->sp, make_view(q, ld, layout), nq, r, counts, nullptr, nullptr,
+                  nullptr);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
+                                 const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream)
+{
+    if (!nn || nq < 0 || (nq > 0 && (!q || !offsets || !idx || !dist)) || !valid_layout(layout, nq, ld, nn->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestR arguments");
+    launch_radius(lcfg(stream), nn_args(nn), nn->sp, make_view(q, ld, layout), nq, r, nullptr, offsets, idx, dist);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks)
+{
+    if (!nn)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "nn is NULL");
+    RunCounters h{};
+    CUDA_TRY(cudaMemcpy(&h, nn->ctr.dev + nn->ctr.last, sizeof(h), cudaMemcpyDeviceToHost));
+    if (queries)
+        *queries = nn->queries;
+    if (rechecked)
+        *rechecked = h.rechecked;
+    if (fallbacks)
+        *fallbacks = h.fallbacks;
+    return GBO_OK;
+}
+
+gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream)
+{
+    if (!flops)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "flops is NULL");
+    if (auto st = ensure_device())
+        return st;
+    *flops = measure_fp32_peak(lcfg(stream));
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+}  // extern "C"

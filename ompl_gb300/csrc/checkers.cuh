@@ -1,0 +1,244 @@
+// Validity predicates on the device.
+//
+// FP64 forms reproduce the reference's arithmetic operation for operation (exact _rn intrinsics):
+//   circles          tests/resources/circles2D.h:141-151
+//   kinematic chain  demos/KinematicChain.h:209-276
+//   DH sphere arm    the arm definition shared with the oracle (no OMPL counterpart)
+//
+// FP32_GUARDED forms evaluate every comparison in FP32 together with a bound E on
+// |value_fp32 - value_fp64_reference| and classify it as definitely-true, definitely-false or
+// ambiguous (|value - threshold| <= E). A state whose outcome depends on an ambiguous comparison is
+// re-evaluated with the FP64 form, so the returned boolean always equals the FP64 one.
+#pragma once
+#include "common.cuh"
+
+namespace gbo
+{
+
+enum : int
+{
+    kInvalid = 0,
+    kValid = 1,
+    kAmbiguous = 2
+};
+
+// ---------------------------------------------------------------- circles (FP64)
+// world layout in memory: n rows of (x, y, r*r) doubles (r*r formed in FP64 on the host, as circles2D.h:51).
+__device__ __forceinline__ bool circles_valid64(const double *w, int n, double x, double y)
+{
+    for (int i = 0; i < n; ++i)
+    {
+        double dx = dsub(w[3 * i + 0], x);
+        double dy = dsub(w[3 * i + 1], y);
+        if (dadd(dmul(dx, dx), dmul(dy, dy)) < w[3 * i + 2])
+            return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- kinematic chain (FP64)
+// Segment intersection of demos/KinematicChain.h:251-276.
+__device__ __forceinline__ bool seg_intersect64(double ax0, double ay0, double ax1, double ay1, double bx0, double by0,
+                                                double bx1, double by1)
+{
+    double s10_x = dsub(ax1, ax0);
+    double s10_y = dsub(ay1, ay0);
+    double s32_x = dsub(bx1, bx0);
+    double s32_y = dsub(by1, by0);
+    double denom = dsub(dmul(s10_x, s32_y), dmul(s32_x, s10_y));
+    if (fabs(denom) < kDblEps)
+        return false;
+    bool denomPositive = denom > 0;
+    double s02_x = dsub(ax0, bx0);
+    double s02_y = dsub(ay0, by0);
+    double s_numer = dsub(dmul(s10_x, s02_y), dmul(s10_y, s02_x));
+    if ((s_numer < kFltEps) == denomPositive)
+        return false;
+    double t_numer = dsub(dmul(s32_x, s02_y), dmul(s32_y, s02_x));
+    if ((t_numer < kFltEps) == denomPositive)
+        return false;
+    if (((dsub(s_numer, denom) > -kFltEps) == denomPositive) || ((dsub(t_numer, denom) > kFltEps) == denomPositive))
+        return false;
+    return true;
+}
+
+// Adjacent chain segments (i, i+1) share an endpoint, so in FP64 s02 == -s10 exactly, s_numer == +0 and
+// t_numer == denom bitwise; every branch of the test above then reports "no collision". Both forms
+// therefore skip adjacent pairs without changing any result.
+
+// FK of demos/KinematicChain.h:214-228 into n+2 points (n links plus the 0.001 tip segment).
+template <int MAXD>
+__device__ __forceinline__ void chain_points64(const SpaceParams &s, const double *q, double *X, double *Y)
+{
+    double theta = 0., x = 0., y = 0., c = 1.0, sn = 0.0;
+    X[0] = 0.;
+    Y[0] = 0.;
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i)
+        if (i < s.dim)
+        {
+            theta = dadd(theta, q[i]);
+            sincos(theta, &sn, &c);
+            x = dadd(x, dmul(c, s.link));
+            y = dadd(y, dmul(sn, s.link));
+            X[i + 1] = x;
+            Y[i + 1] = y;
+        }
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i)
+        if (i == s.dim)
+        {
+            X[i + 1] = dadd(x, dmul(c, 0.001));
+            Y[i + 1] = dadd(y, dmul(sn, 0.001));
+        }
+}
+
+// world: n rows of (x0, y0, x1, y1) doubles.
+template <int MAXD>
+__device__ bool chain_valid64(const SpaceParams &s, const double *q, const double *w, int nw)
+{
+    double X[MAXD + 2], Y[MAXD + 2];
+    chain_points64<MAXD>(s, q, X, Y);
+    const int m = s.dim + 1;  // segments
+#pragma unroll
+    for (int i = 0; i < MAXD + 1; ++i)
+#pragma unroll
+        for (int j = i + 2; j < MAXD + 1; ++j)
+            if (j < m)
+                if (seg_intersect64(X[i], Y[i], X[i + 1], Y[i + 1], X[j], Y[j], X[j + 1], Y[j + 1]))
+                    return false;
+#pragma unroll
+    for (int i = 0; i < MAXD + 1; ++i)
+        if (i < m)
+            for (int j = 0; j < nw; ++j)
+                if (seg_intersect64(X[i], Y[i], X[i + 1], Y[i + 1], w[4 * j], w[4 * j + 1], w[4 * j + 2],
+                                    w[4 * j + 3]))
+                    return false;
+    return true;
+}
+
+// ---------------------------------------------------------------- kinematic chain (FP32, guarded)
+// Per world segment, FP32 data plus its error bounds (filled by the host, see chain_bounds in capi.cu):
+//   x0, y0, sx, sy  : start point and direction vector (s32) rounded to FP32
+//   e_den, e_s, e_t : bounds on |fp32 - fp64| of denom, s_numer and t_numer for a link vs this segment
+//   e_u, e_v        : bounds for s_numer - denom and t_numer - denom
+struct ChainSegF32
+{
+    float x0, y0, sx, sy, e_den, e_s, e_t, e_u, e_v, pad0, pad1, pad2;
+};
+
+struct ChainGuard
+{
+    float eps_dir;   // bound on |cos/sin fp32 - fp64| of one link direction
+    float self_den, self_s, self_t, self_u, self_v;  // bounds for link-vs-link tests
+};
+
+// 3-valued "x < thr" with |x - x_ref| <= e: returns 1 (true), 0 (false), 2 (ambiguous).
+__device__ __forceinline__ int lt3(float x, float thr, float e)
+{
+    return x < thr - e ? 1 : (x >= thr + e ? 0 : 2);
+}
+__device__ __forceinline__ int gt3(float x, float thr, float e)
+{
+    return x > thr + e ? 1 : (x <= thr - e ? 0 : 2);
+}
+
+// Guarded segment test: returns kInvalid (definite collision), kValid (definite none) or kAmbiguous.
+__device__ __forceinline__ int seg_intersect32(float s10x, float s10y, float s32x, float s32y, float s02x, float s02y,
+                                               float e_den, float e_s, float e_t, float e_u, float e_v)
+{
+    constexpr float kFlt = 1.1920928955078125e-07f;
+    float den = fmaf(s10x, s32y, -s32x * s10y);
+    if (fabsf(den) <= e_den)
+        return kAmbiguous;  // collinearity / sign of denom not decided in FP32
+    const bool P = den > 0.f;
+    // each clause of demos/KinematicChain.h:267-274 is "(cmp) == denomPositive => no collision"
+    float sn = fmaf(s10x, s02y, -s10y * s02x);
+    int S = lt3(sn, kFlt, e_s);
+    if (S != 2 && (S == 1) == P)
+        return kValid;
+    float tn = fmaf(s32x, s02y, -s32y * s02x);
+    int T = lt3(tn, kFlt, e_t);
+    if (T != 2 && (T == 1) == P)
+        return kValid;
+    int U = gt3(sn - den, -kFlt, e_u);
+    if (U != 2 && (U == 1) == P)
+        return kValid;
+    int V = gt3(tn - den, kFlt, e_v);
+    if (V != 2 && (V == 1) == P)
+        return kValid;
+    return (S == 2 || T == 2 || U == 2 || V == 2) ? kAmbiguous : kInvalid;
+}
+
+// FP32 link directions: theta accumulated in FP64 exactly as the reference, reduced to [-pi, pi]
+// and evaluated with FP32 sincos. |error| <= guard.eps_dir per component.
+__device__ __forceinline__ void dir32(double theta, float &c, float &s)
+{
+    double k = rint(theta * (1.0 / kTwoPi));
+    double r = fma(-k, kTwoPi, theta);
+    sincosf((float)r, &s, &c);
+}
+
+template <int MAXD>
+__device__ int chain_valid32(const SpaceParams &s, const double *q, const ChainSegF32 *w, int nw, const ChainGuard &g)
+{
+    float X[MAXD + 2], Y[MAXD + 2], VX[MAXD + 1], VY[MAXD + 1];
+    const float L = (float)s.link;
+    double theta = 0.;
+    float x = 0.f, y = 0.f, c = 1.f, sn = 0.f;
+    X[0] = 0.f;
+    Y[0] = 0.f;
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i)
+        if (i < s.dim)
+        {
+            theta = dadd(theta, q[i]);
+            dir32(theta, c, sn);
+            VX[i] = c * L;
+            VY[i] = sn * L;
+            x = fmaf(c, L, x);
+            y = fmaf(sn, L, y);
+            X[i + 1] = x;
+            Y[i + 1] = y;
+        }
+#pragma unroll
+    for (int i = 0; i < MAXD; ++i)
+        if (i == s.dim)
+        {
+            VX[i] = c * 0.001f;
+            VY[i] = sn * 0.001f;
+            X[i + 1] = fmaf(c, 0.001f, x);
+            Y[i + 1] = fmaf(sn, 0.001f, y);
+        }
+    const int m = s.dim + 1;
+    bool amb = false;
+#pragma unroll
+    for (int i = 0; i < MAXD + 1; ++i)
+#pragma unroll
+        for (int j = i + 2; j < MAXD + 1; ++j)
+            if (j < m)
+            {
+                int r = seg_intersect32(VX[i], VY[i], VX[j], VY[j], X[i] - X[j], Y[i] - Y[j], g.self_den, g.self_s,
+                                        g.self_t, g.self_u, g.self_v);
+                if (r == kInvalid)
+                    return kInvalid;
+                amb |= (r == kAmbiguous);
+            }
+    for (int j = 0; j < nw; ++j)
+    {
+        const ChainSegF32 ws = w[j];
+#pragma unroll
+        for (int i = 0; i < MAXD + 1; ++i)
+            if (i < m)
+            {
+                int r = seg_intersect32(VX[i], VY[i], ws.sx, ws.sy, X[i] - ws.x0, Y[i] - ws.y0, ws.e_den, ws.e_s,
+                                        ws.e_t, ws.e_u, ws.e_v);
+                if (r == kInvalid)
+                    return kInvalid;
+                amb |= (r == kAmbiguous);
+            }
+    }
+    return amb ? kAmbiguous : kValid;
+}
+
+}  // namespace gbo

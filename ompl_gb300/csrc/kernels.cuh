@@ -1,0 +1,216 @@
+// Kernel-side argument structures and the launcher interface between the C ABI (capi.cu) and the
+// kernel translation units.
+#pragma once
+#include "common.cuh"
+#include "checkers.cuh"
+
+namespace gbo
+{
+
+struct RunCounters
+{
+    unsigned long long queue;      // work-queue head of persistent kernels (reset before each launch)
+    unsigned long long evaluated;  // states evaluated
+    unsigned long long rechecked;  // states (or segment counts / kNN queries) re-evaluated in FP64
+    unsigned long long fallbacks;  // kNN queries answered by the exact FP64 scan
+    unsigned int timeout;          // a bounded wait ran out
+    unsigned int error;
+};
+
+struct DHArm
+{
+    int joints;
+    int spl;          // spheres per link
+    double rs;        // robot sphere radius
+    double a[8], d[8];
+    float ca[8], sa[8];  // cos/sin of alpha (exactly 0 or +-1)
+    float af[8], dfl[8];
+};
+
+struct WorldArgs
+{
+    int kind;
+    int n;
+    const void *data64;   // FP64 rows (circles x,y,r*r | segments x0,y0,x1,y1 | spheres x,y,z,r)
+    unsigned bytes64;     // padded to 16 bytes
+    int stage64;          // stage data64 into shared memory
+    const void *data32;   // FP32 rows (ChainSegF32 | float4 spheres)
+    unsigned bytes32;
+    int stage32;
+    ChainGuard guard;
+    float e_dist;         // bound on |fp32 - fp64| of the chain workspace distance
+    float inv_lvs32;      // 1 / longest valid segment, FP32
+    DHArm arm;
+    // uniform grid over the world spheres (cells hold spheres whose box grown by rs + margin overlaps)
+    const int *cell_start;
+    const int *cell_items;
+    int grid_n;
+    float glo[3], ginv[3];
+    double glo64[3], ginv64[3];
+    float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere test near contact
+};
+
+struct LaunchCfg
+{
+    cudaStream_t stream;
+    int sm_count;
+};
+
+int persistent_grid(const void *kernel, int block, unsigned smem, const LaunchCfg &lc, int64_t max_blocks);
+unsigned world_smem_bytes(const WorldArgs &wa, int precision);
+void note_launch();
+
+void launch_validity(const LaunchCfg &lc, int precision, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
+                     int64_t n, uint8_t *out, RunCounters *ctr);
+void launch_motion(const LaunchCfg &lc, int precision, int schedule, const SpaceParams &sp, const WorldArgs &wa,
+                   StatesView v1, StatesView v2, int64_t n, uint8_t *ok, int32_t *fj, int32_t *nd, RunCounters *ctr);
+void launch_states_chain(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v, int64_t n,
+                         unsigned long long *first, RunCounters *ctr);
+void launch_last_valid(const LaunchCfg &lc, const SpaceParams &sp, StatesView v1, StatesView v2, const int32_t *fj,
+                       const int32_t *nd, int64_t n, double *last_t, MutStatesView out);
+void launch_distance(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, int64_t n, double *out);
+void launch_interpolate(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, const double *t,
+                        int64_t n, MutStatesView out);
+
+// ---------------------------------------------------------------- DH sphere arm
+// FP64 form: the arm definition (sphere centres in the exact operation order of the oracle's
+// definition), candidates from the uniform grid (a superset of every colliding sphere), exact test.
+template <int MAXD>
+__device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, const WorldArgs &wa)
+{
+    double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double p[3] = {0, 0, 0};
+    const int G = wa.grid_n;
+#pragma unroll 1
+    for (int i = 0; i < arm.joints; ++i)
+    {
+        double cq, sq;
+        sincos(q[i], &sq, &cq);
+        const double ca = (double)arm.ca[i], sa = (double)arm.sa[i];
+        const double A[3][3] = {{cq, dmul(-sq, ca), dmul(sq, sa)}, {sq, dmul(cq, ca), dmul(-cq, sa)}, {0.0, sa, ca}};
+        const double pA[3] = {dmul(arm.a[i], cq), dmul(arm.a[i], sq), arm.d[i]};
+        double Rn[3][3], pn[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                Rn[r][k] = dadd(dadd(dmul(R[r][0], A[0][k]), dmul(R[r][1], A[1][k])), dmul(R[r][2], A[2][k]));
+            pn[r] = dadd(dadd(dadd(dmul(R[r][0], pA[0]), dmul(R[r][1], pA[1])), dmul(R[r][2], pA[2])), p[r]);
+        }
+#pragma unroll 1
+        for (int k = 0; k < arm.spl; ++k)
+        {
+            const double f = ddiv(dadd((double)k, 0.5), (double)arm.spl);
+            double c[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                c[r] = dadd(p[r], dmul(f, dsub(pn[r], p[r])));
+            int cell[3];
+            bool inside = true;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+            {
+                double g = floor((c[r] - wa.glo64[r]) * wa.ginv64[r]);
+                inside &= (g >= 0.0 && g < (double)G);
+                cell[r] = (int)g;
+            }
+            if (!inside)
+                continue;
+            const int cid = (cell[0] * G + cell[1]) * G + cell[2];
+            const int b = wa.cell_start[cid], e = wa.cell_start[cid + 1];
+            for (int it = b; it < e; ++it)
+            {
+                const double *o = w + 4 * wa.cell_items[it];
+                double dx = dsub(c[0], o[0]);
+                double dy = dsub(c[1], o[1]);
+                double dz = dsub(c[2], o[2]);
+                double rr = dadd(arm.rs, o[3]);
+                if (dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < dmul(rr, rr))
+                    return false;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+            p[r] = pn[r];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                R[r][k] = Rn[r][k];
+        }
+    }
+    return true;
+}
+
+// FP32 form: FK, centres and the narrow phase in FP32; a pair whose d^2 - (rs+ro)^2 lies within
+// +-dh_e is ambiguous (dh_e bounds the FP32 error of that difference near contact).
+template <int MAXD>
+__device__ int dh_valid32(const DHArm &arm, const double *q, const float4 *sph, const WorldArgs &wa)
+{
+    float R[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+    float p[3] = {0.f, 0.f, 0.f};
+    const int G = wa.grid_n;
+    const float rs = (float)arm.rs, E = wa.dh_e;
+    const float inv_spl = 1.0f / (float)arm.spl;
+    bool amb = false;
+#pragma unroll 1
+    for (int i = 0; i < arm.joints; ++i)
+    {
+        float cq, sq;
+        sincosf((float)q[i], &sq, &cq);
+        const float ca = arm.ca[i], sa = arm.sa[i];
+        const float A[3][3] = {{cq, -sq * ca, sq * sa}, {sq, cq * ca, -cq * sa}, {0.f, sa, ca}};
+        const float pA[3] = {arm.af[i] * cq, arm.af[i] * sq, arm.dfl[i]};
+        float Rn[3][3], pn[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                Rn[r][k] = fmaf(R[r][2], A[2][k], fmaf(R[r][1], A[1][k], R[r][0] * A[0][k]));
+            pn[r] = fmaf(R[r][2], pA[2], fmaf(R[r][1], pA[1], fmaf(R[r][0], pA[0], p[r])));
+        }
+#pragma unroll 1
+        for (int k = 0; k < arm.spl; ++k)
+        {
+            const float f = ((float)k + 0.5f) * inv_spl;
+            float c[3];
+            int cell[3];
+            bool inside = true;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+            {
+                c[r] = fmaf(f, pn[r] - p[r], p[r]);
+                float g = floorf((c[r] - wa.glo[r]) * wa.ginv[r]);
+                inside &= (g >= 0.f && g < (float)G);
+                cell[r] = (int)g;
+            }
+            if (!inside)
+                continue;
+            const int cid = (cell[0] * G + cell[1]) * G + cell[2];
+            const int b = __ldg(wa.cell_start + cid), e = __ldg(wa.cell_start + cid + 1);
+            for (int it = b; it < e; ++it)
+            {
+                const int oi = __ldg(wa.cell_items + it);
+                const float4 o = wa.stage32 ? sph[oi] : __ldg(sph + oi);
+                const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
+                const float rr = rs + o.w;
+                const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
+                if (t < -E)
+                    return kInvalid;
+                amb |= (t <= E);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+            p[r] = pn[r];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                R[r][k] = Rn[r][k];
+        }
+    }
+    return amb ? kAmbiguous : kValid;
+}
+
+}  // namespace gbo

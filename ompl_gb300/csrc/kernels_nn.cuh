@@ -1,0 +1,42 @@
+// Device-resident nearest-neighbour index arguments and launchers.
+#pragma once
+#include "kernels.cuh"
+
+namespace gbo
+{
+
+struct NNArgs
+{
+    const double *pts64;        // SoA FP64 elements [dim][cap]
+    const float *feat32;        // SoA FP32 features [F][cap]
+    const unsigned char *alive; // 1 = present, 0 = removed (tombstone)
+    int64_t cap;
+    int64_t size;               // keys handed out so far (removed ones included)
+    float eps32;                // bound on |distance_fp32 - distance_fp64|
+};
+
+void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, int64_t nq, int k,
+                      const int64_t *prefix, int64_t *idx, double *dist, const unsigned long long *list,
+                      const unsigned long long *list_n, int64_t max_items);
+bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
+                     int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
+                     unsigned long long *fb_n, RunCounters *ctr);
+void launch_features(const LaunchCfg &lc, const SpaceParams &sp, StatesView v, int64_t n, float *out, int64_t ld_out);
+void launch_store_points(const LaunchCfg &lc, StatesView v, int64_t n, int dim, double *pts, int64_t cap,
+                         int64_t first, unsigned char *alive);
+void launch_remove(const LaunchCfg &lc, const int64_t *keys, int64_t n, int64_t size, unsigned char *alive);
+void launch_radius(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, int64_t nq, double r,
+                   int64_t *counts, const int64_t *offsets, int64_t *idx, double *dist);
+
+// sampler
+struct SamplerState
+{
+    unsigned int mt[624];
+    unsigned int pos;     // next word index in mt (624 = twist needed)
+    unsigned int pad[3];
+};
+void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
+                           StatesView nearv, double distance, int64_t n, MutStatesView out);
+double measure_fp32_peak(const LaunchCfg &lc);
+
+}  // namespace gbo

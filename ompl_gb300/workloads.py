@@ -12,8 +12,8 @@ Workloads (index = configuration number):
      endpoints U[-1,1]^2, 1M states, 100k edges at segment fraction 0.005, kNN k=16 over the 1M
      states for 100k queries drawn from the set.
   2  7-DoF DH arm (a, d ~ U(0,0.4), alpha in {0, +pi/2, -pi/2}), 8 spheres of radius 0.05 per link,
-     4,096 world spheres (centre U[-1,1]^3, r U(0.02,0.1)), 256k edges whose lengths give
-     log-uniform 2..2000 interpolation steps.
+     4,096 world spheres (centre uniform in [-1,1]^3 outside a 0.8 m ball around the base,
+     r U(0.02,0.1)), 256k edges whose lengths give log-uniform 2..2000 interpolation steps.
   3  serving: per-client worlds of 1,024..8,192 spheres with the workload-2 arm.
   4  PRM roadmap for the workload-2 arm among 16,384 spheres in the wrap-L2 joint space.
 """
@@ -68,10 +68,19 @@ def dh_arm(rng, joints=7):
     return np.ascontiguousarray(np.stack([a, d, code], axis=1))
 
 
-def sphere_world(rng, n, rmin=0.02, rmax=0.1):
-    c = rng.uniform(-1.0, 1.0, size=(n, 3))
+FREE_RADIUS = 0.8
+
+
+def sphere_world(rng, n, rmin=0.02, rmax=0.1, free_radius=FREE_RADIUS):
+    """n spheres, centres uniform in [-1,1]^3 outside a ball of radius `free_radius` around the arm
+    base, radii U(rmin, rmax). With the whole cube filled no arm state is collision-free (0 of 400
+    sampled states for 1,024..16,384 spheres); the empty ball leaves 30-36% of states valid."""
+    out = np.empty((0, 3))
+    while out.shape[0] < n:
+        c = rng.uniform(-1.0, 1.0, size=(2 * n, 3))
+        out = np.vstack([out, c[np.linalg.norm(c, axis=1) >= free_radius]])
     r = rng.uniform(rmin, rmax, size=(n, 1))
-    return np.ascontiguousarray(np.hstack([c, r]))
+    return np.ascontiguousarray(np.hstack([out[:n], r]))
 
 
 def random_pairs(rng, states, n_edges):

@@ -1,0 +1,280 @@
+"""GPU parity: libgbompl.so through its C ABI against OMPL's own outputs (golden fixtures) and the
+oracle on seeded inputs. Booleans, first-invalid indices, segment counts, samples, and kNN index
+sets must match exactly; FP64 values are compared bitwise except where the kinematic-chain space
+evaluates sin/cos (CUDA's FP64 sin/cos vs glibc's may differ in the last bit; tolerance 4 ulp)."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import checker_of, same_bits, space_of
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from ompl_gb300 import base as B  # noqa: E402
+from ompl_gb300 import capi  # noqa: E402
+from ompl_gb300 import workloads as W  # noqa: E402
+from oracle.oracle import CheckerDesc, SpaceDesc  # noqa: E402
+
+SCHEDULES = [capi.SCHEDULE_PLAIN, capi.SCHEDULE_TILE, capi.SCHEDULE_WARP]
+
+
+def gpu_space(g_or_desc):
+    d = g_or_desc if isinstance(g_or_desc, SpaceDesc) else space_of(g_or_desc)
+    if d.kind == capi.SPACE_REAL_VECTOR:
+        s = B.RealVectorStateSpace(d.dim, d.low, d.high)
+    elif d.kind == capi.SPACE_SO2:
+        s = B.SO2StateSpace()
+    elif d.kind == capi.SPACE_KINEMATIC_CHAIN:
+        s = B.KinematicChainSpace(d.dim, d.link_length)
+    else:
+        s = B.WrapL2StateSpace(d.dim)
+    s.setLongestValidSegmentFraction(d.lvs_fraction)
+    s.setValidSegmentCountFactor(d.factor)
+    return s
+
+
+def gpu_checker(space, ck: CheckerDesc):
+    if ck.kind == capi.CHECK_CIRCLES:
+        return B.CirclesValidityChecker(space, ck.obstacles)
+    if ck.kind == capi.CHECK_CHAIN_SEGMENTS:
+        return B.KinematicChainValidityChecker(space, ck.obstacles)
+    if ck.kind == capi.CHECK_DH_SPHERES:
+        return B.DHSphereArmValidityChecker(space, ck.dh, ck.obstacles, ck.spheres_per_link, ck.sphere_radius)
+    return B.AllValidStateValidityChecker(space)
+
+
+def ulp_close(a, b, ulps=4):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    diff = np.abs(a - b)
+    tol = ulps * np.spacing(np.maximum(np.abs(a), np.abs(b)))
+    return bool(np.all(both_nan | (diff <= tol) | (a == b)))
+
+
+# ------------------------------------------------------------------ spaces and samplers
+@pytest.mark.parametrize("name", ["rv2", "rv7", "so2", "chain10", "wrap7"])
+def test_space_distance_interpolate_vs_ompl(golden, name):
+    g = golden(f"space_{name}")
+    s = gpu_space(g)
+    assert s.getMaximumExtent() == g["extent"] and s.getLongestValidSegmentLength() == g["lvs"]
+    d = s.distance(g["a"], g["b"])
+    it = s.interpolate(g["a"], g["b"], g["t"])
+    if name == "chain10":
+        assert ulp_close(d, g["distance"])
+    else:
+        assert same_bits(d, g["distance"])
+    assert same_bits(it, g["interpolate"])
+
+
+@pytest.mark.parametrize("name", ["rv2", "rv7", "so2", "chain10", "wrap7"])
+def test_sampler_stream_vs_ompl(golden, name):
+    g = golden(f"space_{name}")
+    s = gpu_space(g)
+    smp = B.StateSampler(s, int(g["sample_seed"]))
+    # the stream continues across calls of odd sizes (word pairs straddle 624-word blocks)
+    parts = [smp.sampleUniform(n) for n in (1, 155, 313, 231)]
+    assert same_bits(np.vstack(parts), g["sample"])
+    near = B.StateSampler(s, 11).sampleUniformNear(g["near"], float(g["near_distance"]))
+    assert same_bits(near, g["sample_near"])
+
+
+def test_sampler_large_stream_vs_oracle(port):
+    d = SpaceDesc(capi.SPACE_REAL_VECTOR, 7, np.full(7, -math.pi), np.full(7, math.pi))
+    s = gpu_space(d)
+    smp = B.StateSampler(s, 4)
+    a = smp.sampleUniform(100_000, soa=True)      # SoA output
+    b = smp.sampleUniform(77_777)
+    ref = port.sample_uniform(d, 4, 177_777)
+    assert same_bits(a.T, ref[:100_000]) and same_bits(b, ref[100_000:])
+
+
+# ------------------------------------------------------------------ validity / motion vs OMPL fixtures
+CASES = ["circles_seeded", "circles_ompl_tests", "chain_seeded", "chain_horn", "dh_arm"]
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("precision", ["fp64", "fp32_guarded"])
+def test_validity_vs_ompl(golden, name, precision):
+    g = golden(name)
+    s = gpu_space(g)
+    ck = gpu_checker(s, checker_of(g))
+    ck.setPrecision(precision)
+    assert np.array_equal(ck.isValid(g["states"]), g["valid"].astype(bool))
+    assert np.array_equal(ck.isValidHost(g["states"]), g["valid"].astype(bool))
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("precision", ["fp64", "fp32_guarded"])
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_discrete_motion_vs_ompl(golden, name, precision, schedule):
+    g = golden(name)
+    s = gpu_space(g)
+    ck = gpu_checker(s, checker_of(g))
+    ck.setPrecision(precision)
+    mv = B.DiscreteMotionValidator(ck)
+    r = mv.checkMotions(g["s1"], g["s2"], schedule=schedule, last_valid=True)
+    assert np.array_equal(r["ok"], g["ok"])
+    assert np.array_equal(r["ok"], g["ok_bisect"])
+    assert np.array_equal(r["nd"], g["nd"])
+    assert np.array_equal(r["first_j"], g["first_j"])
+    assert same_bits(r["last_t"], g["last_t"])
+    assert same_bits(r["last_state"], g["last_state"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_motion_host_dropin_vs_ompl(golden, name):
+    g = golden(name)
+    s = gpu_space(g)
+    ck = gpu_checker(s, checker_of(g))
+    mv = B.DiscreteMotionValidator(ck)
+    ok, lt, ls = mv.checkMotionHost(g["s1"], g["s2"])
+    assert np.array_equal(ok, g["ok"].astype(bool))
+    assert same_bits(lt, g["last_t"]) and same_bits(ls, g["last_state"])
+    # single-edge OMPL-style call
+    lv = [None, 0.0]
+    i = int(np.argmin(g["ok"]))
+    assert mv.checkMotion(g["s1"][i], g["s2"][i], lv) == bool(g["ok"][i])
+    if not g["ok"][i]:
+        assert lv[1] == g["last_t"][i]
+
+
+def test_motion_states_vs_ompl(golden):
+    g = golden("motion_states")
+    s = gpu_space(g)
+    mv = B.DiscreteMotionValidator(gpu_checker(s, checker_of(g)))
+    off = 0
+    for i in range(len(g["count"])):
+        n = int(g["lengths"][i])
+        st = g["states"][off:off + n]
+        off += n
+        if n == 0:
+            continue
+        ok, fi = mv.checkMotionStates(st)
+        assert ok == bool(g["ok"][i])
+        if not ok:
+            assert fi == g["first_invalid"][i]
+
+
+# ------------------------------------------------------------------ larger seeded cases vs the oracle
+@pytest.fixture(scope="module")
+def chain_case(port):
+    w = W.config1(n_states=200_000, n_edges=10, n_queries=10)
+    sp = SpaceDesc(w.space_kind, w.dim, link_length=w.link_length, lvs_fraction=w.lvs_fraction)
+    ck = CheckerDesc(w.checker_kind, w.obstacles)
+    port.set_threads(16)
+    valid = port.is_valid(sp, ck, w.states)
+    return w, sp, ck, valid
+
+
+def test_chain_validity_200k_vs_oracle(chain_case):
+    w, sp, ckd, valid = chain_case
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    for p in ("fp64", "fp32_guarded"):
+        ck.setPrecision(p)
+        got = ck.isValid(torch.as_tensor(w.states.T.copy(), device="cuda"), soa=True).cpu().numpy()
+        assert np.array_equal(got, valid), p
+
+
+def test_chain_motion_valid_endpoints_vs_oracle(chain_case, port):
+    w, sp, ckd, valid = chain_case
+    vs = w.states[valid == 1]
+    rng = np.random.default_rng(3)
+    i, j = rng.integers(0, len(vs), 3000), rng.integers(0, len(vs), 3000)
+    s1, s2 = vs[i], vs[j]
+    ref = port.check_motion(sp, ckd, s1, s2, want_state=False, want_bisect=False)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    mv = B.DiscreteMotionValidator(ck)
+    for p in ("fp64", "fp32_guarded"):
+        ck.setPrecision(p)
+        for sch in SCHEDULES:
+            r = mv.checkMotions(s1, s2, schedule=sch)
+            assert np.array_equal(r["ok"], ref["ok"]) and np.array_equal(r["first_j"], ref["first_j"])
+            assert np.array_equal(r["nd"], ref["nd"])
+
+
+def test_dh_arm_motion_vs_oracle(port):
+    w = W.config2(n_edges=400, n_world=1024)
+    sp = SpaceDesc(w.space_kind, 7, w.low, w.high, lvs_fraction=w.lvs_fraction)
+    ckd = CheckerDesc(w.checker_kind, w.obstacles, dh=w.dh, spheres_per_link=8, sphere_radius=0.05)
+    port.set_threads(16)
+    ref = port.check_motion(sp, ckd, w.s1, w.s2, want_state=False, want_bisect=False)
+    st = np.random.default_rng(9).uniform(-math.pi, math.pi, size=(3000, 7))
+    vref = port.is_valid(sp, ckd, st)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    mv = B.DiscreteMotionValidator(ck)
+    for p in ("fp64", "fp32_guarded"):
+        ck.setPrecision(p)
+        assert np.array_equal(ck.isValid(st), vref.astype(bool)), p
+        for sch in SCHEDULES:
+            r = mv.checkMotions(w.s1, w.s2, schedule=sch)
+            assert np.array_equal(r["ok"], ref["ok"]) and np.array_equal(r["first_j"], ref["first_j"]), (p, sch)
+            assert np.array_equal(r["nd"], ref["nd"])
+
+
+# ------------------------------------------------------------------ nearest neighbours
+@pytest.mark.parametrize("name", ["rv2", "chain10", "wrap7"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_guarded"])
+def test_knn_vs_ompl(golden, name, precision):
+    g = golden(f"knn_{name}")
+    s = gpu_space(g)
+    nn = B.NearestNeighborsGPU(s, capacity=len(g["pts"]) + 10, precision=precision)
+    nn.add(g["pts"])
+    assert nn.size() == len(g["pts"])
+    k = int(g["k"])
+    idx, dist = nn.nearestK(g["q"], k)
+    assert np.array_equal(idx, g["linear_idx"])
+    if name == "chain10":
+        assert ulp_close(dist, g["linear_dist"])
+    else:
+        assert same_bits(dist, g["linear_dist"])
+    pi_, pd_ = nn.nearestK(g["q"], k, prefix=g["prefix_limit"])
+    assert np.array_equal(pi_, g["prefix_idx"])
+    counts, ri, rd = nn.nearestR(g["q"], float(g["r"]))
+    assert np.array_equal(counts, g["radius_counts"]) and np.array_equal(ri, g["radius_idx"])
+
+
+def test_knn_add_remove_pattern_vs_oracle(port):
+    # interleaved add / query / remove like nearestneighbors.cpp:205-280 (randomAccessPatternTest)
+    rng = np.random.default_rng(21)
+    d = SpaceDesc(capi.SPACE_WRAP_L2, 7, lvs_fraction=0.01)
+    s = gpu_space(d)
+    nn = B.NearestNeighborsGPU(s, capacity=5000)
+    pts = rng.uniform(-math.pi, math.pi, size=(4000, 7))
+    alive = np.zeros(4000, dtype=bool)
+    added = 0
+    for step in range(8):
+        n = 500
+        nn.add(pts[added:added + n])
+        alive[added:added + n] = True
+        added += n
+        kill = rng.choice(np.flatnonzero(alive), size=120, replace=False)
+        nn.remove(kill)
+        alive[kill] = False
+        assert nn.size() == alive.sum()
+        q = rng.uniform(-math.pi, math.pi, size=(64, 7))
+        k = int(rng.integers(1, 20))
+        idx, dist = nn.nearestK(q, k)
+        keys = np.flatnonzero(alive)
+        ri, rd = port.knn(d, pts[keys], q, k)
+        assert np.array_equal(idx, keys[ri]) and same_bits(dist, rd)
+
+
+def test_knn_chain_large_vs_oracle(chain_case, port):
+    w, sp, _, _ = chain_case
+    s = gpu_space(sp)
+    nn = B.NearestNeighborsGPU(s, capacity=len(w.states))
+    nn.add(torch.as_tensor(w.states, device="cuda"))
+    q = w.states[np.random.default_rng(2).integers(0, len(w.states), 40)]
+    idx, dist = nn.nearestK(q, 16)
+    ri, rd = port.knn(sp, w.states, q, 16)
+    assert np.array_equal(idx, ri) and ulp_close(dist, rd)
+    assert idx[:, 0].tolist() == [int(np.flatnonzero((w.states == qq).all(1))[0]) for qq in q]
