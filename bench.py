@@ -226,6 +226,19 @@ def ours(args, rank, world, local_rank):
     mean_ms = statistics.mean(step_ms)
     mean_checked = statistics.mean(checked[i % N_BATCHES] for i in range(args.steps))
 
+    # each persistent schedule on its own (the autotuner picks between them)
+    sched_eps = {}
+    for name, sch in (("tile", capi.SCHEDULE_TILE), ("warp", capi.SCHEDULE_WARP)):
+        run(0, sch)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for i in range(N_BATCHES):
+            run(i, sch)
+        a1.record()
+        torch.cuda.synchronize()
+        sched_eps[name] = N_BATCHES * N_EDGES / (a0.elapsed_time(a1) * 1e-3)
+
     # plain one-launch-per-batch FP64 form on the same batches
     checker.setPrecision("fp64")
     run(0, capi.SCHEDULE_PLAIN)
@@ -303,6 +316,7 @@ def ours(args, rank, world, local_rank):
                          "sample": f"{sample} edges of batch 0, oracle restatement, all host threads"},
         "plain_fp64_edges_per_s": plain_eps,
         "batched_vs_plain": value / world / plain_eps,
+        "schedule_edges_per_s": sched_eps,
         "states_per_s": states_per_s,
         "knn_queries_per_s": knn_qps,
         "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},

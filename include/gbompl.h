@@ -161,6 +161,17 @@ gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_
                                  const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream);
 gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks);
 
+/* Host-memory drop-ins for NearestNeighbors<T> (AoS rows; synchronous). nearest_r_host answers one
+ * query: at most `cap` results are written, *count receives the full count. */
+gbo_status gbo_nn_add_host(gbo_nn *nn, const double *states, int64_t n, int64_t *first_key);
+gbo_status gbo_nn_remove_host(gbo_nn *nn, const int64_t *keys, int64_t n);
+gbo_status gbo_nn_nearest_k_host(gbo_nn *nn, const double *q, int64_t nq, int k, int64_t *idx, double *dist);
+gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t cap, int64_t *count, int64_t *idx,
+                                 double *dist);
+/* Host-memory sampling (AoS rows; synchronous). */
+gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out);
+gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out);
+
 /* ---- measurement helper ---- FP32 FMA throughput of this GPU (FLOP/s), for roofline denominators. */
 gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
 /* Number of kernels this library launched since load (for launch accounting). */

@@ -1,0 +1,372 @@
+/*
+ * OMPL plugins backed by libgbompl (include/gbompl.h). Header-only; compile against OMPL's headers
+ * and link libgbompl.so. Each class derives from the OMPL interface it replaces:
+ *
+ *   gbompl::GpuStateValidityChecker   : ompl::base::StateValidityChecker   (StateValidityChecker.h:90-173)
+ *   gbompl::GpuDiscreteMotionValidator: ompl::base::MotionValidator        (MotionValidator.h:64-140),
+ *                                       DiscreteMotionValidator semantics   (DiscreteMotionValidator.cpp:48-145)
+ *   gbompl::GpuStateSampler           : ompl::base::StateSampler           (StateSampler.h:64-108)
+ *   gbompl::GpuNearestNeighbors<T>    : ompl::NearestNeighbors<T>          (NearestNeighbors.h:46-115)
+ *
+ * Single-state virtual calls go through the same batch kernels with n = 1; the batch methods
+ * (isValidBatch, checkMotionBatch, sampleUniformBatch, add(vector)) amortise the launch. Errors are
+ * raised as ompl::Exception, the exception OMPL itself throws for misconfiguration.
+ */
+#pragma once
+
+#include <ompl/base/MotionValidator.h>
+#include <ompl/base/SpaceInformation.h>
+#include <ompl/base/StateSampler.h>
+#include <ompl/base/StateValidityChecker.h>
+#include <ompl/datastructures/NearestNeighbors.h>
+#include <ompl/util/Exception.h>
+
+#include <functional>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbompl.h"
+
+namespace gbompl
+{
+inline void throwIf(gbo_status s, const char *what)
+{
+    if (s != GBO_OK)
+        throw ompl::Exception(std::string("gbompl: ") + what + ": " + gbo_last_error());
+}
+
+/* The GPU objects bound to one OMPL state space: its metric and segment length (read from the OMPL
+ * space, never recomputed) and optionally a world for validity checking. */
+class GpuContext
+{
+public:
+    /* spaceKind: GBO_SPACE_*; param: link length for GBO_SPACE_KINEMATIC_CHAIN. The OMPL space must be
+     * set up (SpaceInformation::setup) so that getLongestValidSegmentLength() is final. */
+    GpuContext(ompl::base::StateSpacePtr space, int spaceKind, double param = 0.0) : ompl_(std::move(space))
+    {
+        dim_ = ompl_->getDimension();
+        std::vector<double> lo(dim_, 0.0), hi(dim_, 0.0);
+        if (spaceKind == GBO_SPACE_REAL_VECTOR)
+        {
+            const auto &b = ompl_->as<ompl::base::RealVectorStateSpace>()->getBounds();
+            lo = b.low;
+            hi = b.high;
+        }
+        throwIf(gbo_space_create(spaceKind, (int)dim_, lo.data(), hi.data(), param,
+                                 ompl_->getLongestValidSegmentLength(), 0.0, ompl_->getValidSegmentCountFactor(),
+                                 &space_),
+                "space");
+    }
+    ~GpuContext()
+    {
+        if (checker_)
+            gbo_checker_destroy(checker_);
+        gbo_space_destroy(space_);
+    }
+    GpuContext(const GpuContext &) = delete;
+    GpuContext &operator=(const GpuContext &) = delete;
+
+    /* world rows: circles (x, y, r), segments (x0, y0, x1, y1) or spheres (x, y, z, r). */
+    void bindWorld(int checkerKind, const std::vector<double> &world, int rowLength, const std::vector<double> &dh = {},
+                   int spheresPerLink = 0, double sphereRadius = 0.0, int precision = GBO_PRECISION_FP32_GUARDED)
+    {
+        if (checker_)
+            gbo_checker_destroy(checker_);
+        checker_ = nullptr;
+        throwIf(gbo_checker_create(space_, checkerKind, world.data(), (int64_t)(world.size() / rowLength),
+                                   dh.empty() ? nullptr : dh.data(), (int)(dh.size() / 3), spheresPerLink,
+                                   sphereRadius, &checker_),
+                "checker");
+        throwIf(gbo_checker_set_precision(checker_, precision), "precision");
+    }
+
+    gbo_space *space() const { return space_; }
+    gbo_checker *checker() const
+    {
+        if (!checker_)
+            throw ompl::Exception("gbompl: no world bound to the GPU context");
+        return checker_;
+    }
+    const ompl::base::StateSpacePtr &omplSpace() const { return ompl_; }
+    unsigned dim() const { return dim_; }
+
+    void toRow(const ompl::base::State *s, double *row) const
+    {
+        auto *st = const_cast<ompl::base::State *>(s);
+        for (unsigned i = 0; i < dim_; ++i)
+            row[i] = *ompl_->getValueAddressAtIndex(st, i);
+    }
+    void fromRow(const double *row, ompl::base::State *s) const
+    {
+        for (unsigned i = 0; i < dim_; ++i)
+            *ompl_->getValueAddressAtIndex(s, i) = row[i];
+    }
+
+private:
+    ompl::base::StateSpacePtr ompl_;
+    unsigned dim_ = 0;
+    gbo_space *space_ = nullptr;
+    gbo_checker *checker_ = nullptr;
+};
+using GpuContextPtr = std::shared_ptr<GpuContext>;
+
+class GpuStateValidityChecker : public ompl::base::StateValidityChecker
+{
+public:
+    GpuStateValidityChecker(const ompl::base::SpaceInformationPtr &si, GpuContextPtr ctx)
+      : ompl::base::StateValidityChecker(si), ctx_(std::move(ctx))
+    {
+    }
+    bool isValid(const ompl::base::State *state) const override
+    {
+        std::vector<double> row(ctx_->dim());
+        ctx_->toRow(state, row.data());
+        uint8_t ok = 0;
+        throwIf(gbo_is_valid_host(ctx_->checker(), row.data(), 1, &ok), "isValid");
+        return ok != 0;
+    }
+    /* Batch form: out[i] = isValid(states[i]). */
+    void isValidBatch(const std::vector<const ompl::base::State *> &states, std::vector<bool> &out) const
+    {
+        const unsigned d = ctx_->dim();
+        std::vector<double> rows(states.size() * d);
+        for (size_t i = 0; i < states.size(); ++i)
+            ctx_->toRow(states[i], rows.data() + i * d);
+        std::vector<uint8_t> ok(states.size());
+        throwIf(gbo_is_valid_host(ctx_->checker(), rows.data(), (int64_t)states.size(), ok.data()), "isValid");
+        out.assign(ok.begin(), ok.end());
+    }
+
+private:
+    GpuContextPtr ctx_;
+};
+
+class GpuDiscreteMotionValidator : public ompl::base::MotionValidator
+{
+public:
+    GpuDiscreteMotionValidator(const ompl::base::SpaceInformationPtr &si, GpuContextPtr ctx)
+      : ompl::base::MotionValidator(si), ctx_(std::move(ctx))
+    {
+    }
+    bool checkMotion(const ompl::base::State *s1, const ompl::base::State *s2) const override
+    {
+        return one(s1, s2, nullptr);
+    }
+    bool checkMotion(const ompl::base::State *s1, const ompl::base::State *s2,
+                     std::pair<ompl::base::State *, double> &lastValid) const override
+    {
+        return one(s1, s2, &lastValid);
+    }
+    /* Batch form over edges (s1[i], s2[i]); lastValidTime[i] as lastValid.second (NaN when valid). */
+    void checkMotionBatch(const std::vector<const ompl::base::State *> &s1,
+                          const std::vector<const ompl::base::State *> &s2, std::vector<bool> &ok,
+                          std::vector<double> *lastValidTime = nullptr) const
+    {
+        const unsigned d = ctx_->dim();
+        const size_t n = s1.size();
+        std::vector<double> a(n * d), b(n * d), lt(n);
+        for (size_t i = 0; i < n; ++i)
+        {
+            ctx_->toRow(s1[i], a.data() + i * d);
+            ctx_->toRow(s2[i], b.data() + i * d);
+        }
+        std::vector<uint8_t> r(n);
+        throwIf(gbo_check_motion_host(ctx_->checker(), a.data(), b.data(), (int64_t)n, r.data(),
+                                      lastValidTime ? lt.data() : nullptr, nullptr),
+                "checkMotion");
+        ok.assign(r.begin(), r.end());
+        std::lock_guard<std::mutex> lk(mu_);
+        for (auto v : r)
+            (v ? valid_ : invalid_)++;
+        if (lastValidTime)
+            *lastValidTime = lt;
+    }
+
+private:
+    bool one(const ompl::base::State *s1, const ompl::base::State *s2,
+             std::pair<ompl::base::State *, double> *lastValid) const
+    {
+        const unsigned d = ctx_->dim();
+        std::vector<double> a(d), b(d), ls(d);
+        ctx_->toRow(s1, a.data());
+        ctx_->toRow(s2, b.data());
+        uint8_t ok = 0;
+        double lt = 0.0;
+        throwIf(gbo_check_motion_host(ctx_->checker(), a.data(), b.data(), 1, &ok, lastValid ? &lt : nullptr,
+                                      lastValid && lastValid->first ? ls.data() : nullptr),
+                "checkMotion");
+        if (!ok && lastValid)
+        {
+            lastValid->second = lt;
+            if (lastValid->first)
+                ctx_->fromRow(ls.data(), lastValid->first);
+        }
+        std::lock_guard<std::mutex> lk(mu_);
+        (ok ? valid_ : invalid_)++;
+        return ok != 0;
+    }
+    GpuContextPtr ctx_;
+    mutable std::mutex mu_;
+};
+
+/* The space's default sampler with its RNG stream on the GPU: the stream of RNG::setLocalSeed(seed)
+ * drawn by RealVectorStateSampler / SO2StateSampler, reproduced value for value. */
+class GpuStateSampler : public ompl::base::StateSampler
+{
+public:
+    GpuStateSampler(const ompl::base::StateSpace *space, GpuContextPtr ctx, uint32_t localSeed)
+      : ompl::base::StateSampler(space), ctx_(std::move(ctx))
+    {
+        throwIf(gbo_sampler_create(ctx_->space(), localSeed, &s_), "sampler");
+    }
+    ~GpuStateSampler() override { gbo_sampler_destroy(s_); }
+    void sampleUniform(ompl::base::State *state) override
+    {
+        std::vector<double> row(ctx_->dim());
+        throwIf(gbo_sample_uniform_host(s_, 1, row.data()), "sampleUniform");
+        ctx_->fromRow(row.data(), state);
+    }
+    void sampleUniformNear(ompl::base::State *state, const ompl::base::State *near, double distance) override
+    {
+        std::vector<double> nr(ctx_->dim()), row(ctx_->dim());
+        ctx_->toRow(near, nr.data());
+        throwIf(gbo_sample_uniform_near_host(s_, nr.data(), distance, 1, row.data()), "sampleUniformNear");
+        ctx_->fromRow(row.data(), state);
+    }
+    void sampleGaussian(ompl::base::State *, const ompl::base::State *, double) override
+    {
+        throw ompl::Exception("gbompl: sampleGaussian is not provided by the GPU sampler");
+    }
+    /* n consecutive sampleUniform draws. */
+    void sampleUniformBatch(std::vector<ompl::base::State *> &states)
+    {
+        const unsigned d = ctx_->dim();
+        std::vector<double> rows(states.size() * d);
+        throwIf(gbo_sample_uniform_host(s_, (int64_t)states.size(), rows.data()), "sampleUniform");
+        for (size_t i = 0; i < states.size(); ++i)
+            ctx_->fromRow(rows.data() + i * d, states[i]);
+    }
+
+private:
+    GpuContextPtr ctx_;
+    gbo_sampler *s_ = nullptr;
+};
+
+/* NearestNeighbors<T> over a device-resident index of the elements' states. `stateOf` maps an element
+ * to its state (e.g. [](Motion *m) { return m->state; }). Results are ordered by (distance, insertion
+ * order). The distance function must be the space's own metric: setDistanceFunction checks it on the
+ * stored elements and throws otherwise. */
+template <typename T>
+class GpuNearestNeighbors : public ompl::NearestNeighbors<T>
+{
+public:
+    GpuNearestNeighbors(GpuContextPtr ctx, std::function<const ompl::base::State *(const T &)> stateOf,
+                        int64_t capacity = 1 << 20)
+      : ctx_(std::move(ctx)), stateOf_(std::move(stateOf))
+    {
+        throwIf(gbo_nn_create(ctx_->space(), capacity, &nn_), "nearest neighbours");
+    }
+    ~GpuNearestNeighbors() override { gbo_nn_destroy(nn_); }
+
+    void setDistanceFunction(const typename ompl::NearestNeighbors<T>::DistanceFunction &df) override
+    {
+        ompl::NearestNeighbors<T>::setDistanceFunction(df);
+        for (size_t i = 0; i + 1 < elems_.size() && i < 8; ++i)
+        {
+            const double a = df(elems_[i], elems_[i + 1]);
+            const double b = ctx_->omplSpace()->distance(stateOf_(elems_[i]), stateOf_(elems_[i + 1]));
+            if (a != b)
+                throw ompl::Exception("gbompl: GpuNearestNeighbors supports the state space's own metric only");
+        }
+    }
+    bool reportsSortedResults() const override { return true; }
+    void clear() override
+    {
+        throwIf(gbo_nn_clear(nn_), "clear");
+        elems_.clear();
+        alive_.clear();
+    }
+    void add(const T &data) override { add(std::vector<T>{data}); }
+    void add(const std::vector<T> &data) override
+    {
+        const unsigned d = ctx_->dim();
+        std::vector<double> rows(data.size() * d);
+        for (size_t i = 0; i < data.size(); ++i)
+            ctx_->toRow(stateOf_(data[i]), rows.data() + i * d);
+        int64_t first = 0;
+        throwIf(gbo_nn_add_host(nn_, rows.data(), (int64_t)data.size(), &first), "add");
+        elems_.insert(elems_.end(), data.begin(), data.end());
+        alive_.resize(elems_.size(), 1);
+    }
+    bool remove(const T &data) override
+    {
+        for (int64_t i = (int64_t)elems_.size() - 1; i >= 0; --i)
+            if (alive_[i] && elems_[i] == data)
+            {
+                throwIf(gbo_nn_remove_host(nn_, &i, 1), "remove");
+                alive_[i] = 0;
+                return true;
+            }
+        return false;
+    }
+    T nearest(const T &data) const override
+    {
+        std::vector<T> nbh;
+        nearestK(data, 1, nbh);
+        if (nbh.empty())
+            throw ompl::Exception("No elements found in nearest neighbors data structure");
+        return nbh[0];
+    }
+    void nearestK(const T &data, std::size_t k, std::vector<T> &nbh) const override
+    {
+        nbh.clear();
+        if (k == 0)
+            return;
+        std::vector<double> q(ctx_->dim());
+        ctx_->toRow(stateOf_(data), q.data());
+        std::vector<int64_t> idx(k);
+        throwIf(gbo_nn_nearest_k_host(nn_, q.data(), 1, (int)k, idx.data(), nullptr), "nearestK");
+        for (auto i : idx)
+            if (i >= 0)
+                nbh.push_back(elems_[i]);
+    }
+    void nearestR(const T &data, double radius, std::vector<T> &nbh) const override
+    {
+        nbh.clear();
+        std::vector<double> q(ctx_->dim());
+        ctx_->toRow(stateOf_(data), q.data());
+        const int64_t cap = (int64_t)elems_.size();
+        std::vector<int64_t> idx(cap + 1);
+        std::vector<double> dist(cap + 1);
+        int64_t count = 0;
+        throwIf(gbo_nn_nearest_r_host(nn_, q.data(), radius, cap, &count, idx.data(), dist.data()), "nearestR");
+        for (int64_t i = 0; i < count && i < cap; ++i)
+            nbh.push_back(elems_[idx[i]]);
+    }
+    std::size_t size() const override
+    {
+        std::size_t c = 0;
+        for (auto a : alive_)
+            c += a;
+        return c;
+    }
+    void list(std::vector<T> &data) const override
+    {
+        data.clear();
+        for (size_t i = 0; i < elems_.size(); ++i)
+            if (alive_[i])
+                data.push_back(elems_[i]);
+    }
+
+private:
+    GpuContextPtr ctx_;
+    std::function<const ompl::base::State *(const T &)> stateOf_;
+    gbo_nn *nn_ = nullptr;
+    std::vector<T> elems_;
+    std::vector<unsigned char> alive_;
+};
+
+}  // namespace gbompl

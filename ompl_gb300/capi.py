@@ -55,6 +55,12 @@ SIGNATURES = {
     "gbo_nn_nearest_r_count": (C.c_int, [_P, _P, _I64, _I64, C.c_int, C.c_double, _P, _P]),
     "gbo_nn_nearest_r_fill": (C.c_int, [_P, _P, _I64, _I64, C.c_int, C.c_double, _P, _P, _P, _P]),
     "gbo_nn_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "gbo_nn_add_host": (C.c_int, [_P, _P, _I64, C.POINTER(_I64)]),
+    "gbo_nn_remove_host": (C.c_int, [_P, _P, _I64]),
+    "gbo_nn_nearest_k_host": (C.c_int, [_P, _P, _I64, C.c_int, _P, _P]),
+    "gbo_nn_nearest_r_host": (C.c_int, [_P, _P, C.c_double, _I64, C.POINTER(_I64), _P, _P]),
+    "gbo_sample_uniform_host": (C.c_int, [_P, _I64, _P]),
+    "gbo_sample_uniform_near_host": (C.c_int, [_P, _P, C.c_double, _I64, _P]),
     "gbo_measure_fp32_peak": (C.c_int, [_D, _P]),
     "gbo_launch_count": (C.c_uint64, []),
 }

@@ -207,8 +207,14 @@ struct gbo_sampler
 {
     SpaceParams sp{};
     SamplerState *st = nullptr;
+    std::mutex mu;
+    cudaStream_t host_stream = nullptr;
+    Pinned pin;
+    DevBuf dev;
     ~gbo_sampler()
     {
+        if (host_stream)
+            cudaStreamDestroy(host_stream);
         if (st)
             cudaFree(st);
     }
@@ -224,11 +230,17 @@ struct gbo_nn
     float *feat32 = nullptr;
     unsigned char *alive = nullptr;
     float eps32 = 0.f;
-    DevBuf qfeat, fb_list;
+    DevBuf qfeat, fb_list, part;
     CounterRing ctr;
     unsigned long long queries = 0;
+    std::mutex mu;
+    cudaStream_t host_stream = nullptr;
+    Pinned pin;
+    DevBuf dev;
     ~gbo_nn()
     {
+        if (host_stream)
+            cudaStreamDestroy(host_stream);
         if (pts64)
             cudaFree(pts64);
         if (feat32)
@@ -994,6 +1006,11 @@ gbo_status gbo_sampler_create(const gbo_space *space, uint32_t local_seed, gbo_s
         return fail(GBO_ERR_OUT_OF_MEMORY, "sampler allocation failed");
     }
     cudaMemcpy(s->st, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (cudaStreamCreateWithFlags(&s->host_stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete s;
+        return fail(GBO_ERR_CUDA, "stream creation failed");
+    }
     *out = s;
     return GBO_OK;
 }
@@ -1046,6 +1063,11 @@ gbo_status gbo_nn_create(const gbo_space *space, int64_t capacity, gbo_nn **out)
         return fail(GBO_ERR_OUT_OF_MEMORY, "nearest-neighbour index allocation failed");
     }
     cudaMemset(nn->alive, 0, capacity);
+    if (cudaStreamCreateWithFlags(&nn->host_stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete nn;
+        return fail(GBO_ERR_CUDA, "stream creation failed");
+    }
     *out = nn;
     return GBO_OK;
 }
@@ -1160,9 +1182,16 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         if (auto st = nn->fb_list.reserve(sizeof(unsigned long long) * nq))
             return st;
         unsigned long long *fb_n = &ctr->queue;
+        const int P = knn_chunks(lc, nq, nn->size);
+        const int keep = k <= 12 ? 16 : 24;
+        const size_t pl = (size_t)P * nq * keep;
+        if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + 64))
+            return st;
+        int64_t *part_k = (int64_t *)nn->part.p;
+        float *part_d = (float *)(part_k + pl);
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
         if (launch_knn_fp32(lc, a, nn->sp, qv, (const float *)nn->qfeat.p, nq, k, prefix, idx, dist,
-                            (unsigned long long *)nn->fb_list.p, fb_n, ctr))
+                            (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P))
         {
             // queries whose FP32 band overflowed: exact FP64 scan (count read on the device)
             launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist, (const unsigned long long *)nn->fb_list.p,
@@ -1209,6 +1238,141 @@ gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked
         *rechecked = h.rechecked;
     if (fallbacks)
         *fallbacks = h.fallbacks;
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_add_host(gbo_nn *nn, const double *states, int64_t n, int64_t *first_key)
+{
+    if (!nn || n < 0 || (n > 0 && !states))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad add arguments");
+    std::lock_guard<std::mutex> lk(nn->mu);
+    const size_t b = (size_t)n * nn->sp.dim * sizeof(double);
+    if (auto st = nn->pin.reserve(b + 16))
+        return st;
+    if (auto st = nn->dev.reserve(b + 16))
+        return st;
+    std::memcpy(nn->pin.p, states, b);
+    CUDA_TRY(cudaMemcpyAsync(nn->dev.p, nn->pin.p, b, cudaMemcpyHostToDevice, nn->host_stream));
+    if (auto st = gbo_nn_add(nn, (const double *)nn->dev.p, n, nn->sp.dim, GBO_LAYOUT_AOS, first_key,
+                             nn->host_stream))
+        return st;
+    CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_remove_host(gbo_nn *nn, const int64_t *keys, int64_t n)
+{
+    if (!nn || n < 0 || (n > 0 && !keys))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad remove arguments");
+    std::lock_guard<std::mutex> lk(nn->mu);
+    const size_t b = (size_t)n * sizeof(int64_t);
+    if (auto st = nn->dev.reserve(b + 16))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(nn->dev.p, keys, b, cudaMemcpyHostToDevice, nn->host_stream));
+    if (auto st = gbo_nn_remove(nn, (const int64_t *)nn->dev.p, n, nn->host_stream))
+        return st;
+    CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_nearest_k_host(gbo_nn *nn, const double *q, int64_t nq, int k, int64_t *idx, double *dist)
+{
+    if (!nn || nq < 0 || k < 1 || (nq > 0 && (!q || !idx)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestK arguments");
+    std::lock_guard<std::mutex> lk(nn->mu);
+    const size_t bq = (size_t)nq * nn->sp.dim * sizeof(double), bo = (size_t)nq * k * 8;
+    if (auto st = nn->pin.reserve(std::max(bq, 2 * bo) + 16))
+        return st;
+    if (auto st = nn->dev.reserve(bq + 2 * bo + 32))
+        return st;
+    char *d = (char *)nn->dev.p;
+    std::memcpy(nn->pin.p, q, bq);
+    CUDA_TRY(cudaMemcpyAsync(d, nn->pin.p, bq, cudaMemcpyHostToDevice, nn->host_stream));
+    int64_t *di = (int64_t *)(d + pad16(bq));
+    double *dd = (double *)(d + pad16(bq) + bo);
+    if (auto st = gbo_nn_nearest_k(nn, (const double *)d, nq, nn->sp.dim, GBO_LAYOUT_AOS, k, nullptr, di,
+                                   dist ? dd : nullptr, nn->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(nn->pin.p, di, bo, cudaMemcpyDeviceToHost, nn->host_stream));
+    if (dist)
+        CUDA_TRY(cudaMemcpyAsync((char *)nn->pin.p + bo, dd, bo, cudaMemcpyDeviceToHost, nn->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
+    std::memcpy(idx, nn->pin.p, bo);
+    if (dist)
+        std::memcpy(dist, (char *)nn->pin.p + bo, bo);
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t cap, int64_t *count, int64_t *idx,
+                                 double *dist)
+{
+    if (!nn || !q || !count || cap < 0 || (cap > 0 && (!idx || !dist)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestR arguments");
+    std::lock_guard<std::mutex> lk(nn->mu);
+    const int dim = nn->sp.dim;
+    if (auto st = nn->dev.reserve(64 + 16 * (size_t)(nn->size + 1) + 16 * (size_t)dim))
+        return st;
+    char *d = (char *)nn->dev.p;
+    double *dq = (double *)d;
+    int64_t *dcount = (int64_t *)(d + 16 * ((dim * 8 + 15) / 16));
+    int64_t *doff = dcount + 1;
+    int64_t *didx = dcount + 2;
+    double *ddist = (double *)(didx + nn->size + 1);
+    CUDA_TRY(cudaMemcpyAsync(dq, q, dim * sizeof(double), cudaMemcpyHostToDevice, nn->host_stream));
+    CUDA_TRY(cudaMemsetAsync(doff, 0, sizeof(int64_t), nn->host_stream));
+    if (auto st = gbo_nn_nearest_r_count(nn, dq, 1, dim, GBO_LAYOUT_AOS, r, dcount, nn->host_stream))
+        return st;
+    if (auto st = gbo_nn_nearest_r_fill(nn, dq, 1, dim, GBO_LAYOUT_AOS, r, doff, didx, ddist, nn->host_stream))
+        return st;
+    int64_t c = 0;
+    CUDA_TRY(cudaMemcpyAsync(&c, dcount, sizeof(int64_t), cudaMemcpyDeviceToHost, nn->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
+    *count = c;
+    const int64_t m = std::min(c, cap);
+    if (m > 0)
+    {
+        CUDA_TRY(cudaMemcpy(idx, didx, m * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(dist, ddist, m * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return GBO_OK;
+}
+
+gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out)
+{
+    if (!s || n < 0 || (n > 0 && !out))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const size_t b = (size_t)n * s->sp.dim * sizeof(double);
+    if (auto st = s->dev.reserve(b + 16))
+        return st;
+    if (auto st = s->pin.reserve(b + 16))
+        return st;
+    if (auto st = gbo_sample_uniform(s, n, (double *)s->dev.p, s->sp.dim, GBO_LAYOUT_AOS, s->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(s->pin.p, s->dev.p, b, cudaMemcpyDeviceToHost, s->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(s->host_stream));
+    std::memcpy(out, s->pin.p, b);
+    return GBO_OK;
+}
+
+gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out)
+{
+    if (!s || n < 0 || (n > 0 && (!out || !near)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniformNear arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const size_t b = (size_t)n * s->sp.dim * sizeof(double);
+    if (auto st = s->dev.reserve(2 * b + 32))
+        return st;
+    if (auto st = s->pin.reserve(b + 16))
+        return st;
+    double *dn = (double *)s->dev.p, *dout = (double *)((char *)s->dev.p + pad16(b));
+    std::memcpy(s->pin.p, near, b);
+    CUDA_TRY(cudaMemcpyAsync(dn, s->pin.p, b, cudaMemcpyHostToDevice, s->host_stream));
+    if (auto st = gbo_sample_uniform_near(s, dn, distance, n, s->sp.dim, GBO_LAYOUT_AOS, dout, s->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(s->pin.p, dout, b, cudaMemcpyDeviceToHost, s->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(s->host_stream));
+    std::memcpy(out, s->pin.p, b);
     return GBO_OK;
 }
 

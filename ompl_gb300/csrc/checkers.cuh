@@ -85,7 +85,7 @@ __device__ __forceinline__ void chain_points64(const SpaceParams &s, const doubl
             Y[i + 1] = y;
         }
 #pragma unroll
-    for (int i = 0; i < MAXD; ++i)
+    for (int i = 0; i <= MAXD; ++i)
         if (i == s.dim)
         {
             X[i + 1] = dadd(x, dmul(c, 0.001));
@@ -202,7 +202,7 @@ __device__ int chain_valid32(const SpaceParams &s, const double *q, const ChainS
             Y[i + 1] = y;
         }
 #pragma unroll
-    for (int i = 0; i < MAXD; ++i)
+    for (int i = 0; i <= MAXD; ++i)
         if (i == s.dim)
         {
             VX[i] = c * 0.001f;

@@ -6,11 +6,13 @@
 //
 //   knn_exact_kernel  FP64, one warp per query: lanes scan keys lane, lane+32, ... keeping a sorted
 //                     register top-k; the warp then merges the 32 lists with shuffle argmin rounds.
-//   knn_fp32_kernel   FP32 bulk, one thread per query, element features staged in shared memory
-//                     tiles; keeps the best K_KEEP by FP32 distance. Every kept element within
-//                     2*eps of the k-th FP32 distance is re-evaluated in FP64 and the final order is
-//                     decided in FP64. If more than K_KEEP elements fall in that band the query is
-//                     queued for knn_exact_kernel (FP64 scan).
+//   knn_scan_kernel   FP32 bulk, one thread per query over one chunk of the elements (CTA grid =
+//                     query blocks x chunks, so that few queries still fill the GPU), element features
+//                     staged in shared-memory tiles and read as float4; keeps the best K_KEEP by FP32
+//                     distance (kinematic chain: an L1 lower bound skips the square roots of far elements).
+//   knn_finish_kernel merges the chunk lists; every kept element within 2*eps of the k-th FP32
+//                     distance is re-evaluated in FP64 and the final order is decided in FP64. If the
+//                     band may hold more than K_KEEP elements the query is queued for knn_exact_kernel.
 //   radius kernels    FP64 count / fill (CSR), sorted by (distance, key).
 #include "kernels_nn.cuh"
 
@@ -202,33 +204,37 @@ __device__ __forceinline__ float chain_dist32(const float *a, const float *b, in
     return s;
 }
 
-template <int KIND, int MAXD, int MAXF, int K_KEEP>
-__global__ void __launch_bounds__(128) knn_fp32_kernel(NNArgs nn, SpaceParams sp, StatesView qv, const float *qf,
-                                                       int64_t nq, int k, const int64_t *prefix, int64_t *idx,
-                                                       double *dist, unsigned long long *fb_list,
-                                                       unsigned long long *fb_n, RunCounters *ctr)
+// Partial scan: CTA (x = block of 128 queries, y = chunk of elements). Each thread keeps the K_KEEP
+// smallest FP32 distances (squared for box/wrapped kinds) of its query within the chunk.
+template <int KIND, int MAXF, int K_KEEP>
+__global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp, const float *qf, int64_t nq,
+                                                       const int64_t *prefix, int64_t chunk, float *part_d,
+                                                       int64_t *part_k)
 {
     constexpr int TILE = 128;
-    __shared__ float tile[MAXF][TILE];
+    constexpr int FP = (MAXF + 3) / 4 * 4;
+    __shared__ __align__(16) float tile[TILE][FP];
     __shared__ unsigned char tile_alive[TILE];
-    __shared__ int64_t s_limit;
+    __shared__ unsigned long long s_limit;
     const int F = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 2 * sp.dim : sp.dim;
     const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = qi < nq;
-    float qfe[MAXF];
+    const int64_t c0 = (int64_t)blockIdx.y * chunk;
+    const int64_t c1 = min(c0 + chunk, nn.size);
+    float qfe[FP];
 #pragma unroll
-    for (int f = 0; f < MAXF; ++f)
+    for (int f = 0; f < FP; ++f)
         qfe[f] = (active && f < F) ? qf[(int64_t)f * nq + qi] : 0.f;
-    int64_t limit = nn.size;
+    int64_t limit = c1;
     if (active && prefix)
         limit = min(limit, prefix[qi]);
     if (threadIdx.x == 0)
         s_limit = 0;
     __syncthreads();
-    if (active)
-        atomicMax((unsigned long long *)&s_limit, (unsigned long long)limit);
+    if (active && limit > c0)
+        atomicMax(&s_limit, (unsigned long long)limit);
     __syncthreads();
-    const int64_t block_limit = s_limit;
+    const int64_t block_end = (int64_t)s_limit;
 
     float dk[K_KEEP];
     int64_t ik[K_KEEP];
@@ -238,37 +244,41 @@ __global__ void __launch_bounds__(128) knn_fp32_kernel(NNArgs nn, SpaceParams sp
         dk[j] = __int_as_float(0x7f800000);
         ik[j] = -1;
     }
-    const float lb_scale = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 0.70710678f * (1.0f - 1e-5f) : 1.0f;
-    for (int64_t base = 0; base < block_limit; base += TILE)
+    const float lscale = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 0.70710678f * (1.0f - 1e-5f) * (float)sp.link : 1.0f;
+    for (int64_t base = c0; base < block_end; base += TILE)
     {
         __syncthreads();
-        for (int t = threadIdx.x; t < TILE; t += blockDim.x)
+        for (int i = threadIdx.x; i < TILE * F; i += blockDim.x)
         {
+            const int f = i / TILE, t = i - f * TILE;
             const int64_t key = base + t;
-            const bool in = key < block_limit;
-            tile_alive[t] = in ? nn.alive[key] : 0;
-#pragma unroll
-            for (int f = 0; f < MAXF; ++f)
-                if (f < F)
-                    tile[f][t] = in ? nn.feat32[(int64_t)f * nn.cap + key] : 0.f;
+            tile[t][f] = key < block_end ? nn.feat32[(int64_t)f * nn.cap + key] : 0.f;
         }
+        for (int t = threadIdx.x; t < TILE; t += blockDim.x)
+            tile_alive[t] = (base + t < block_end) ? nn.alive[base + t] : 0;
         __syncthreads();
         if (!active)
             continue;
-        const int tn = (int)min((int64_t)TILE, limit - base);
+        const int tn = (int)max((int64_t)0, min((int64_t)TILE, limit - base));
         for (int t = 0; t < tn; ++t)
         {
             if (!tile_alive[t])
                 continue;
-            float pf[MAXF];
+            float pf[FP];
 #pragma unroll
-            for (int f = 0; f < MAXF; ++f)
-                pf[f] = f < F ? tile[f][t] : 0.f;
+            for (int f = 0; f < FP; f += 4)
+            {
+                const float4 v = *reinterpret_cast<const float4 *>(&tile[t][f]);
+                pf[f] = v.x;
+                pf[f + 1] = v.y;
+                pf[f + 2] = v.z;
+                pf[f + 3] = v.w;
+            }
             float lower;
             float d = dist32_sq_or_d<KIND, MAXF>(pf, qfe, sp.dim, lower);
             if constexpr (KIND == GBO_SPACE_KINEMATIC_CHAIN)
             {
-                if (lower * lb_scale * (float)sp.link >= dk[K_KEEP - 1])
+                if (lower * lscale >= dk[K_KEEP - 1])
                     continue;
                 d = chain_dist32<KIND, MAXF>(pf, qfe, sp.dim) * (float)sp.link;
             }
@@ -278,9 +288,51 @@ __global__ void __launch_bounds__(128) knn_fp32_kernel(NNArgs nn, SpaceParams sp
     }
     if (!active)
         return;
-    // Re-check band in FP64. For squared-distance kinds the band is applied on squared values.
+    const int64_t o = ((int64_t)blockIdx.y * nq + qi) * K_KEEP;
+#pragma unroll
+    for (int j = 0; j < K_KEEP; ++j)
+    {
+        part_d[o + j] = dk[j];
+        part_k[o + j] = ik[j];
+    }
+}
+
+// Merge the per-chunk lists, then decide in FP64: every element within 2*eps of the k-th FP32
+// distance is re-evaluated with the reference-order FP64 distance and the final order is
+// (FP64 distance, key). If the band may hold more than K_KEEP elements the query goes to the FP64 scan.
+template <int KIND, int MAXD, int K_KEEP>
+__global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams sp, StatesView qv, int64_t nq, int k,
+                                                         int P, const float *part_d, const int64_t *part_k,
+                                                         int64_t *idx, double *dist, unsigned long long *fb_list,
+                                                         unsigned long long *fb_n, RunCounters *ctr)
+{
+    const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq)
+        return;
+    float dk[K_KEEP];
+    int64_t ik[K_KEEP];
+#pragma unroll
+    for (int j = 0; j < K_KEEP; ++j)
+    {
+        dk[j] = __int_as_float(0x7f800000);
+        ik[j] = -1;
+    }
+    // dropped: smallest distance of an element that fell out of some chunk's list (bounds the rest)
+    for (int c = 0; c < P; ++c)
+    {
+        const int64_t o = ((int64_t)c * nq + qi) * K_KEEP;
+        for (int j = 0; j < K_KEEP; ++j)
+        {
+            const int64_t key = part_k[o + j];
+            if (key < 0)
+                break;
+            const float d = part_d[o + j];
+            if (d < dk[K_KEEP - 1] || (d == dk[K_KEEP - 1] && ik[K_KEEP - 1] < 0))
+                topk_insert<K_KEEP>(dk, ik, d, key);
+        }
+    }
     const float eps = nn.eps32;
-    const float kth = dk[k - 1 < K_KEEP ? k - 1 : K_KEEP - 1];
+    const float kth = dk[k - 1];
     float band;
     if constexpr (KIND == GBO_SPACE_KINEMATIC_CHAIN)
         band = kth + 2.f * eps;
@@ -289,11 +341,16 @@ __global__ void __launch_bounds__(128) knn_fp32_kernel(NNArgs nn, SpaceParams sp
         const float r = sqrtf(kth) + 2.f * eps;
         band = r * r * (1.0f + 1e-6f);
     }
-    const int64_t live = min(limit, (int64_t)nn.size);  // upper bound on candidates
-    (void)live;
-    if (k < K_KEEP && !(dk[K_KEEP - 1] > band) && ik[K_KEEP - 1] >= 0)
+    // A full kept list whose last entry is inside the band, or any chunk list that was full and whose
+    // last entry is inside the band, means elements of the band may have been dropped.
+    bool overflow = ik[K_KEEP - 1] >= 0 && !(dk[K_KEEP - 1] > band);
+    for (int c = 0; c < P && !overflow; ++c)
     {
-        // more than K_KEEP elements may lie in the band: exact scan
+        const int64_t o = ((int64_t)c * nq + qi) * K_KEEP;
+        overflow = part_k[o + K_KEEP - 1] >= 0 && !(part_d[o + K_KEEP - 1] > band);
+    }
+    if (overflow)
+    {
         const unsigned long long pos = atomicAdd(fb_n, 1ull);
         fb_list[pos] = (unsigned long long)qi;
         atomicAdd(&ctr->fallbacks, 1ull);
@@ -303,40 +360,38 @@ __global__ void __launch_bounds__(128) knn_fp32_kernel(NNArgs nn, SpaceParams sp
     load_query<MAXD>(qv, qi, sp.dim, q64);
     double d64[K_KEEP];
     int64_t k64[K_KEEP];
-    int nc = 0;
 #pragma unroll
     for (int j = 0; j < K_KEEP; ++j)
     {
         d64[j] = __longlong_as_double(0x7ff0000000000000ll);
         k64[j] = INT64_MAX;
     }
-#pragma unroll
+    int nc = 0;
     for (int j = 0; j < K_KEEP; ++j)
-        if (ik[j] >= 0 && (j < k || dk[j] <= band))
-        {
-            double x[MAXD];
-            load_point<MAXD>(nn.pts64, nn.cap, sp.dim, ik[j], x);
-            const double d = distance64<MAXD>(sp, x, q64);
-            // insertion into (d, key) order
-            double cd = d;
-            int64_t ck = ik[j];
+    {
+        if (ik[j] < 0 || !(j < k || dk[j] <= band))
+            break;
+        double x[MAXD];
+        load_point<MAXD>(nn.pts64, nn.cap, sp.dim, ik[j], x);
+        double cd = distance64<MAXD>(sp, x, q64);
+        int64_t ck = ik[j];
 #pragma unroll
-            for (int m = 0; m < K_KEEP; ++m)
-                if (less_dk(cd, ck, d64[m], k64[m]))
-                {
-                    const double td = d64[m];
-                    const int64_t tk = k64[m];
-                    d64[m] = cd;
-                    k64[m] = ck;
-                    cd = td;
-                    ck = tk;
-                }
-            ++nc;
-        }
+        for (int m = 0; m < K_KEEP; ++m)
+            if (less_dk(cd, ck, d64[m], k64[m]))
+            {
+                const double td = d64[m];
+                const int64_t tk = k64[m];
+                d64[m] = cd;
+                k64[m] = ck;
+                cd = td;
+                ck = tk;
+            }
+        ++nc;
+    }
     atomicAdd(&ctr->rechecked, (unsigned long long)nc);
     for (int j = 0; j < k; ++j)
     {
-        const bool have = j < K_KEEP && k64[j] != INT64_MAX;
+        const bool have = k64[j] != INT64_MAX;
         idx[qi * k + j] = have ? k64[j] : -1;
         if (dist)
             dist[qi * k + j] = have ? d64[j] : __longlong_as_double(0x7ff0000000000000ll);
@@ -490,36 +545,55 @@ void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &
         launch_exact_t<16>(lc, nn, sp, qv, nq, k, prefix, idx, dist, list, list_n, max_items);
 }
 
-template <int KIND, int MAXD, int MAXF>
+template <int KIND, int MAXD, int MAXF, int K_KEEP>
 static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                           int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist,
-                          unsigned long long *fb_list, unsigned long long *fb_n, RunCounters *ctr)
+                          unsigned long long *fb_list, unsigned long long *fb_n, RunCounters *ctr, float *part_d,
+                          int64_t *part_k, int P, int64_t chunk)
 {
-    const int grid = (int)((nq + 127) / 128);
-    if (k <= 12)
-        knn_fp32_kernel<KIND, MAXD, MAXF, 16><<<grid, 128, 0, lc.stream>>>(nn, sp, qv, qf, nq, k, prefix, idx, dist,
-                                                                           fb_list, fb_n, ctr);
-    else
-        knn_fp32_kernel<KIND, MAXD, MAXF, 24><<<grid, 128, 0, lc.stream>>>(nn, sp, qv, qf, nq, k, prefix, idx, dist,
-                                                                           fb_list, fb_n, ctr);
+    const int qb = (int)((nq + 127) / 128);
+    knn_scan_kernel<KIND, MAXF, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix, chunk, part_d,
+                                                                           part_k);
+    knn_finish_kernel<KIND, MAXD, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,
+                                                                    fb_list, fb_n, ctr);
     note_launch();
+    note_launch();
+}
+
+int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size)
+{
+    const int64_t qb = (nq + 127) / 128;
+    int64_t P = (lc.sm_count * 8 + qb - 1) / qb;
+    P = std::min<int64_t>(P, std::max<int64_t>(1, size / 4096));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(P, 64));
 }
 
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                     unsigned long long *fb_n, RunCounters *ctr)
+                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
 {
     if (k > 20 || nq == 0)
         return false;
+    const int64_t chunk = (nn.size + P - 1) / P;
+#define GBO_FP32(KIND, MAXD, MAXF)                                                                                     \
+    do                                                                                                                \
+    {                                                                                                                 \
+        if (k <= 12)                                                                                                  \
+            launch_fp32_t<KIND, MAXD, MAXF, 16>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
+                                                part_d, part_k, P, chunk);                                            \
+        else                                                                                                          \
+            launch_fp32_t<KIND, MAXD, MAXF, 24>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
+                                                part_d, part_k, P, chunk);                                            \
+    } while (0)
     if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN && sp.dim <= 10)
-        launch_fp32_t<GBO_SPACE_KINEMATIC_CHAIN, 10, 20>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n,
-                                                          ctr);
+        GBO_FP32(GBO_SPACE_KINEMATIC_CHAIN, 10, 20);
     else if (sp.kind == GBO_SPACE_WRAP_L2 && sp.dim <= 8)
-        launch_fp32_t<GBO_SPACE_WRAP_L2, 8, 8>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr);
+        GBO_FP32(GBO_SPACE_WRAP_L2, 8, 8);
     else if (sp.kind == GBO_SPACE_REAL_VECTOR && sp.dim <= 8)
-        launch_fp32_t<GBO_SPACE_REAL_VECTOR, 8, 8>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr);
+        GBO_FP32(GBO_SPACE_REAL_VECTOR, 8, 8);
     else
         return false;
+#undef GBO_FP32
     return true;
 }
 

@@ -20,7 +20,8 @@ void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &
                       const unsigned long long *list_n, int64_t max_items);
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                     unsigned long long *fb_n, RunCounters *ctr);
+                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P);
+int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size);
 void launch_features(const LaunchCfg &lc, const SpaceParams &sp, StatesView v, int64_t n, float *out, int64_t ld_out);
 void launch_store_points(const LaunchCfg &lc, StatesView v, int64_t n, int dim, double *pts, int64_t cap,
                          int64_t first, unsigned char *alive);

@@ -1,0 +1,106 @@
+// Builds the gbompl OMPL plugins against OMPL's own headers and objects and compares them with
+// OMPL's DiscreteMotionValidator / StateValidityChecker / NearestNeighborsLinear on the same
+// SpaceInformation. Without a GPU it checks that construction fails with ompl::Exception.
+#include <ompl/base/DiscreteMotionValidator.h>
+#include <ompl/base/SpaceInformation.h>
+#include <ompl/base/spaces/RealVectorStateSpace.h>
+#include <ompl/datastructures/NearestNeighborsLinear.h>
+
+#include <cstdio>
+#include <random>
+
+#include "gbompl_ompl.hpp"
+
+namespace ob = ompl::base;
+
+struct Circles : ob::StateValidityChecker
+{
+    Circles(ob::SpaceInformation *si, std::vector<double> c) : ob::StateValidityChecker(si), c_(std::move(c)) {}
+    bool isValid(const ob::State *s) const override
+    {
+        const double *xy = s->as<ob::RealVectorStateSpace::StateType>()->values;
+        for (size_t i = 0; i < c_.size(); i += 3)
+        {
+            double dx = c_[i] - xy[0], dy = c_[i + 1] - xy[1];
+            if (dx * dx + dy * dy < c_[i + 2] * c_[i + 2])
+                return false;
+        }
+        return true;
+    }
+    std::vector<double> c_;
+};
+
+int main()
+{
+    std::mt19937_64 g(5);
+    std::uniform_real_distribution<double> U(0, 1), R(0.02, 0.06);
+    std::vector<double> world;
+    for (int i = 0; i < 100; ++i)
+        world.insert(world.end(), {U(g), U(g), R(g)});
+    auto space = std::make_shared<ob::RealVectorStateSpace>(2);
+    space->setBounds(0.0, 1.0);
+    auto si = std::make_shared<ob::SpaceInformation>(space);
+    si->setStateValidityChecker(std::make_shared<Circles>(si.get(), world));
+    si->setStateValidityCheckingResolution(0.01);
+    si->setup();
+    gbompl::GpuContextPtr ctx;
+    try
+    {
+        ctx = std::make_shared<gbompl::GpuContext>(space, GBO_SPACE_REAL_VECTOR);
+        ctx->bindWorld(GBO_CHECK_CIRCLES, world, 3, {}, 0, 0.0, GBO_PRECISION_FP64);
+    }
+    catch (const ompl::Exception &e)
+    {
+        std::printf("NO_DEVICE %s\n", e.what());
+        return 0;
+    }
+    gbompl::GpuStateValidityChecker gsvc(si, ctx);
+    gbompl::GpuDiscreteMotionValidator gmv(si, ctx);
+    ob::DiscreteMotionValidator ref(si);
+    auto a = si->allocState(), b = si->allocState(), la = si->allocState(), lb = si->allocState();
+    int mism = 0;
+    for (int i = 0; i < 2000; ++i)
+    {
+        auto *va = a->as<ob::RealVectorStateSpace::StateType>()->values;
+        auto *vb = b->as<ob::RealVectorStateSpace::StateType>()->values;
+        va[0] = U(g); va[1] = U(g); vb[0] = U(g); vb[1] = U(g);
+        mism += gsvc.isValid(a) != si->isValid(a);
+        std::pair<ob::State *, double> l1(la, -7.0), l2(lb, -7.0);
+        bool r1 = gmv.checkMotion(a, b, l1), r2 = ref.checkMotion(a, b, l2);
+        mism += r1 != r2 || gmv.checkMotion(a, b) != ref.checkMotion(a, b);
+        if (!r1 && !r2)
+            mism += l1.second != l2.second || !space->equalStates(la, lb);
+    }
+    // nearest neighbours over State* elements
+    std::vector<ob::State *> pts(3000);
+    for (auto &p : pts)
+    {
+        p = si->allocState();
+        auto *v = p->as<ob::RealVectorStateSpace::StateType>()->values;
+        v[0] = U(g);
+        v[1] = U(g);
+    }
+    gbompl::GpuNearestNeighbors<ob::State *> gnn(ctx, [](ob::State *const &s) { return (const ob::State *)s; }, 4096);
+    ompl::NearestNeighborsLinear<ob::State *> lnn;
+    auto df = [&](ob::State *const &x, ob::State *const &y) { return space->distance(x, y); };
+    gnn.setDistanceFunction(df);
+    lnn.setDistanceFunction(df);
+    gnn.add(pts);
+    lnn.add(pts);
+    gnn.remove(pts[7]);
+    lnn.remove(pts[7]);
+    std::vector<ob::State *> n1, n2;
+    for (int q = 0; q < 100; ++q)
+    {
+        gnn.nearestK(pts[q * 13], 10, n1);
+        lnn.nearestK(pts[q * 13], 10, n2);
+        mism += n1 != n2;
+        gnn.nearestR(pts[q * 13], 0.05, n1);
+        lnn.nearestR(pts[q * 13], 0.05, n2);
+        mism += n1 != n2;
+    }
+    mism += gnn.size() != lnn.size();
+    std::printf("%s mismatches=%d valid=%u invalid=%u\n", mism ? "MISMATCH" : "MATCH", mism,
+                gmv.getValidMotionCount(), gmv.getInvalidMotionCount());
+    return mism ? 1 : 0;
+}
