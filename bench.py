@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks"],
+                   help="launch one kernel kind twice on the chain workload (for ncu) and exit")
     return p.parse_args()
 
 
@@ -326,8 +328,48 @@ def ours(args, rank, world, local_rank):
     print(json.dumps(out))
 
 
+def profile(kind):
+    """Two launches of one kernel kind on the 10-link chain workload (first = warm-up), for ncu."""
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import capi
+    w = workload()
+    space = B.KinematicChainSpace(w.dim, w.link_length)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.KinematicChainValidityChecker(space, w.obstacles)
+    checker.setPrecision("fp64" if kind == "motion_plain" else "fp32_guarded")
+    if kind == "peaks":
+        print(json.dumps({"fp32_flops": B.measure_fp32_peak(), "fp64_flops": B.measure_fp64_peak()}))
+        return
+    states = torch.as_tensor(w.states.T.copy(), device="cuda")
+    if kind == "validity":
+        for _ in range(2):
+            checker.isValid(states, soa=True)
+    elif kind in ("motion", "motion_plain"):
+        valid = checker.isValid(states, soa=True).cpu().numpy().astype(bool)
+        (a, b), = make_batches(w.states[valid], 1)
+        s1, s2 = torch.as_tensor(a.T.copy(), device="cuda"), torch.as_tensor(b.T.copy(), device="cuda")
+        mv = B.DiscreteMotionValidator(checker)
+        sch = capi.SCHEDULE_PLAIN if kind == "motion_plain" else capi.SCHEDULE_TILE
+        n = 20_000 if kind == "motion_plain" else N_EDGES
+        for _ in range(2):
+            mv.checkMotions(s1[:, :n].contiguous(), s2[:, :n].contiguous(), schedule=sch, soa=True)
+    elif kind == "knn":
+        nn = B.NearestNeighborsGPU(space, capacity=N_STATES)
+        nn.add(states, soa=True)
+        q = states[:, :2048].contiguous()
+        for _ in range(2):
+            nn.nearestK(q, 16, soa=True, want_dist=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": kind, "ok": True}))
+
+
 def main():
     args = parse()
+    if args.profile:
+        profile(args.profile)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -174,6 +174,8 @@ gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, doub
 
 /* ---- measurement helper ---- FP32 FMA throughput of this GPU (FLOP/s), for roofline denominators. */
 gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
+/* FP64 FMA throughput of this GPU (FLOP/s). */
+gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
 /* Number of kernels this library launched since load (for launch accounting). */
 uint64_t gbo_launch_count(void);
 

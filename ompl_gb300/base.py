@@ -431,5 +431,11 @@ def measure_fp32_peak():
     return f.value
 
 
+def measure_fp64_peak():
+    f = C.c_double()
+    check(lib().gbo_measure_fp64_peak(C.byref(f), _stream(None)))
+    return f.value
+
+
 def launch_count():
     return int(lib().gbo_launch_count())

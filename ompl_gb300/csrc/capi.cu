@@ -1387,4 +1387,15 @@ gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream)
     return GBO_OK;
 }
 
+gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream)
+{
+    if (!flops)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "flops is NULL");
+    if (auto st = ensure_device())
+        return st;
+    *flops = measure_fp64_peak(lcfg(stream));
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
 }  // extern "C"

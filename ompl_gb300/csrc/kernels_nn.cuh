@@ -39,5 +39,6 @@ struct SamplerState
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
                            StatesView nearv, double distance, int64_t n, MutStatesView out);
 double measure_fp32_peak(const LaunchCfg &lc);
+double measure_fp64_peak(const LaunchCfg &lc);
 
 }  // namespace gbo

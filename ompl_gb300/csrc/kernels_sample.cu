@@ -212,6 +212,49 @@ __global__ void __launch_bounds__(256) fma_peak_kernel(float *sink, int iters, f
         sink[0] = r;
 }
 
+__global__ void __launch_bounds__(256) dfma_peak_kernel(double *sink, int iters, double seed)
+{
+    double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
+    const double b = 0.999999, c = 1e-7;
+    for (int i = 0; i < iters; ++i)
+    {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            a0 = fma(a0, b, c);
+            a1 = fma(a1, b, c);
+            a2 = fma(a2, b, c);
+            a3 = fma(a3, b, c);
+        }
+    }
+    const double r = a0 + a1 + a2 + a3;
+    if (r == 12345.678)
+        sink[0] = r;
+}
+
+double measure_fp64_peak(const LaunchCfg &lc)
+{
+    double *sink = nullptr;
+    cudaMalloc(&sink, 16);
+    const int blocks = lc.sm_count * 8, iters = 256;
+    dfma_peak_kernel<<<blocks, 256, 0, lc.stream>>>(sink, 8, 1.0);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, lc.stream);
+    dfma_peak_kernel<<<blocks, 256, 0, lc.stream>>>(sink, iters, 1.0);
+    cudaEventRecord(e1, lc.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    note_launch();
+    note_launch();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    return ms > 0.f ? 2.0 * 4 * 8 * (double)iters * blocks * 256 / (ms * 1e-3) : 0.0;
+}
+
 double measure_fp32_peak(const LaunchCfg &lc)
 {
     float *sink = nullptr;

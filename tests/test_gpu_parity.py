@@ -1,7 +1,8 @@
 """GPU parity: libgbompl.so through its C ABI against OMPL's own outputs (golden fixtures) and the
 oracle on seeded inputs. Booleans, first-invalid indices, segment counts, samples, and kNN index
 sets must match exactly; FP64 values are compared bitwise except where the kinematic-chain space
-evaluates sin/cos (CUDA's FP64 sin/cos vs glibc's may differ in the last bit; tolerance 4 ulp)."""
+evaluates sin/cos (CUDA's FP64 sin/cos vs glibc's may differ in the last bit; relative tolerance
+1e-12 on those distances, see ulp_close)."""
 import math
 
 import numpy as np
@@ -48,12 +49,15 @@ def gpu_checker(space, ck: CheckerDesc):
     return B.AllValidStateValidityChecker(space)
 
 
-def ulp_close(a, b, ulps=4):
+def ulp_close(a, b, rel=1e-12):
+    """The kinematic-chain metric sums differences of sin/cos values; CUDA's FP64 sin/cos and glibc's
+    differ in the last bit, and the cancellation in cos(t1) - cos(t2) magnifies that to a relative
+    difference of up to ~1e-13 in the distance. Tolerance: relative 1e-12."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     both_nan = np.isnan(a) & np.isnan(b)
     diff = np.abs(a - b)
-    tol = ulps * np.spacing(np.maximum(np.abs(a), np.abs(b)))
+    tol = rel * np.maximum(np.abs(a), np.abs(b))
     return bool(np.all(both_nan | (diff <= tol) | (a == b)))
 
 
