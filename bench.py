@@ -351,7 +351,7 @@ def profile(kind):
         (a, b), = make_batches(w.states[valid], 1)
         s1, s2 = torch.as_tensor(a.T.copy(), device="cuda"), torch.as_tensor(b.T.copy(), device="cuda")
         mv = B.DiscreteMotionValidator(checker)
-        sch = capi.SCHEDULE_PLAIN if kind == "motion_plain" else capi.SCHEDULE_TILE
+        sch = capi.SCHEDULE_PLAIN if kind == "motion_plain" else capi.SCHEDULE_WARP
         n = 20_000 if kind == "motion_plain" else N_EDGES
         for _ in range(2):
             mv.checkMotions(s1[:, :n].contiguous(), s2[:, :n].contiguous(), schedule=sch, soa=True)

@@ -68,6 +68,10 @@ void launch_states_chain(const LaunchCfg &lc, const SpaceParams &sp, const World
                          unsigned long long *first, RunCounters *ctr);
 void launch_last_valid(const LaunchCfg &lc, const SpaceParams &sp, StatesView v1, StatesView v2, const int32_t *fj,
                        const int32_t *nd, int64_t n, double *last_t, MutStatesView out);
+bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
+                                int64_t n, uint8_t *out, RunCounters *ctr);
+bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v1,
+                              StatesView v2, int64_t n, uint8_t *ok, int32_t *fj, int32_t *nd, RunCounters *ctr);
 void launch_distance(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, int64_t n, double *out);
 void launch_interpolate(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, const double *t,
                         int64_t n, MutStatesView out);

@@ -1,0 +1,301 @@
+// Kinematic-chain kernels built on the warp-cooperative FP32 evaluator (chain_warp.cuh).
+//
+//   chain_validity_warp_kernel  StateValidityChecker::isValid, one warp per state
+//   chain_motion_warp_kernel    DiscreteMotionValidator::checkMotion, persistent, one warp per edge
+//                               taken from the device work queue; states j = 1..nd-1 then s2 in order
+//                               (DiscreteMotionValidator.cpp:48-91), stopping at the first invalid one.
+// Interpolated joints are formed in float-float from exact splits of s1 and s2:
+//   q_i(t) = s1_i + D_i t, D_i the shortest-arc difference of KinematicChain.h:150-176 (the wrap by
+//   2*pi that interpolate applies changes no sine or cosine), t = j / nd in float-float.
+// Anything the FP32 error bounds leave undecided is settled with the FP64 reference-order code:
+// an ambiguous state, an undecided segment count, or an edge whose joint difference lies within
+// 1e-9 of pi (where the interpolation branch itself would be uncertain).
+#include "chain_warp.cuh"
+#include "kernels.cuh"
+#include "tma.cuh"
+
+namespace gbo
+{
+
+struct ChainSmem
+{
+    const ChainSegF32 *w32;
+    const unsigned *tab;
+    ChainTables t;
+};
+
+__device__ bool chain_setup(const SpaceParams &sp, const WorldArgs &wa, unsigned char *smem, uint64_t *bar,
+                            RunCounters *ctr, ChainSmem &cs)
+{
+    if (!stage_bulk(smem, wa.data32, wa.bytes32, bar, &ctr->timeout))
+        return false;
+    unsigned *tab = (unsigned *)(smem + wa.bytes32);
+    build_chain_tables(sp.dim, wa.n, tab, cs.t);
+    __syncthreads();
+    cs.w32 = (const ChainSegF32 *)smem;
+    cs.tab = tab;
+    return true;
+}
+
+__device__ __forceinline__ ff lane_joint(const StatesView &v, int64_t i, int lane, int dim)
+{
+    return lane < dim ? split_double(v(i, lane)) : ff{0.f, 0.f};
+}
+
+// Cold FP64 paths (reference operation order), one thread, kept out of line so that the FP32
+// kernels keep a small register footprint.
+__device__ __noinline__ void load_pair64(const StatesView &v1, const StatesView &v2, int64_t e, int dim, double *a,
+                                         double *b)
+{
+    for (int d = 0; d < GBO_MAXD; ++d)
+    {
+        a[d] = d < dim ? v1(e, d) : 0.0;
+        b[d] = d < dim ? v2(e, d) : 0.0;
+    }
+}
+
+// DiscreteMotionValidator.cpp:48-91 for one edge.
+__device__ __noinline__ void chain_motion64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v1,
+                                           const StatesView &v2, int64_t e, int &nd, int &first)
+{
+    double a[GBO_MAXD], b[GBO_MAXD];
+    load_pair64(v1, v2, e, sp.dim, a, b);
+    nd = segment_count_from_distance(sp, distance64<GBO_MAXD>(sp, a, b));
+    first = -1;
+    const int top = nd > 1 ? nd : 1;
+    for (int j = 1; j <= top; ++j)
+    {
+        double q[GBO_MAXD];
+        if (j == top)
+            for (int d = 0; d < GBO_MAXD; ++d)
+                q[d] = b[d];
+        else
+            interpolate64<GBO_MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
+        if (!chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n))
+        {
+            first = j == top ? nd : j;
+            return;
+        }
+    }
+}
+
+__device__ __noinline__ int chain_nd64(const SpaceParams &sp, const StatesView &v1, const StatesView &v2, int64_t e)
+{
+    double a[GBO_MAXD], b[GBO_MAXD];
+    load_pair64(v1, v2, e, sp.dim, a, b);
+    return segment_count_from_distance(sp, distance64<GBO_MAXD>(sp, a, b));
+}
+
+// Validity of checked state j of an edge (j == top: s2 itself) in FP64.
+__device__ __noinline__ bool chain_state64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v1,
+                                          const StatesView &v2, int64_t e, int j, int nd, int top)
+{
+    double a[GBO_MAXD], b[GBO_MAXD], q[GBO_MAXD];
+    load_pair64(v1, v2, e, sp.dim, a, b);
+    if (j == top)
+        for (int d = 0; d < GBO_MAXD; ++d)
+            q[d] = b[d];
+    else
+        interpolate64<GBO_MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
+    return chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n);
+}
+
+__device__ __noinline__ bool chain_valid_row64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v,
+                                              int64_t i)
+{
+    double q[GBO_MAXD];
+    for (int d = 0; d < GBO_MAXD; ++d)
+        q[d] = d < sp.dim ? v(i, d) : 0.0;
+    return chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n);
+}
+
+__global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v,
+                                                                  int64_t n, uint8_t *out, RunCounters *ctr)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    ChainSmem cs;
+    if (!chain_setup(sp, wa, smem, &bar, ctr, cs))
+        return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float L = (float)sp.link;
+    unsigned rechecks = 0, evaluated = 0;
+    for (int64_t i = warp; i < n; i += nwarps)
+    {
+        ++evaluated;
+        float vx, vy, px, py;
+        chain_segments32(lane_joint(v, i, lane, sp.dim), lane, sp.dim, L, vx, vy, px, py);
+        int r = chain_state_warp32(lane, vx, vy, px, py, cs.w32, cs.tab, cs.t, wa.guard);
+        if (r == kAmbiguous)
+        {
+            if (lane == 0)
+            {
+                r = chain_valid_row64(sp, wa, v, i) ? kValid : kInvalid;
+                ++rechecks;
+            }
+            r = __shfl_sync(0xffffffffu, r, 0);
+        }
+        if (lane == 0)
+            out[i] = r == kValid ? 1 : 0;
+    }
+    if (lane == 0)
+    {
+        if (evaluated)
+            atomicAdd(&ctr->evaluated, (unsigned long long)evaluated);
+        if (rechecks)
+            atomicAdd(&ctr->rechecked, (unsigned long long)rechecks);
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1,
+                                                                StatesView v2, int64_t n, uint8_t *ok,
+                                                                int32_t *first_j, int32_t *nd_out, RunCounters *ctr)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    ChainSmem cs;
+    if (!chain_setup(sp, wa, smem, &bar, ctr, cs))
+        return;
+    const int lane = threadIdx.x & 31;
+    const int dim = sp.dim;
+    const float L = (float)sp.link;
+    constexpr float kPiF = 3.14159265358979323846f;
+    unsigned evaluated = 0, rechecks = 0;
+    for (;;)
+    {
+        unsigned long long ei = 0;
+        if (lane == 0)
+            ei = atomicAdd(&ctr->queue, 1ull);
+        const int64_t e = (int64_t)__shfl_sync(0xffffffffu, ei, 0);
+        if (e >= n)
+            break;
+        const ff a = lane_joint(v1, e, lane, dim), b = lane_joint(v2, e, lane, dim);
+        // shortest-arc difference per joint; an edge whose |difference| is within 1e-9 of pi is
+        // decided entirely in FP64 (the reference's branch on fabs(diff) <= pi is not settled here)
+        ff diff = two_sum(b.hi, -a.hi);
+        diff = fast_two_sum(diff.hi, diff.lo + (b.lo - a.lo));
+        const float adh = fabsf(diff.hi);
+        const bool near_pi = lane < dim && fabsf((adh - kPiF) + (diff.hi < 0.f ? -diff.lo : diff.lo) -
+                                                 (-8.742278e-08f)) < 1e-9f;
+        int nd = -2, first = -1;
+        if (__any_sync(0xffffffffu, near_pi))
+        {
+            if (lane == 0)
+            {
+                chain_motion64(sp, wa, v1, v2, e, nd, first);
+                ++rechecks;
+            }
+            nd = __shfl_sync(0xffffffffu, nd, 0);
+            first = __shfl_sync(0xffffffffu, first, 0);
+        }
+        else
+        {
+            ff D = diff;
+            if (lane < dim && adh > kPiF)
+            {
+                // D = diff - sign(diff) * 2*pi in float-float
+                const float sgn = diff.hi > 0.f ? -1.f : 1.f;
+                const ff t1 = two_sum(diff.hi, sgn * 6.28125f);
+                const ff t2 = two_sum(t1.hi, sgn * (519505.0f / 268435456.0f));
+                D = fast_two_sum(t2.hi, (t1.lo + t2.lo) + (diff.lo + sgn * 2.4308403e-10f));
+            }
+            nd = chain_segment_count_warp(a, b, lane, dim, L, wa.inv_lvs32, wa.e_dist, sp.factor);
+            if (nd < 0)
+            {
+                if (lane == 0)
+                {
+                    nd = chain_nd64(sp, v1, v2, e);
+                    ++rechecks;
+                }
+                nd = __shfl_sync(0xffffffffu, nd, 0);
+            }
+            const int top = nd > 1 ? nd : 1;
+            // 1/nd in float-float
+            const float inv_hi = __frcp_rn((float)(nd > 0 ? nd : 1));
+            const float inv_lo = fmaf(-inv_hi, (float)(nd > 0 ? nd : 1), 1.0f) * inv_hi;
+            for (int j = 1; j <= top; ++j)
+            {
+                ff q;
+                if (j == top)
+                    q = b;
+                else
+                {
+                    const float jf = (float)j;
+                    const float t_hi = jf * inv_hi;
+                    const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
+                    const float p_hi = D.hi * t_hi;
+                    const float p_lo = fmaf(D.hi, t_hi, -p_hi) + fmaf(D.hi, t_lo, D.lo * t_hi);
+                    q = lane < dim ? ff_add(a, {p_hi, p_lo}) : ff{0.f, 0.f};
+                }
+                float vx, vy, px, py;
+                chain_segments32(q, lane, dim, L, vx, vy, px, py);
+                int r = chain_state_warp32(lane, vx, vy, px, py, cs.w32, cs.tab, cs.t, wa.guard);
+                ++evaluated;
+                if (r == kAmbiguous)
+                {
+                    if (lane == 0)
+                    {
+                        r = chain_state64(sp, wa, v1, v2, e, j, nd, top) ? kValid : kInvalid;
+                        ++rechecks;
+                    }
+                    r = __shfl_sync(0xffffffffu, r, 0);
+                }
+                if (r == kInvalid)
+                {
+                    first = j == top ? nd : j;
+                    break;
+                }
+            }
+        }
+        if (lane == 0)
+        {
+            ok[e] = first < 0 ? 1 : 0;
+            if (first_j)
+                first_j[e] = first;
+            if (nd_out)
+                nd_out[e] = nd;
+        }
+    }
+    if (lane == 0)
+    {
+        if (evaluated)
+            atomicAdd(&ctr->evaluated, (unsigned long long)evaluated);
+        if (rechecks)
+            atomicAdd(&ctr->rechecked, (unsigned long long)rechecks);
+    }
+}
+
+static unsigned chain_smem(const SpaceParams &sp, const WorldArgs &wa)
+{
+    const int m = sp.dim + 1;
+    const int n_tests = (m - 1) * (m - 2) / 2 + m * wa.n;
+    return wa.bytes32 + (unsigned)((4 * n_tests + 15) & ~15);
+}
+
+bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
+                                int64_t n, uint8_t *out, RunCounters *ctr)
+{
+    if (sp.dim > 31 || !wa.stage32)
+        return false;
+    const unsigned sm = chain_smem(sp, wa);
+    const int grid = persistent_grid((const void *)chain_validity_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
+    chain_validity_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v, n, out, ctr);
+    note_launch();
+    return true;
+}
+
+bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v1,
+                              StatesView v2, int64_t n, uint8_t *ok, int32_t *fj, int32_t *nd, RunCounters *ctr)
+{
+    if (sp.dim > 31 || !wa.stage32)
+        return false;
+    const unsigned sm = chain_smem(sp, wa);
+    const int grid = persistent_grid((const void *)chain_motion_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
+    chain_motion_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v1, v2, n, ok, fj, nd, ctr);
+    note_launch();
+    return true;
+}
+
+}  // namespace gbo

@@ -604,12 +604,18 @@ static void launch_chain_t(const LaunchCfg &lc, const SpaceParams &sp, const Wor
 void launch_validity(const LaunchCfg &lc, int precision, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
                      int64_t n, uint8_t *out, RunCounters *ctr)
 {
+    if (wa.kind == GBO_CHECK_CHAIN_SEGMENTS && precision == GBO_PRECISION_FP32_GUARDED &&
+        launch_chain_validity_warp(lc, sp, wa, v, n, out, ctr))
+        return;
     GBO_DISPATCH(wa.kind, sp.dim, precision, (launch_validity_t<CK, MAXD, PREC>(lc, sp, wa, v, n, out, ctr)));
 }
 
 void launch_motion(const LaunchCfg &lc, int precision, int schedule, const SpaceParams &sp, const WorldArgs &wa,
                    StatesView v1, StatesView v2, int64_t n, uint8_t *ok, int32_t *fj, int32_t *nd, RunCounters *ctr)
 {
+    if (wa.kind == GBO_CHECK_CHAIN_SEGMENTS && precision == GBO_PRECISION_FP32_GUARDED &&
+        schedule == GBO_SCHEDULE_WARP && launch_chain_motion_warp(lc, sp, wa, v1, v2, n, ok, fj, nd, ctr))
+        return;
     GBO_DISPATCH(wa.kind, sp.dim, precision,
                  (launch_motion_t<CK, MAXD, PREC>(lc, schedule, sp, wa, v1, v2, n, ok, fj, nd, ctr)));
 }
