@@ -174,6 +174,9 @@ gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, doub
 
 /* ---- measurement helper ---- FP32 FMA throughput of this GPU (FLOP/s), for roofline denominators. */
 gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
+/* The FP32 cos/sin of the guarded kinematic-chain path for n FP64 angles (device arrays); exposed so
+ * that its stated error bound (1.3e-7 per component, |angle| < 100) can be tested against FP64. */
+gbo_status gbo_sincos32(const double *theta, int64_t n, float *cos_out, float *sin_out, gbo_stream stream);
 /* FP64 FMA throughput of this GPU (FLOP/s). */
 gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
 /* Number of kernels this library launched since load (for launch accounting). */

@@ -63,6 +63,7 @@ SIGNATURES = {
     "gbo_sample_uniform_near_host": (C.c_int, [_P, _P, C.c_double, _I64, _P]),
     "gbo_measure_fp32_peak": (C.c_int, [_D, _P]),
     "gbo_measure_fp64_peak": (C.c_int, [_D, _P]),
+    "gbo_sincos32": (C.c_int, [_P, _I64, _P, _P, _P]),
     "gbo_launch_count": (C.c_uint64, []),
 }
 

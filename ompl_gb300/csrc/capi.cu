@@ -78,6 +78,9 @@ LaunchCfg lcfg(gbo_stream s)
 }
 
 constexpr double kU32 = 5.9604644775390625e-08;  // 2^-24, FP32 unit roundoff
+// Bound on |cos/sin FP32 - exact| of one link direction (sincos_ff, chain_warp.cuh): Horner rounding
+// <= 2 ulp (1.2e-7), Taylor truncation <= 2e-9, reduction and low-part terms < 1e-12.
+constexpr double kEpsDir = 1.3e-7;
 constexpr double kPiH = 3.141592653589793238462643383279502884;
 
 bool valid_layout(int layout, int64_t n, int64_t ld, int dim)
@@ -305,7 +308,7 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
                   float &e_dist)
 {
     const double u = kU32, L = sp.link, nl = sp.dim;
-    const double eps_dir = kU32 * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+    const double eps_dir = kEpsDir;
     const double R = nl * L + 0.001;
     const double dV = L * (eps_dir + 2 * u) + 1e-15;
     const double dP = (nl + 1) * (L * (eps_dir + u) + u * R) + 1e-15;
@@ -361,7 +364,7 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
 float chain_knn_eps(const SpaceParams &sp)
 {
     const double u = kU32, L = sp.link;
-    const double eps_dir = kU32 * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+    const double eps_dir = kEpsDir;
     double e = 0.0;
     for (int i = 1; i <= sp.dim; ++i)
     {
@@ -1383,6 +1386,17 @@ gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream)
     if (auto st = ensure_device())
         return st;
     *flops = measure_fp32_peak(lcfg(stream));
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+gbo_status gbo_sincos32(const double *theta, int64_t n, float *cos_out, float *sin_out, gbo_stream stream)
+{
+    if (n < 0 || (n > 0 && (!theta || !cos_out || !sin_out)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sincos32 arguments");
+    if (auto st = ensure_device())
+        return st;
+    launch_sincos32(lcfg(stream), theta, n, cos_out, sin_out);
     CHECK_LAUNCH();
     return GBO_OK;
 }

@@ -1,0 +1,131 @@
+// Warp-cooperative kinematic-chain state test (uses the guarded segment test of checkers.cuh and
+// the FP32 arithmetic of chain_warp.cuh).
+#pragma once
+#include "checkers.cuh"
+
+namespace gbo
+{
+
+// Per-CTA test tables: tests [0, n_self) are link-link pairs (a, b), tests [n_self, n_self + 11*W)
+// link-world pairs; entry = a | (b << 8) for self pairs and link | (world << 8) otherwise.
+struct ChainTables
+{
+    int n_self;
+    int n_tests;
+};
+
+__device__ __forceinline__ void build_chain_tables(int n_links, int nw, unsigned *tab, ChainTables &t)
+{
+    const int m = n_links + 1;  // segments incl. the tip
+    int n_self = 0;
+    for (int i = 0; i < m; ++i)
+        for (int j = i + 2; j < m; ++j)
+            ++n_self;
+    t.n_self = n_self;
+    t.n_tests = n_self + m * nw;
+    for (int idx = threadIdx.x; idx < t.n_tests; idx += blockDim.x)
+    {
+        unsigned e;
+        if (idx < n_self)
+        {
+            int r = idx, i = 0;
+            while (r >= m - (i + 2))
+            {
+                r -= m - (i + 2);
+                ++i;
+            }
+            e = (unsigned)i | ((unsigned)(i + 2 + r) << 8);
+        }
+        else
+        {
+            const int r = idx - n_self;
+            e = (unsigned)(r % m) | ((unsigned)(r / m) << 8);  // world-major: 11 links of a segment adjacent
+        }
+        tab[idx] = e;
+    }
+}
+
+// Link directions of one state: lane k < n holds joint k as float-float (zero elsewhere).
+// Returns, in lane k <= n, the segment vector V_k and start point P_k (lane n = tip segment).
+__device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L, float &vx, float &vy, float &px,
+                                                 float &py)
+{
+    float c, s;
+    sincos_ff(warp_scan_ff(q, lane), c, s);
+    // tip segment (lane n) uses the last link's direction with length 0.001
+    const float cl = __shfl_sync(0xffffffffu, c, n > 0 ? n - 1 : 0);
+    const float sl = __shfl_sync(0xffffffffu, s, n > 0 ? n - 1 : 0);
+    const bool tip = lane == n;
+    vx = lane < n ? c * L : (tip ? cl * 0.001f : 0.f);
+    vy = lane < n ? s * L : (tip ? sl * 0.001f : 0.f);
+    // end point of segment k = sum_{m<=k} V_m ; start point = end point of segment k-1
+    const float ex = warp_scan_f(vx, lane), ey = warp_scan_f(vy, lane);
+    px = __shfl_up_sync(0xffffffffu, ex, 1);
+    py = __shfl_up_sync(0xffffffffu, ey, 1);
+    if (lane == 0)
+    {
+        px = 0.f;
+        py = 0.f;
+    }
+}
+
+// Warp-cooperative guarded state test. Returns kInvalid, kValid or kAmbiguous (same in all lanes).
+__device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, float px, float py,
+                                                  const ChainSegF32 *w, const unsigned *tab, const ChainTables &t,
+                                                  const ChainGuard &g)
+{
+    bool amb = false;
+    for (int base = 0; base < t.n_tests; base += 32)
+    {
+        const int idx = base + lane;
+        int r = kValid;
+        const unsigned e = idx < t.n_tests ? tab[idx] : 0u;
+        const int a = (int)(e & 0xff), b = (int)(e >> 8);
+        const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
+        const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
+        const bool self = idx < t.n_self;
+        const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
+        const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
+        if (idx < t.n_tests)
+        {
+            if (self)
+                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_den, g.self_s, g.self_t, g.self_u,
+                                    g.self_v);
+            else
+            {
+                const ChainSegF32 ws = w[b];
+                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.e_den, ws.e_s, ws.e_t, ws.e_u,
+                                    ws.e_v);
+            }
+        }
+        if (__any_sync(0xffffffffu, r == kInvalid))
+            return kInvalid;
+        amb |= __any_sync(0xffffffffu, r == kAmbiguous);
+    }
+    return amb ? kAmbiguous : kValid;
+}
+
+// Workspace distance of two states (lane k < n holds joint k of each) and the FP32 segment count.
+// Returns the segment count, or -1 when ceil(distance / lvs) is not decided by the error bound.
+__device__ __forceinline__ int chain_segment_count_warp(ff qa, ff qb, int lane, int n, float L, float inv_lvs,
+                                                        float e_dist, unsigned factor)
+{
+    float c1, s1, c2, s2;
+    sincos_ff(warp_scan_ff(qa, lane), c1, s1);
+    sincos_ff(warp_scan_ff(qb, lane), c2, s2);
+    const float dx = warp_scan_f(lane < n ? c1 - c2 : 0.f, lane);
+    const float dy = warp_scan_f(lane < n ? s1 - s2 : 0.f, lane);
+    const float dist = warp_sum_f(lane < n ? sqrtf(fmaf(dx, dx, dy * dy)) : 0.f) * L;
+    const float lo = (dist - e_dist) * inv_lvs * (1.0f - 4.0f * 5.96e-8f);
+    const float hi = (dist + e_dist) * inv_lvs * (1.0f + 4.0f * 5.96e-8f);
+    if (!(lo > 0.f) || !(hi < 4.0e6f))
+        return -1;
+    float cl = rint_add(lo), ch = rint_add(hi);
+    cl += cl < lo ? 1.f : 0.f;  // ceil
+    ch += ch < hi ? 1.f : 0.f;
+    if (cl == ch)
+        return (int)(factor * (unsigned)int_of(cl));
+    return -1;
+}
+
+}  // namespace gbo

@@ -10,7 +10,7 @@
 // then world segments; a round with a definite intersection ends the evaluation (ballot). Every
 // comparison is classified with the error bounds of the guarded FP32 test (checkers.cuh).
 #pragma once
-#include "checkers.cuh"
+#include "common.cuh"
 
 namespace gbo
 {
@@ -39,8 +39,9 @@ __device__ __forceinline__ ff ff_add(ff a, ff b)
     return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
 
-// Exact split of a double into hi + lo floats using integer operations only (|x| >= 2^-100 or 0;
-// smaller magnitudes become 0). hi keeps the top 24 significand bits, lo the next 24.
+// Exact split of a double into hi + lo floats with integer operations only (no conversion
+// instruction): hi keeps the top 24 significand bits, lo the next 24 (the last 5 of the 53 are
+// truncated, relative error 2^-48). |x| < 2^-74 keeps hi only; |x| < 2^-100 becomes 0.
 __device__ __forceinline__ ff split_double(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -50,30 +51,72 @@ __device__ __forceinline__ ff split_double(double x)
         return {0.f, 0.f};
     const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
     const float hi = __int_as_float((int)(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29)));
-    const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);                    // 29 low bits, weight 2^(e-52)
-    const float lo_abs = e >= -74 ? __uint2float_rz(rem) * __int_as_float((e - 52 + 127) << 23) : 0.f;
-    return {hi, sign ? -lo_abs : lo_abs};
+    const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);  // 29 low bits, weight 2^(e-52)
+    float lo = 0.f;
+    if (rem != 0u && e >= -74)
+    {
+        const int lz = __clz(rem);                        // >= 3
+        const int p = 31 - lz;                            // position of the leading bit
+        const unsigned mant = p >= 23 ? rem >> (p - 23) : rem << (23 - p);
+        lo = __int_as_float((int)(sign | ((unsigned)(p + e - 52 + 127) << 23) | (mant & 0x7FFFFFu)));
+    }
+    return {hi, lo};
 }
 
-// 2*pi = C1 + C2 + C3: C1 has 8 significant bits and C2 20, so k*C1 and k*C2 are exact for |k| < 2^11.
-__device__ __forceinline__ ff reduce_2pi(ff t)
+// Round to the nearest integer for |x| < 2^22 in the FP32 adder (no rounding instruction).
+__device__ __forceinline__ float rint_add(float x)
 {
-    constexpr float C1 = 6.28125f;
-    constexpr float C2 = 519505.0f / 268435456.0f;         // 2*pi - C1 rounded to 20 bits (exact)
-    constexpr float C3 = 2.4308403e-10f;                   // 2*pi - C1 - C2 (residual ~5e-18)
-    const float k = rintf(t.hi * 0.15915494309189535f);
-    const float r1 = fmaf(-k, C1, t.hi);                   // exact
-    const ff s = two_sum(r1, -k * C2);                      // k*C2 exact
-    return fast_two_sum(s.hi, s.lo + fmaf(-k, C3, t.lo));
+    return (x + 12582912.0f) - 12582912.0f;
 }
 
-// cos/sin of a reduced float-float angle: sincosf(hi) corrected to first order in lo.
-__device__ __forceinline__ void sincos_ff(ff r, float &c, float &s)
+// Non-negative integer value of a float that holds an integer below 2^22.
+__device__ __forceinline__ int int_of(float x)
 {
-    float s0, c0;
-    sincosf(r.hi, &s0, &c0);
-    c = fmaf(-s0, r.lo, c0);
-    s = fmaf(c0, r.lo, s0);
+    return __float_as_int(x + 12582912.0f) - 0x4B400000;
+}
+
+// Float of a non-negative integer below 2^23.
+__device__ __forceinline__ float float_of(int i)
+{
+    return __int_as_float(0x4B000000 | i) - 8388608.0f;
+}
+
+// cos and sin of a float-float angle |t| < 64*pi/2 in FP32 arithmetic only.
+// Reduction: k = nearest integer to t*2/pi, y = t - k*pi/2 with pi/2 = P1 + P2 + P3 (P1 8 and P2 18
+// significant bits, so k*P1 and k*P2 are exact for |k| < 64; residual of the split ~6e-18).
+// On |y| <= pi/4, Taylor polynomials of sin (to y^9) and cos (to y^10), truncation <= 2e-9,
+// evaluated by Horner with FMA (rounding <= 2 FP32 ulp); the low part of y enters to first order.
+// |result - exact| <= 1.3e-7 per component.
+__device__ __forceinline__ void sincos_ff(ff t, float &c, float &s)
+{
+    constexpr float P1 = 1.5703125f;
+    constexpr float P2 = 259753.0f / 536870912.0f;
+    constexpr float P3 = -8.705516e-10f;
+    const float m = fmaf(t.hi, 0.63661975f, 12582912.0f);
+    const float k = m - 12582912.0f;
+    const int q = __float_as_int(m) & 3;
+    const float y1 = fmaf(-k, P1, t.hi);  // exact
+    const ff sy = two_sum(y1, -k * P2);   // k*P2 exact
+    const ff y = fast_two_sum(sy.hi, sy.lo + fmaf(-k, P3, t.lo));
+    const float x = y.hi, x2 = x * x;
+    float sp = fmaf(x2, 2.7557319e-06f, -1.984127e-04f);
+    sp = fmaf(sp, x2, 8.333334e-03f);
+    sp = fmaf(sp, x2, -0.16666667f);
+    const float sn = fmaf(sp * x2, x, x);
+    float cp = fmaf(x2, -2.755732e-07f, 2.4801588e-05f);
+    cp = fmaf(cp, x2, -1.3888889e-03f);
+    cp = fmaf(cp, x2, 4.1666668e-02f);
+    cp = fmaf(cp, x2, -0.5f);
+    const float cs = fmaf(cp, x2, 1.0f);
+    const float s1 = fmaf(cs, y.lo, sn), c1 = fmaf(-sn, y.lo, cs);
+    float so = (q & 1) ? c1 : s1;
+    float co = (q & 1) ? s1 : c1;
+    if (q & 2)
+        so = -so;
+    if ((q + 1) & 2)
+        co = -co;
+    s = so;
+    c = co;
 }
 
 // Inclusive warp scan of a float-float value over lanes [0, 32).
@@ -108,125 +151,6 @@ __device__ __forceinline__ float warp_sum_f(float v)
     for (int o = 16; o > 0; o >>= 1)
         v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// Per-CTA test tables: tests [0, n_self) are link-link pairs (a, b), tests [n_self, n_self + 11*W)
-// link-world pairs; entry = a | (b << 8) for self pairs and link | (world << 8) otherwise.
-struct ChainTables
-{
-    int n_self;
-    int n_tests;
-};
-
-__device__ __forceinline__ void build_chain_tables(int n_links, int nw, unsigned *tab, ChainTables &t)
-{
-    const int m = n_links + 1;  // segments incl. the tip
-    int n_self = 0;
-    for (int i = 0; i < m; ++i)
-        for (int j = i + 2; j < m; ++j)
-            ++n_self;
-    t.n_self = n_self;
-    t.n_tests = n_self + m * nw;
-    for (int idx = threadIdx.x; idx < t.n_tests; idx += blockDim.x)
-    {
-        unsigned e;
-        if (idx < n_self)
-        {
-            int r = idx, i = 0;
-            while (r >= m - (i + 2))
-            {
-                r -= m - (i + 2);
-                ++i;
-            }
-            e = (unsigned)i | ((unsigned)(i + 2 + r) << 8);
-        }
-        else
-        {
-            const int r = idx - n_self;
-            e = (unsigned)(r % m) | ((unsigned)(r / m) << 8);  // world-major: 11 links of a segment adjacent
-        }
-        tab[idx] = e;
-    }
-}
-
-// Link directions of one state: lane k < n holds joint k as float-float (zero elsewhere).
-// Returns, in lane k <= n, the segment vector V_k and start point P_k (lane n = tip segment).
-__device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L, float &vx, float &vy, float &px,
-                                                 float &py)
-{
-    const ff th = reduce_2pi(warp_scan_ff(q, lane));
-    float c, s;
-    sincos_ff(th, c, s);
-    // tip segment (lane n) uses the last link's direction with length 0.001
-    const float cl = __shfl_sync(0xffffffffu, c, n > 0 ? n - 1 : 0);
-    const float sl = __shfl_sync(0xffffffffu, s, n > 0 ? n - 1 : 0);
-    const bool tip = lane == n;
-    vx = lane < n ? c * L : (tip ? cl * 0.001f : 0.f);
-    vy = lane < n ? s * L : (tip ? sl * 0.001f : 0.f);
-    // end point of segment k = sum_{m<=k} V_m ; start point = end point of segment k-1
-    const float ex = warp_scan_f(vx, lane), ey = warp_scan_f(vy, lane);
-    px = __shfl_up_sync(0xffffffffu, ex, 1);
-    py = __shfl_up_sync(0xffffffffu, ey, 1);
-    if (lane == 0)
-    {
-        px = 0.f;
-        py = 0.f;
-    }
-}
-
-// Warp-cooperative guarded state test. Returns kInvalid, kValid or kAmbiguous (same in all lanes).
-__device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, float px, float py,
-                                                  const ChainSegF32 *w, const unsigned *tab, const ChainTables &t,
-                                                  const ChainGuard &g)
-{
-    bool amb = false;
-    for (int base = 0; base < t.n_tests; base += 32)
-    {
-        const int idx = base + lane;
-        int r = kValid;
-        const unsigned e = idx < t.n_tests ? tab[idx] : 0u;
-        const int a = (int)(e & 0xff), b = (int)(e >> 8);
-        const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
-        const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
-        const bool self = idx < t.n_self;
-        const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
-        const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
-        if (idx < t.n_tests)
-        {
-            if (self)
-                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_den, g.self_s, g.self_t, g.self_u,
-                                    g.self_v);
-            else
-            {
-                const ChainSegF32 ws = w[b];
-                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.e_den, ws.e_s, ws.e_t, ws.e_u,
-                                    ws.e_v);
-            }
-        }
-        if (__any_sync(0xffffffffu, r == kInvalid))
-            return kInvalid;
-        amb |= __any_sync(0xffffffffu, r == kAmbiguous);
-    }
-    return amb ? kAmbiguous : kValid;
-}
-
-// Workspace distance of two states (lane k < n holds joint k of each) and the FP32 segment count.
-// Returns the segment count, or -1 when ceil(distance / lvs) is not decided by the error bound.
-__device__ __forceinline__ int chain_segment_count_warp(ff qa, ff qb, int lane, int n, float L, float inv_lvs,
-                                                        float e_dist, unsigned factor)
-{
-    float c1, s1, c2, s2;
-    sincos_ff(reduce_2pi(warp_scan_ff(qa, lane)), c1, s1);
-    sincos_ff(reduce_2pi(warp_scan_ff(qb, lane)), c2, s2);
-    const float dx = warp_scan_f(lane < n ? c1 - c2 : 0.f, lane);
-    const float dy = warp_scan_f(lane < n ? s1 - s2 : 0.f, lane);
-    const float dist = warp_sum_f(lane < n ? sqrtf(fmaf(dx, dx, dy * dy)) : 0.f) * L;
-    const float lo = (dist - e_dist) * inv_lvs * (1.0f - 4.0f * 5.96e-8f);
-    const float hi = (dist + e_dist) * inv_lvs * (1.0f + 4.0f * 5.96e-8f);
-    const float cl = ceilf(lo), ch = ceilf(hi);
-    if (cl == ch && lo > 0.f)
-        return (int)(factor * (unsigned)cl);
-    return -1;
 }
 
 }  // namespace gbo

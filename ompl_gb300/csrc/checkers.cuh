@@ -11,6 +11,7 @@
 // re-evaluated with the FP64 form, so the returned boolean always equals the FP64 one.
 #pragma once
 #include "common.cuh"
+#include "chain_warp.cuh"
 
 namespace gbo
 {
@@ -170,13 +171,11 @@ __device__ __forceinline__ int seg_intersect32(float s10x, float s10y, float s32
     return (S == 2 || T == 2 || U == 2 || V == 2) ? kAmbiguous : kInvalid;
 }
 
-// FP32 link directions: theta accumulated in FP64 exactly as the reference, reduced to [-pi, pi]
-// and evaluated with FP32 sincos. |error| <= guard.eps_dir per component.
+// FP32 link directions from an FP64 angle (thread-per-state forms): the angle is split exactly into
+// a float-float pair and evaluated with sincos_ff (chain_warp.cuh); |error| <= 1.3e-7 per component.
 __device__ __forceinline__ void dir32(double theta, float &c, float &s)
 {
-    double k = rint(theta * (1.0 / kTwoPi));
-    double r = fma(-k, kTwoPi, theta);
-    sincosf((float)r, &s, &c);
+    sincos_ff(split_double(theta), c, s);
 }
 
 template <int MAXD>

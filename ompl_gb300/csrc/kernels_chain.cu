@@ -10,7 +10,7 @@
 // Anything the FP32 error bounds leave undecided is settled with the FP64 reference-order code:
 // an ambiguous state, an undecided segment count, or an edge whose joint difference lies within
 // 1e-9 of pi (where the interpolation branch itself would be uncertain).
-#include "chain_warp.cuh"
+#include "chain_state.cuh"
 #include "kernels.cuh"
 #include "tma.cuh"
 
@@ -213,16 +213,18 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
             }
             const int top = nd > 1 ? nd : 1;
             // 1/nd in float-float
-            const float inv_hi = __frcp_rn((float)(nd > 0 ? nd : 1));
-            const float inv_lo = fmaf(-inv_hi, (float)(nd > 0 ? nd : 1), 1.0f) * inv_hi;
+            const float ndf = float_of(nd > 0 ? nd : 1);
+            const float inv_hi = __frcp_rn(ndf);
+            const float inv_lo = fmaf(-inv_hi, ndf, 1.0f) * inv_hi;
+            float jf = 0.f;
             for (int j = 1; j <= top; ++j)
             {
+                jf += 1.0f;
                 ff q;
                 if (j == top)
                     q = b;
                 else
                 {
-                    const float jf = (float)j;
                     const float t_hi = jf * inv_hi;
                     const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
                     const float p_hi = D.hi * t_hi;

@@ -40,5 +40,6 @@ void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpacePar
                            StatesView nearv, double distance, int64_t n, MutStatesView out);
 double measure_fp32_peak(const LaunchCfg &lc);
 double measure_fp64_peak(const LaunchCfg &lc);
+void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s);
 
 }  // namespace gbo

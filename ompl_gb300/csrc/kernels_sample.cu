@@ -212,6 +212,21 @@ __global__ void __launch_bounds__(256) fma_peak_kernel(float *sink, int iters, f
         sink[0] = r;
 }
 
+__global__ void sincos32_kernel(const double *theta, int64_t n, float *c, float *s)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        sincos_ff(split_double(theta[i]), c[i], s[i]);
+}
+
+void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s)
+{
+    if (n == 0)
+        return;
+    sincos32_kernel<<<(int)((n + 255) / 256), 256, 0, lc.stream>>>(theta, n, c, s);
+    note_launch();
+}
+
 __global__ void __launch_bounds__(256) dfma_peak_kernel(double *sink, int iters, double seed)
 {
     double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;

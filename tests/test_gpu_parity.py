@@ -61,6 +61,21 @@ def ulp_close(a, b, rel=1e-12):
     return bool(np.all(both_nan | (diff <= tol) | (a == b)))
 
 
+# ------------------------------------------------------------------ FP32 arithmetic error bounds
+def test_fp32_sincos_error_bound():
+    """The guard band of the FP32 chain path assumes |cos/sin error| <= 1.3e-7 per component."""
+    rng = np.random.default_rng(8)
+    th = np.concatenate([rng.uniform(-35, 35, 2_000_000), np.linspace(-35, 35, 200_001),
+                         np.arange(-22, 23) * (math.pi / 4), np.array([0.0, 1e-30, -1e-20, 5e-9])])
+    t = torch.as_tensor(th, device="cuda")
+    c = torch.empty(len(th), dtype=torch.float32, device="cuda")
+    s = torch.empty_like(c)
+    capi.check(capi.lib().gbo_sincos32(B._ptr(t), len(th), B._ptr(c), B._ptr(s), B._stream(None)))
+    ec = np.abs(c.cpu().numpy().astype(np.float64) - np.cos(th)).max()
+    es = np.abs(s.cpu().numpy().astype(np.float64) - np.sin(th)).max()
+    assert ec <= 1.3e-7 and es <= 1.3e-7, (ec, es)
+
+
 # ------------------------------------------------------------------ spaces and samplers
 @pytest.mark.parametrize("name", ["rv2", "rv7", "so2", "chain10", "wrap7"])
 def test_space_distance_interpolate_vs_ompl(golden, name):
