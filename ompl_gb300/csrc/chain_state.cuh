@@ -6,43 +6,50 @@
 namespace gbo
 {
 
-// Per-CTA test tables: tests [0, n_self) are link-link pairs (a, b), tests [n_self, n_self + 11*W)
-// link-world pairs; entry = a | (b << 8) for self pairs and link | (world << 8) otherwise.
+// Per-CTA test tables: one entry per segment test, a | (b << 8) with bit 31 set for a link-link pair
+// (a, b) and clear for link a vs world segment b.
 struct ChainTables
 {
     int n_self;
     int n_tests;
 };
 
-__device__ __forceinline__ void build_chain_tables(int n_links, int nw, unsigned *tab, ChainTables &t)
+__device__ __forceinline__ int chain_test_count(int n_links, int nw, int &n_self)
 {
     const int m = n_links + 1;  // segments incl. the tip
-    int n_self = 0;
-    for (int i = 0; i < m; ++i)
-        for (int j = i + 2; j < m; ++j)
-            ++n_self;
-    t.n_self = n_self;
-    t.n_tests = n_self + m * nw;
-    for (int idx = threadIdx.x; idx < t.n_tests; idx += blockDim.x)
+    n_self = (m - 1) * (m - 2) / 2;
+    return n_self + m * nw;
+}
+
+// Default order: self pairs row by row, then world-major link-world pairs.
+__host__ __device__ inline unsigned chain_test_entry(int idx, int n_links, int nw)
+{
+    const int m = n_links + 1;
+    const int n_self = (m - 1) * (m - 2) / 2;
+    if (idx < n_self)
     {
-        unsigned e;
-        if (idx < n_self)
+        int r = idx, i = 0;
+        while (r >= m - (i + 2))
         {
-            int r = idx, i = 0;
-            while (r >= m - (i + 2))
-            {
-                r -= m - (i + 2);
-                ++i;
-            }
-            e = (unsigned)i | ((unsigned)(i + 2 + r) << 8);
+            r -= m - (i + 2);
+            ++i;
         }
-        else
-        {
-            const int r = idx - n_self;
-            e = (unsigned)(r % m) | ((unsigned)(r / m) << 8);  // world-major: 11 links of a segment adjacent
-        }
-        tab[idx] = e;
+        return (unsigned)i | ((unsigned)(i + 2 + r) << 8) | 0x80000000u;
     }
+    const int r = idx - n_self;
+    return (unsigned)(r % m) | ((unsigned)(r / m) << 8);
+}
+
+// Tables in shared memory: `order` (device, optional) is a permutation of the default entries chosen
+// on the host so that likely intersections come first (bit 31 marks a link-link pair).
+__device__ __forceinline__ void build_chain_tables(int n_links, int nw, const unsigned *order, unsigned *tab,
+                                                   ChainTables &t)
+{
+    int n_self;
+    t.n_tests = chain_test_count(n_links, nw, n_self);
+    t.n_self = n_self;
+    for (int idx = threadIdx.x; idx < t.n_tests; idx += blockDim.x)
+        tab[idx] = order ? order[idx] : chain_test_entry(idx, n_links, nw);
 }
 
 // Link directions of one state: lane k < n holds joint k as float-float (zero elsewhere).
@@ -80,10 +87,10 @@ __device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, 
         const int idx = base + lane;
         int r = kValid;
         const unsigned e = idx < t.n_tests ? tab[idx] : 0u;
-        const int a = (int)(e & 0xff), b = (int)(e >> 8);
+        const int a = (int)(e & 0xff), b = (int)((e >> 8) & 0xffffff);
         const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
         const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
-        const bool self = idx < t.n_self;
+        const bool self = (e & 0x80000000u) != 0u;
         const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
         const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
         if (idx < t.n_tests)
@@ -103,6 +110,39 @@ __device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, 
         amb |= __any_sync(0xffffffffu, r == kAmbiguous);
     }
     return amb ? kAmbiguous : kValid;
+}
+
+// Definite-intersection bitmap of one state over all tests in default order (no early exit).
+__device__ __forceinline__ void chain_state_hits32(int lane, float vx, float vy, float px, float py,
+                                                   const ChainSegF32 *w, int n_links, int nw, int n_tests,
+                                                   const ChainGuard &g, unsigned *bits)
+{
+    for (int base = 0; base < n_tests; base += 32)
+    {
+        const int idx = base + lane;
+        const unsigned e = idx < n_tests ? chain_test_entry(idx, n_links, nw) : 0u;
+        const int a = (int)(e & 0xff), b = (int)((e >> 8) & 0xffffff);
+        const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
+        const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
+        const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
+        const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
+        int r = kValid;
+        if (idx < n_tests)
+        {
+            if (e & 0x80000000u)
+                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_den, g.self_s, g.self_t, g.self_u,
+                                    g.self_v);
+            else
+            {
+                const ChainSegF32 ws = w[b];
+                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.e_den, ws.e_s, ws.e_t, ws.e_u,
+                                    ws.e_v);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, r == kInvalid);
+        if (lane == 0)
+            bits[base / 32] = m;
+    }
 }
 
 // Workspace distance of two states (lane k < n holds joint k of each) and the FP32 segment count.

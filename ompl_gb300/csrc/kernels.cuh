@@ -48,6 +48,7 @@ struct WorldArgs
     float glo[3], ginv[3];
     double glo64[3], ginv64[3];
     float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere test near contact
+    const unsigned *test_order;  // kinematic chain: segment-test order (likely intersections first)
 };
 
 struct LaunchCfg
@@ -68,6 +69,8 @@ void launch_states_chain(const LaunchCfg &lc, const SpaceParams &sp, const World
                          unsigned long long *first, RunCounters *ctr);
 void launch_last_valid(const LaunchCfg &lc, const SpaceParams &sp, StatesView v1, StatesView v2, const int32_t *fj,
                        const int32_t *nd, int64_t n, double *last_t, MutStatesView out);
+void launch_chain_hits(cudaStream_t s, const SpaceParams &sp, const WorldArgs &wa, const double *states, int n,
+                       unsigned *bits, int words);
 bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
                                 int64_t n, uint8_t *out, RunCounters *ctr);
 bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v1,

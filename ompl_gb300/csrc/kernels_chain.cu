@@ -30,7 +30,7 @@ __device__ bool chain_setup(const SpaceParams &sp, const WorldArgs &wa, unsigned
     if (!stage_bulk(smem, wa.data32, wa.bytes32, bar, &ctr->timeout))
         return false;
     unsigned *tab = (unsigned *)(smem + wa.bytes32);
-    build_chain_tables(sp.dim, wa.n, tab, cs.t);
+    build_chain_tables(sp.dim, wa.n, wa.test_order, tab, cs.t);
     __syncthreads();
     cs.w32 = (const ChainSegF32 *)smem;
     cs.tab = tab;
@@ -267,6 +267,42 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
         if (rechecks)
             atomicAdd(&ctr->rechecked, (unsigned long long)rechecks);
     }
+}
+
+// Hit bitmaps of n states (SoA FP64, ld = n) for the host's test ordering: one warp per state.
+__global__ void __launch_bounds__(256) chain_hits_kernel(SpaceParams sp, WorldArgs wa, const double *states, int n,
+                                                         unsigned *bits, int words)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    RunCounters *none = nullptr;
+    (void)none;
+    __shared__ unsigned timeout;
+    if (threadIdx.x == 0)
+        timeout = 0;
+    __syncthreads();
+    if (!stage_bulk(smem, wa.data32, wa.bytes32, &bar, &timeout))
+        return;
+    const ChainSegF32 *w = (const ChainSegF32 *)smem;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    int n_self;
+    const int n_tests = chain_test_count(sp.dim, wa.n, n_self);
+    StatesView v{states, 1, (int64_t)n};
+    for (int i = warp; i < n; i += nwarps)
+    {
+        float vx, vy, px, py;
+        chain_segments32(lane_joint(v, i, lane, sp.dim), lane, sp.dim, (float)sp.link, vx, vy, px, py);
+        chain_state_hits32(lane, vx, vy, px, py, w, sp.dim, wa.n, n_tests, wa.guard, bits + (size_t)i * words);
+    }
+}
+
+void launch_chain_hits(cudaStream_t s, const SpaceParams &sp, const WorldArgs &wa, const double *states, int n,
+                       unsigned *bits, int words)
+{
+    chain_hits_kernel<<<64, 256, wa.bytes32, s>>>(sp, wa, states, n, bits, words);
+    note_launch();
 }
 
 static unsigned chain_smem(const SpaceParams &sp, const WorldArgs &wa)
