@@ -161,6 +161,17 @@ gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_
                                  const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream);
 gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks);
 
+/* nearestK exactly as gbo_nn_nearest_k, but the call allocates no device memory (no counterpart in
+ * OMPL). For callers that cannot allocate once set up: work captured into CUDA graphs, real-time
+ * planning loops, processes whose GPU memory belongs to another allocator's pool. Scratch comes from
+ * one fixed 16 MiB device array inside the library (held on every GPU that loads it until exit);
+ * batches that do not fit are rejected with GBO_ERR_OUT_OF_MEMORY (about 44,000 queries for the
+ * kinematic-chain metric, more for box spaces). The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and must come before any stream capture; every call shares the array, so
+ * calls that overlap on the GPU race. */
+gbo_status gbo_nn_nearest_k_noalloc(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
+                                    const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream);
+
 /* Host-memory drop-ins for NearestNeighbors<T> (AoS rows; synchronous). nearest_r_host answers one
  * query: at most `cap` results are written, *count receives the full count. */
 gbo_status gbo_nn_add_host(gbo_nn *nn, const double *states, int64_t n, int64_t *first_key);

@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbo_nn_nearest_r_count": (C.c_int, [_P, _P, _I64, _I64, C.c_int, C.c_double, _P, _P]),
     "gbo_nn_nearest_r_fill": (C.c_int, [_P, _P, _I64, _I64, C.c_int, C.c_double, _P, _P, _P, _P]),
     "gbo_nn_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "gbo_nn_nearest_k_noalloc": (C.c_int, [_P, _P, _I64, _I64, C.c_int, C.c_int, _P, _P, _P, _P]),
     "gbo_nn_add_host": (C.c_int, [_P, _P, _I64, C.POINTER(_I64)]),
     "gbo_nn_remove_host": (C.c_int, [_P, _P, _I64]),
     "gbo_nn_nearest_k_host": (C.c_int, [_P, _P, _I64, C.c_int, _P, _P]),

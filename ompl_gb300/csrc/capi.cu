@@ -1501,3 +1501,31 @@ gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- internal accessors (noalloc.cu)
+namespace gbo
+{
+gbo_status internal_fail(gbo_status s, const char *msg)
+{
+    return fail(s, msg);
+}
+
+gbo_status internal_ensure_device(int *sm_count)
+{
+    if (auto st = ensure_device())
+        return st;
+    *sm_count = g_sm_count;
+    return GBO_OK;
+}
+
+bool internal_nn_view(const gbo_nn *nn, NNArgs *a, SpaceParams *sp, int *precision, int *features)
+{
+    if (!nn)
+        return false;
+    *a = nn_args(nn);
+    *sp = nn->sp;
+    *precision = nn->precision;
+    *features = nn->F;
+    return true;
+}
+}  // namespace gbo
