@@ -219,6 +219,7 @@ def ours(args, rank, world, local_rank):
         wall = time.perf_counter() - t0
     launches = B.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
+    stats = checker.stats()  # states evaluated / re-checked in FP64 by the last timed step
     dev_s = sum(step_ms) * 1e-3
     t_local = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
     if world > 1:
@@ -253,7 +254,6 @@ def ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     plain_eps = N_BATCHES * N_EDGES / (p0.elapsed_time(p1) * 1e-3)
     checker.setPrecision("fp32_guarded")
-    stats = checker.stats()
 
     # end to end through the host-memory C-ABI call
     mv.checkMotionHost(*host_batches[0])

@@ -76,21 +76,70 @@ __device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L,
     }
 }
 
-// Warp-cooperative guarded state test. Returns kInvalid, kValid or kAmbiguous (same in all lanes).
-__device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, float px, float py,
-                                                  const ChainSegF32 *w, const unsigned *tab, const ChainTables &t,
-                                                  const ChainGuard &g)
+// FP64 segments of one state in the reference's operation order (KinematicChain.h:214-228): theta
+// and the end points accumulate sequentially (lane m's values reach every lane by shuffle), cos/sin
+// are evaluated lane-parallel. Lane k <= n receives segment k (lane n: the 0.001 tip segment).
+__device__ __forceinline__ void chain_segments64_warp(double q, int lane, int n, double L, double &x0, double &y0,
+                                                      double &x1, double &y1)
 {
-    bool amb = false;
+    double th = 0.0, mine = 0.0;
+    for (int m = 0; m < n; ++m)
+    {
+        th = dadd(th, __shfl_sync(0xffffffffu, q, m));
+        if (m == lane)
+            mine = th;
+    }
+    double sn, cs;
+    sincos(mine, &sn, &cs);
+    double x = 0.0, y = 0.0, cl = 1.0, sl = 0.0;
+    x0 = y0 = x1 = y1 = 0.0;
+    for (int m = 0; m < n; ++m)
+    {
+        cl = __shfl_sync(0xffffffffu, cs, m);
+        sl = __shfl_sync(0xffffffffu, sn, m);
+        if (m == lane)
+        {
+            x0 = x;
+            y0 = y;
+        }
+        x = dadd(x, dmul(cl, L));
+        y = dadd(y, dmul(sl, L));
+        if (m == lane)
+        {
+            x1 = x;
+            y1 = y;
+        }
+    }
+    if (lane == n)
+    {
+        x0 = x;
+        y0 = y;
+        x1 = dadd(x, dmul(cl, 0.001));
+        y1 = dadd(y, dmul(sl, 0.001));
+    }
+}
+
+// Warp-cooperative state test: kInvalid or kValid (same in all lanes). Tests run 32 per round in
+// table order; a lane whose FP32 comparison is ambiguous re-evaluates its own test with the FP64
+// reference code on the state's FP64 segments (built once per state, on the first ambiguity, from
+// q64(lane) = joint `lane` of the state in FP64). `rechecked` counts states that needed FP64.
+template <class Q64>
+__device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, float vx, float vy, float px,
+                                                  float py, const ChainSegF32 *w, const double *w64,
+                                                  const unsigned *tab, ChainTables t, ChainGuard g, Q64 q64,
+                                                  unsigned &rechecked)
+{
+    bool have64 = false;
+    double sx0 = 0.0, sy0 = 0.0, sx1 = 0.0, sy1 = 0.0;
     for (int base = 0; base < t.n_tests; base += 32)
     {
         const int idx = base + lane;
         int r = kValid;
         const unsigned e = idx < t.n_tests ? tab[idx] : 0u;
         const int a = (int)(e & 0xff), b = (int)((e >> 8) & 0xffffff);
+        const bool self = (e & 0x80000000u) != 0u;
         const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
         const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
-        const bool self = (e & 0x80000000u) != 0u;
         const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
         const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
         if (idx < t.n_tests)
@@ -105,17 +154,41 @@ __device__ __forceinline__ int chain_state_warp32(int lane, float vx, float vy, 
                                     ws.e_v);
             }
         }
+        if (__any_sync(0xffffffffu, r == kAmbiguous))
+        {
+            if (!have64)
+            {
+                chain_segments64_warp(q64(lane), lane, n, L64, sx0, sy0, sx1, sy1);
+                have64 = true;
+                ++rechecked;
+            }
+            const double ax0 = __shfl_sync(0xffffffffu, sx0, a), ay0 = __shfl_sync(0xffffffffu, sy0, a);
+            const double ax1 = __shfl_sync(0xffffffffu, sx1, a), ay1 = __shfl_sync(0xffffffffu, sy1, a);
+            const double bx0 = __shfl_sync(0xffffffffu, sx0, b & 31), by0 = __shfl_sync(0xffffffffu, sy0, b & 31);
+            const double bx1 = __shfl_sync(0xffffffffu, sx1, b & 31), by1 = __shfl_sync(0xffffffffu, sy1, b & 31);
+            if (r == kAmbiguous)
+            {
+                bool hit;
+                if (self)
+                    hit = seg_intersect64(ax0, ay0, ax1, ay1, bx0, by0, bx1, by1);
+                else
+                {
+                    const double *o = w64 + 4 * (size_t)b;
+                    hit = seg_intersect64(ax0, ay0, ax1, ay1, o[0], o[1], o[2], o[3]);
+                }
+                r = hit ? kInvalid : kValid;
+            }
+        }
         if (__any_sync(0xffffffffu, r == kInvalid))
             return kInvalid;
-        amb |= __any_sync(0xffffffffu, r == kAmbiguous);
     }
-    return amb ? kAmbiguous : kValid;
+    return kValid;
 }
 
 // Definite-intersection bitmap of one state over all tests in default order (no early exit).
 __device__ __forceinline__ void chain_state_hits32(int lane, float vx, float vy, float px, float py,
                                                    const ChainSegF32 *w, int n_links, int nw, int n_tests,
-                                                   const ChainGuard &g, unsigned *bits)
+                                                   ChainGuard g, unsigned *bits)
 {
     for (int base = 0; base < n_tests; base += 32)
     {

@@ -86,29 +86,6 @@ __device__ __noinline__ int chain_nd64(const SpaceParams &sp, const StatesView &
     return segment_count_from_distance(sp, distance64<GBO_MAXD>(sp, a, b));
 }
 
-// Validity of checked state j of an edge (j == top: s2 itself) in FP64.
-__device__ __noinline__ bool chain_state64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v1,
-                                          const StatesView &v2, int64_t e, int j, int nd, int top)
-{
-    double a[GBO_MAXD], b[GBO_MAXD], q[GBO_MAXD];
-    load_pair64(v1, v2, e, sp.dim, a, b);
-    if (j == top)
-        for (int d = 0; d < GBO_MAXD; ++d)
-            q[d] = b[d];
-    else
-        interpolate64<GBO_MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
-    return chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n);
-}
-
-__device__ __noinline__ bool chain_valid_row64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v,
-                                              int64_t i)
-{
-    double q[GBO_MAXD];
-    for (int d = 0; d < GBO_MAXD; ++d)
-        q[d] = d < sp.dim ? v(i, d) : 0.0;
-    return chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n);
-}
-
 __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v,
                                                                   int64_t n, uint8_t *out, RunCounters *ctr)
 {
@@ -121,22 +98,19 @@ __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const float L = (float)sp.link;
+    const double L64 = sp.link;
+    const int dim = sp.dim;
+    const ChainGuard g = wa.guard;
+    const double *w64 = (const double *)wa.data64;
     unsigned rechecks = 0, evaluated = 0;
     for (int64_t i = warp; i < n; i += nwarps)
     {
         ++evaluated;
         float vx, vy, px, py;
-        chain_segments32(lane_joint(v, i, lane, sp.dim), lane, sp.dim, L, vx, vy, px, py);
-        int r = chain_state_warp32(lane, vx, vy, px, py, cs.w32, cs.tab, cs.t, wa.guard);
-        if (r == kAmbiguous)
-        {
-            if (lane == 0)
-            {
-                r = chain_valid_row64(sp, wa, v, i) ? kValid : kInvalid;
-                ++rechecks;
-            }
-            r = __shfl_sync(0xffffffffu, r, 0);
-        }
+        chain_segments32(lane_joint(v, i, lane, dim), lane, dim, L, vx, vy, px, py);
+        auto q64 = [&](int ln) { return ln < dim ? v(i, ln) : 0.0; };
+        const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, w64, cs.tab, cs.t, g, q64,
+                                         rechecks);
         if (lane == 0)
             out[i] = r == kValid ? 1 : 0;
     }
@@ -161,6 +135,9 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
     const int lane = threadIdx.x & 31;
     const int dim = sp.dim;
     const float L = (float)sp.link;
+    const double L64 = sp.link;
+    const ChainGuard g = wa.guard;
+    const double *w64 = (const double *)wa.data64;
     constexpr float kPiF = 3.14159265358979323846f;
     unsigned evaluated = 0, rechecks = 0;
     for (;;)
@@ -233,17 +210,17 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
                 }
                 float vx, vy, px, py;
                 chain_segments32(q, lane, dim, L, vx, vy, px, py);
-                int r = chain_state_warp32(lane, vx, vy, px, py, cs.w32, cs.tab, cs.t, wa.guard);
+                // joint `ln` of checked state j in FP64, as DiscreteMotionValidator.cpp:63 forms it
+                auto q64 = [&](int ln) {
+                    if (ln >= dim)
+                        return 0.0;
+                    if (j == top)
+                        return v2(e, ln);
+                    return interp_angle64(v1(e, ln), v2(e, ln), ddiv((double)j, (double)nd));
+                };
+                const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, w64, cs.tab, cs.t, g, q64,
+                                                 rechecks);
                 ++evaluated;
-                if (r == kAmbiguous)
-                {
-                    if (lane == 0)
-                    {
-                        r = chain_state64(sp, wa, v1, v2, e, j, nd, top) ? kValid : kInvalid;
-                        ++rechecks;
-                    }
-                    r = __shfl_sync(0xffffffffu, r, 0);
-                }
                 if (r == kInvalid)
                 {
                     first = j == top ? nd : j;
