@@ -70,14 +70,16 @@ def make_batches(valid_states, n_batches, seed=7):
 
 
 class Clocks:
-    """Samples nvidia-smi during the timed region."""
+    """Samples nvidia-smi every 200 ms from before the warm-up to after the timed region; summary()
+    keeps the samples taken within 0.25 s of the timed region (the nearest one if the region is
+    shorter than the sampling period)."""
 
     def __init__(self, index=0):
         self.samples = []
         self.proc = None
         self.index = index
 
-    def __enter__(self):
+    def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -95,9 +97,9 @@ class Clocks:
         for line in self.proc.stdout:
             p = [x.strip() for x in line.split(",")]
             if len(p) >= 8:
-                self.samples.append(p)
+                self.samples.append((time.perf_counter(), p))
 
-    def __exit__(self, *a):
+    def stop(self):
         if self.proc:
             self.proc.terminate()
             try:
@@ -105,15 +107,18 @@ class Clocks:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, t0, t1):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        win = [p for t, p in self.samples if t0 - 0.25 <= t <= t1 + 0.25]
+        if not win:
+            win = [min(self.samples, key=lambda tp: min(abs(tp[0] - t0), abs(tp[0] - t1)))[1]]
+        sm = [float(s[1]) for s in win if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in win if s[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[4 + k].lower() == "active"})
+        reasons = sorted({names[k] for s in win for k in range(4) if s[4 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(win)}
 
 
 def cpu_edges_per_s(port, sd, cd, s1, s2, threads):
@@ -192,6 +197,7 @@ def ours(args, rank, world, local_rank):
         s1, s2 = dev_batches[i % N_BATCHES]
         return mv.checkMotions(s1, s2, schedule=schedule, soa=True)
 
+    clk = Clocks(local_rank).start()
     for i in range(max(3, args.warmup)):
         run(i, capi.SCHEDULE_AUTO)
     torch.cuda.synchronize()
@@ -208,15 +214,17 @@ def ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     launches0 = B.launch_count()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with Clocks(local_rank) as clk:
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            evs[i][0].record(stream)
-            run(i, capi.SCHEDULE_AUTO)
-            evs[i][1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        run(i, capi.SCHEDULE_AUTO)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    wall = t1 - t0
+    time.sleep(0.3)
+    clk.stop()
     launches = B.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     stats = checker.stats()  # states evaluated / re-checked in FP64 by the last timed step
@@ -297,7 +305,7 @@ def ours(args, rank, world, local_rank):
     threads = os.cpu_count() or 1
     sample = 20_000
     cpu_v = cpu_edges_per_s(port, sd, cd, host_batches[0][0][:sample], host_batches[0][1][:sample], threads)
-    clocks = clk.summary()
+    clocks = clk.summary(t0, t1)
     out = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",

@@ -191,7 +191,7 @@ struct gbo_checker
     unsigned *test_order = nullptr;
     CounterRing ctr;
     int tuned_schedule = -1;
-    std::mutex mu;
+    std::mutex mu, tune_mu;
     cudaStream_t host_stream = nullptr;
     Pinned pin_in, pin_out;
     DevBuf dev_in, dev_out;
@@ -915,7 +915,7 @@ gbo_status gbo_check_motion(gbo_checker *c, const double *s1, const double *s2, 
         return GBO_OK;
     if (schedule == GBO_SCHEDULE_AUTO)
     {
-        std::lock_guard<std::mutex> lk(c->mu);
+        std::lock_guard<std::mutex> lk(c->tune_mu);
         if (c->tuned_schedule < 0)
         {
             // autotune: time both persistent schedules on (a prefix of) this batch
@@ -1028,25 +1028,17 @@ gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double 
     // device layout: s1 | s2 | first_j | nd | ok | last_t | last_state
     const size_t off_fj = 2 * bst, off_nd = off_fj + 4 * (size_t)n, off_ok = off_nd + 4 * (size_t)n;
     const size_t off_lt = pad16(off_ok + (size_t)n), off_ls = off_lt + 8 * (size_t)n, total = off_ls + bst;
-    if (auto st = c->pin_in.reserve(2 * bst))
-        return st;
     if (auto st = c->dev_in.reserve(total))
         return st;
-    const size_t out_bytes = (size_t)n + (last_t ? 8 * (size_t)n : 0) + (last_state ? bst : 0);
-    if (auto st = c->pin_out.reserve(out_bytes + 16))
-        return st;
-    std::memcpy(c->pin_in.p, s1, bst);
-    std::memcpy((char *)c->pin_in.p + bst, s2, bst);
     char *d = (char *)c->dev_in.p;
-    CUDA_TRY(cudaMemcpyAsync(d, c->pin_in.p, 2 * bst, cudaMemcpyHostToDevice, c->host_stream));
-    const int sched = c->precision == GBO_PRECISION_FP64 ? GBO_SCHEDULE_PLAIN : GBO_SCHEDULE_TILE;
-    if (auto st = motion_impl(c, (const double *)d, (const double *)(d + bst), n, dim, GBO_LAYOUT_AOS, sched,
-                              (uint8_t *)(d + off_ok), (int32_t *)(d + off_fj), (int32_t *)(d + off_nd),
-                              c->host_stream))
+    // the endpoints go straight from the caller's arrays to the device (no staging copy on the host)
+    CUDA_TRY(cudaMemcpyAsync(d, s1, bst, cudaMemcpyHostToDevice, c->host_stream));
+    CUDA_TRY(cudaMemcpyAsync(d + bst, s2, bst, cudaMemcpyHostToDevice, c->host_stream));
+    const int sched = c->precision == GBO_PRECISION_FP64 ? GBO_SCHEDULE_PLAIN : GBO_SCHEDULE_AUTO;
+    if (auto st = gbo_check_motion(c, (const double *)d, (const double *)(d + bst), n, dim, GBO_LAYOUT_AOS, sched,
+                                   (uint8_t *)(d + off_ok), (int32_t *)(d + off_fj), (int32_t *)(d + off_nd),
+                                   c->host_stream))
         return st;
-    char *po = (char *)c->pin_out.p;
-    CUDA_TRY(cudaMemcpyAsync(po, d + off_ok, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
-    size_t pos = (size_t)n;
     if (last_t || last_state)
     {
         StatesView v1 = make_view((const double *)d, dim, GBO_LAYOUT_AOS);
@@ -1055,24 +1047,13 @@ gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double 
                           (const int32_t *)(d + off_nd), n, (double *)(d + off_lt),
                           MutStatesView{last_state ? (double *)(d + off_ls) : nullptr, dim, 1});
         CHECK_LAUNCH();
-        if (last_t)
-        {
-            CUDA_TRY(cudaMemcpyAsync(po + pos, d + off_lt, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
-            pos += 8 * (size_t)n;
-        }
-        if (last_state)
-            CUDA_TRY(cudaMemcpyAsync(po + pos, d + off_ls, bst, cudaMemcpyDeviceToHost, c->host_stream));
     }
-    CUDA_TRY(cudaStreamSynchronize(c->host_stream));
-    std::memcpy(ok, po, (size_t)n);
-    pos = (size_t)n;
+    CUDA_TRY(cudaMemcpyAsync(ok, d + off_ok, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
     if (last_t)
-    {
-        std::memcpy(last_t, po + pos, 8 * (size_t)n);
-        pos += 8 * (size_t)n;
-    }
+        CUDA_TRY(cudaMemcpyAsync(last_t, d + off_lt, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
     if (last_state)
-        std::memcpy(last_state, po + pos, bst);
+        CUDA_TRY(cudaMemcpyAsync(last_state, d + off_ls, bst, cudaMemcpyDeviceToHost, c->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(c->host_stream));
     return GBO_OK;
 }
 

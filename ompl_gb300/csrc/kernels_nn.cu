@@ -36,8 +36,8 @@ __device__ __forceinline__ void load_query(const StatesView &v, int64_t i, int d
 }
 
 // Insert (d, key) into an ascending register list; equal distances keep the earlier entry first.
-template <int K, class T>
-__device__ __forceinline__ void topk_insert(T *dk, int64_t *ik, T d, int64_t key)
+template <int K, class T, class I>
+__device__ __forceinline__ void topk_insert(T *dk, I *ik, T d, I key)
 {
 #pragma unroll
     for (int j = K - 1; j >= 0; --j)
@@ -147,40 +147,37 @@ __global__ void __launch_bounds__(256) knn_exact_kernel(NNArgs nn, SpaceParams s
 // ---------------------------------------------------------------- FP32 scan
 
 // Element features: REAL_VECTOR / WRAP_L2 / SO2: the coordinates (F = dim); KINEMATIC_CHAIN: the
-// cumulative link-direction sums (X_1..X_n, Y_1..Y_n), F = 2 dim, so that
-// distance = L * sum_i |(X_i(a) - X_i(b), Y_i(a) - Y_i(b))|.
+// cumulative link-direction sums interleaved (X_1, Y_1, ..., X_n, Y_n), F = 2 dim, so that
+// distance = L * sum_i |(X_i(a) - X_i(b), Y_i(a) - Y_i(b))|. All indices below are compile-time.
 template <int KIND, int MAXF>
-__device__ __forceinline__ float dist32_sq_or_d(const float *a, const float *b, int dim, float &lower)
+__device__ __forceinline__ float box_dist2(const float *a, const float *b, int dim)
 {
-    if constexpr (KIND == GBO_SPACE_KINEMATIC_CHAIN)
-    {
-        // lower bound sum_i (|dx_i| + |dy_i|) / sqrt(2) <= sum_i |(dx_i, dy_i)| (no sqrt needed)
-        float l1 = 0.f;
+    float s = 0.f;
 #pragma unroll
-        for (int i = 0; i < MAXF / 2; ++i)
-            if (i < dim)
-                l1 += fabsf(a[i] - b[i]) + fabsf(a[i + dim] - b[i + dim]);
-        lower = l1;
-        return 0.f;
-    }
-    else
-    {
-        float s = 0.f;
-#pragma unroll
-        for (int i = 0; i < MAXF; ++i)
-            if (i < dim)
+    for (int i = 0; i < MAXF; ++i)
+        if (i < dim)
+        {
+            float d = a[i] - b[i];
+            if constexpr (KIND == GBO_SPACE_WRAP_L2 || KIND == GBO_SPACE_SO2)
             {
-                float d = a[i] - b[i];
-                if constexpr (KIND == GBO_SPACE_WRAP_L2 || KIND == GBO_SPACE_SO2)
-                {
-                    d = fabsf(d);
-                    d = fminf(d, 6.28318530717958647692f - d);
-                }
-                s = fmaf(d, d, s);
+                d = fabsf(d);
+                d = fminf(d, 6.28318530717958647692f - d);
             }
-        lower = s;
-        return s;
-    }
+            s = fmaf(d, d, s);
+        }
+    return s;
+}
+
+// Partial L1 lower bound over links [i0, i1): sum (|dx_i| + |dy_i|) <= sqrt(2) * sum |(dx_i, dy_i)|.
+template <int MAXF>
+__device__ __forceinline__ float chain_l1(const float *a, const float *b, int dim, int i0, int i1)
+{
+    float l1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < MAXF / 2; ++i)
+        if (i >= i0 && i < i1 && i < dim)
+            l1 += fabsf(a[2 * i] - b[2 * i]) + fabsf(a[2 * i + 1] - b[2 * i + 1]);
+    return l1;
 }
 
 __device__ __forceinline__ float sqrt_approx(float x)
@@ -190,7 +187,7 @@ __device__ __forceinline__ float sqrt_approx(float x)
     return r;
 }
 
-template <int KIND, int MAXF>
+template <int MAXF>
 __device__ __forceinline__ float chain_dist32(const float *a, const float *b, int dim)
 {
     float s = 0.f;
@@ -198,7 +195,7 @@ __device__ __forceinline__ float chain_dist32(const float *a, const float *b, in
     for (int i = 0; i < MAXF / 2; ++i)
         if (i < dim)
         {
-            const float dx = a[i] - b[i], dy = a[i + dim] - b[i + dim];
+            const float dx = a[2 * i] - b[2 * i], dy = a[2 * i + 1] - b[2 * i + 1];
             s += sqrt_approx(fmaf(dx, dx, dy * dy));
         }
     return s;
@@ -237,7 +234,7 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
     const int64_t block_end = (int64_t)s_limit;
 
     float dk[K_KEEP];
-    int64_t ik[K_KEEP];
+    int ik[K_KEEP];
 #pragma unroll
     for (int j = 0; j < K_KEEP; ++j)
     {
@@ -274,16 +271,23 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
                 pf[f + 2] = v.z;
                 pf[f + 3] = v.w;
             }
-            float lower;
-            float d = dist32_sq_or_d<KIND, MAXF>(pf, qfe, sp.dim, lower);
+            float d;
             if constexpr (KIND == GBO_SPACE_KINEMATIC_CHAIN)
             {
-                if (lower * lscale >= dk[K_KEEP - 1])
+                // outer links first: their terms are the largest, so most elements stop here
+                const int half = sp.dim >> 1;
+                float lb = chain_l1<MAXF>(pf, qfe, sp.dim, half, sp.dim);
+                if (lb * lscale >= dk[K_KEEP - 1])
                     continue;
-                d = chain_dist32<KIND, MAXF>(pf, qfe, sp.dim) * (float)sp.link;
+                lb += chain_l1<MAXF>(pf, qfe, sp.dim, 0, half);
+                if (lb * lscale >= dk[K_KEEP - 1])
+                    continue;
+                d = chain_dist32<MAXF>(pf, qfe, sp.dim) * (float)sp.link;
             }
+            else
+                d = box_dist2<KIND, MAXF>(pf, qfe, sp.dim);
             if (d < dk[K_KEEP - 1])
-                topk_insert<K_KEEP>(dk, ik, d, base + t);
+                topk_insert<K_KEEP>(dk, ik, d, (int)(base + t));
         }
     }
     if (!active)
@@ -416,8 +420,8 @@ __global__ void features_kernel(SpaceParams sp, StatesView v, int64_t n, float *
             dir32(theta, c, s);
             X += c;
             Y += s;
-            out[(int64_t)d * ld_out + i] = X;
-            out[(int64_t)(d + sp.dim) * ld_out + i] = Y;
+            out[(int64_t)(2 * d) * ld_out + i] = X;
+            out[(int64_t)(2 * d + 1) * ld_out + i] = Y;
         }
     }
     else
