@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm"],
+                   help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
+                        "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
     p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks"],
                    help="launch one kernel kind twice on the chain workload (for ncu) and exit")
     return p.parse_args()
@@ -263,11 +266,23 @@ def ours(args, rank, world, local_rank):
     plain_eps = N_BATCHES * N_EDGES / (p0.elapsed_time(p1) * 1e-3)
     checker.setPrecision("fp32_guarded")
 
-    # end to end through the host-memory C-ABI call
-    mv.checkMotionHost(*host_batches[0])
+    # end to end through the host-memory C-ABI call (gbo_check_motion_host): endpoints in pinned host
+    # memory (OMPL's per-state row layout), results (ok + lastValid fractions) read back to pinned memory
+    import ctypes as C
+    pin_in = [(torch.as_tensor(a).pin_memory(), torch.as_tensor(b).pin_memory()) for a, b in host_batches]
+    ok_h = torch.empty(N_EDGES, dtype=torch.uint8).pin_memory()
+    lt_h = torch.empty(N_EDGES, dtype=torch.float64).pin_memory()
+
+    def e2e_step(i):
+        a, b = pin_in[i % N_BATCHES]
+        capi.check(capi.lib().gbo_check_motion_host(checker._h, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                                    N_EDGES, C.c_void_p(ok_h.data_ptr()),
+                                                    C.c_void_p(lt_h.data_ptr()), None))
+
+    e2e_step(0)
     t = time.perf_counter()
     for i in range(args.steps):
-        mv.checkMotionHost(*host_batches[i % N_BATCHES])
+        e2e_step(i)
     e2e_s = time.perf_counter() - t
     e2e = N_EDGES * args.steps / e2e_s
 
@@ -373,8 +388,84 @@ def profile(kind):
     print(json.dumps({"profile": kind, "ok": True}))
 
 
+def arm_bench(args):
+    """7-DoF DH arm among 4,096 spheres: 256k edges with 2..2000 interpolation steps, one launch."""
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import capi
+    from ompl_gb300 import workloads as W
+    w = W.config2()
+    space = B.RealVectorStateSpace(7, w.low, w.high)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
+    mv = B.DiscreteMotionValidator(checker)
+    s1 = torch.as_tensor(w.s1.T.copy(), device="cuda")
+    s2 = torch.as_tensor(w.s2.T.copy(), device="cuda")
+    n = s1.shape[1]
+    res = {}
+    for prec, sch, name in (("fp32_guarded", capi.SCHEDULE_TILE, "tile"), ("fp32_guarded", capi.SCHEDULE_WARP, "warp"),
+                            ("fp64", capi.SCHEDULE_PLAIN, "plain_fp64")):
+        checker.setPrecision(prec)
+        m = n if name != "plain_fp64" else 16_384
+        a, b = s1[:, :m].contiguous(), s2[:, :m].contiguous()
+        r = mv.checkMotions(a, b, schedule=sch, soa=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps = 3 if name != "plain_fp64" else 1
+        for _ in range(reps):
+            r = mv.checkMotions(a, b, schedule=sch, soa=True)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = reps * m / (e0.elapsed_time(e1) * 1e-3)
+        if name == "tile":
+            fj, nd = r["first_j"].long(), r["nd"].long()
+            checked = int(torch.where(fj >= 0, fj, torch.clamp(nd, min=1)).sum().item())
+            valid = float(r["ok"].float().mean().item())
+            st = checker.stats()
+    print(json.dumps({"metric": "validated edges/s (DH arm, 4096 spheres)", "edges": n,
+                      "edges_per_s": res, "checked_states_per_edge": checked / n, "valid_fraction": valid,
+                      "recheck": st}))
+
+
+def prm_bench(args):
+    """Full PRM roadmap construction (2M uniform samples, validity filter, prefix nearestK k=10 in
+    the wrap-L2 joint space, n->m edges at 0.01 rad) for the DH arm among 16,384 spheres."""
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import prm
+    from ompl_gb300 import workloads as W
+    w = W.config4()
+    n = int(os.environ.get("PRM_SAMPLES", w.extra["n_samples"]))
+    space = B.WrapL2StateSpace(7)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
+    checker.setPrecision("fp32_guarded")
+    prm.construct_roadmap(space, checker, w.extra["sampler_seed"], 20_000)  # warm-up (autotune, allocs)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    rm = prm.construct_roadmap(space, checker, w.extra["sampler_seed"], n)
+    total = time.perf_counter() - t
+    nm = rm.milestones.shape[1]
+    comps = prm.connected_components(nm, rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy())
+    print(json.dumps({"metric": "PRM roadmap construction (DH arm, 16384 spheres)", "samples": n,
+                      "milestones": nm, "candidate_edges": rm.candidate_edges, "edges": int(rm.edge_src.numel()),
+                      "components": comps, "total_s": total, "timings_ms": rm.timings_ms,
+                      "edges_per_s": rm.candidate_edges / (rm.timings_ms["motion"] * 1e-3),
+                      "knn_queries_per_s": nm / (rm.timings_ms["nn add+prefix kNN"] * 1e-3),
+                      "checked_states": rm.checked_states}))
+
+
 def main():
     args = parse()
+    if args.workload == "arm" and not args.profile and args.impl == "ours":
+        arm_bench(args)
+        return
+    if args.workload == "prm" and not args.profile and args.impl == "ours":
+        prm_bench(args)
+        return
     if args.profile:
         profile(args.profile)
         return

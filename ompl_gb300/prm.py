@@ -1,0 +1,93 @@
+"""Batched PRM roadmap construction on the GPU path (the caller of the path named first among the
+next steps): PRM::growRoadmap + PRM::addMilestone (geometric/planners/prm/src/PRM.cpp:364-385,
+570-604) with the default KStrategy (k = 10, ConnectionStrategy.h:77-81) and the default connection
+filter (always true, PRM.cpp:176), done as whole batches:
+
+  1. milestones: PRM samples with UniformValidStateSampler (sampleUniform until isValid), so the
+     milestone sequence is the valid subsequence of the sampler's uniform stream, in order;
+  2. neighbours: milestone m queries nearestK among the milestones added before it (nn_->add(m)
+     runs after the connections, PRM.cpp:601), i.e. a prefix kNN with limit m;
+  3. edges: every neighbour n is connected by checkMotion(state[n], state[m]) (PRM.cpp:590) —
+     direction n -> m — and an edge is added when the motion is valid.
+
+The edge set equals the sequential PRM's for the same sampler seed (each connection attempt is
+independent of the others). Connected components are computed from the edge list on the host.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import base as B
+from . import capi
+
+
+@dataclass
+class Roadmap:
+    samples: int                 # uniform samples drawn
+    milestones: torch.Tensor     # (dim, M) SoA, milestone order
+    sample_index: torch.Tensor   # (M,) index of each milestone in the sample stream
+    edge_src: torch.Tensor       # (E,) neighbour milestone n of each valid edge
+    edge_dst: torch.Tensor       # (E,) new milestone m
+    candidate_edges: int         # connection attempts (checkMotion calls)
+    checked_states: int          # states the ordered DiscreteMotionValidator evaluates
+    timings_ms: dict
+
+
+def construct_roadmap(space: B.StateSpace, checker: B.StateValidityChecker, sampler_seed: int, n_samples: int,
+                      k: int = 10, schedule: int = capi.SCHEDULE_AUTO, stream=None) -> Roadmap:
+    dev = torch.device("cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    ev[0].record()
+    sampler = B.StateSampler(space, sampler_seed)
+    samples = sampler.sampleUniform(n_samples, soa=True, host=False, stream=stream)
+    ev[1].record()
+    valid = checker.isValid(samples, soa=True, stream=stream)
+    sample_index = torch.nonzero(valid).squeeze(1)
+    milestones = samples[:, sample_index].contiguous()
+    nm = milestones.shape[1]
+    ev[2].record()
+    nn = B.NearestNeighborsGPU(space, capacity=max(nm, 1))
+    if nm:
+        nn.add(milestones, soa=True, stream=stream)
+    prefix = torch.arange(nm, device=dev, dtype=torch.int64)
+    nbr, _ = nn.nearestK(milestones, k, prefix=prefix, soa=True, want_dist=False, stream=stream)
+    ev[3].record()
+    dst = torch.arange(nm, device=dev, dtype=torch.int64).repeat_interleave(k)
+    src = nbr.reshape(-1)
+    have = src >= 0
+    src, dst = src[have].contiguous(), dst[have].contiguous()
+    s1 = milestones[:, src].contiguous()
+    s2 = milestones[:, dst].contiguous()
+    ev[4].record()
+    mv = B.DiscreteMotionValidator(checker)
+    r = mv.checkMotions(s1, s2, schedule=schedule, soa=True, stream=stream)
+    ok = r["ok"].bool()
+    fj, nd = r["first_j"].long(), r["nd"].long()
+    checked = int(torch.where(fj >= 0, fj, torch.clamp(nd, min=1)).sum().item())
+    ev[5].record()
+    torch.cuda.synchronize()
+    names = ["sample", "validity+compact", "nn add+prefix kNN", "gather", "motion"]
+    timings = {n: ev[i].elapsed_time(ev[i + 1]) for i, n in enumerate(names)}
+    return Roadmap(n_samples, milestones, sample_index, src[ok], dst[ok], int(src.numel()), checked, timings)
+
+
+def connected_components(num_vertices: int, src: np.ndarray, dst: np.ndarray) -> int:
+    """Number of connected components (PRM::uniteComponents keeps the same partition)."""
+    parent = np.arange(num_vertices)
+
+    def find(x):
+        root = x
+        while parent[root] != root:
+            root = parent[root]
+        while parent[x] != root:
+            parent[x], x = root, parent[x]
+        return root
+
+    for a, b in zip(src.tolist(), dst.tolist()):
+        ra, rb = find(a), find(b)
+        if ra != rb:
+            parent[ra] = rb
+    return int(sum(1 for v in range(num_vertices) if find(v) == v))

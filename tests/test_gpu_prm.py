@@ -1,0 +1,49 @@
+"""Batched PRM roadmap (PRM.cpp:364-385, 570-604 semantics) on the GPU path against the same
+construction done step by step with the oracle: identical milestones (bitwise), identical neighbour
+lists (prefix nearestK, k = 10) and an identical edge set (checkMotion(n, m) valid)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from ompl_gb300 import base as B  # noqa: E402
+from ompl_gb300 import prm  # noqa: E402
+from ompl_gb300 import workloads as W  # noqa: E402
+from oracle.oracle import CheckerDesc, SpaceDesc  # noqa: E402
+
+
+@pytest.mark.parametrize("precision", ["fp32_guarded", "fp64"])
+def test_prm_roadmap_matches_sequential_prm(port, precision):
+    n_samples, k = 2500, 10
+    w = W.config4(n_samples=n_samples, n_world=1024)
+    seed = w.extra["sampler_seed"]
+    space = B.WrapL2StateSpace(7)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
+    checker.setPrecision(precision)
+    rm = prm.construct_roadmap(space, checker, seed, n_samples, k=k)
+
+    port.set_threads(16)
+    sd = SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles, dh=w.dh, spheres_per_link=8, sphere_radius=0.05)
+    samples = port.sample_uniform(sd, seed, n_samples)
+    valid = port.is_valid(sd, cd, samples).astype(bool)
+    M = samples[valid]
+    assert np.array_equal(rm.sample_index.cpu().numpy(), np.flatnonzero(valid))
+    assert np.array_equal(rm.milestones.cpu().numpy().T.view(np.uint64), M.view(np.uint64))
+    nbr, _ = port.knn_prefix(sd, M, M, np.arange(len(M)), k)
+    dst = np.repeat(np.arange(len(M)), k)
+    src = nbr.reshape(-1)
+    have = src >= 0
+    src, dst = src[have], dst[have]
+    assert rm.candidate_edges == len(src)
+    ok = port.check_motion(sd, cd, M[src], M[dst], want_state=False, want_bisect=False)["ok"].astype(bool)
+    ref_edges = set(zip(src[ok].tolist(), dst[ok].tolist()))
+    got_edges = set(zip(rm.edge_src.cpu().tolist(), rm.edge_dst.cpu().tolist()))
+    assert got_edges == ref_edges
+    assert prm.connected_components(len(M), rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy()) == \
+        prm.connected_components(len(M), src[ok], dst[ok])
