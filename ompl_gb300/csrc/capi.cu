@@ -877,6 +877,8 @@ gbo_status gbo_checker_stats(const gbo_checker *c, uint64_t *evaluated, uint64_t
         *rechecked = h.rechecked;
     if (h.timeout)
         return fail(GBO_ERR_TIMEOUT, "a device-side wait ran out in the last call");
+    if (h.error)
+        return fail(GBO_ERR_CUDA, "a kernel refused to stage its world into shared memory in the last call");
     return GBO_OK;
 }
 

@@ -27,7 +27,7 @@ struct ChainSmem
 __device__ bool chain_setup(const SpaceParams &sp, const WorldArgs &wa, unsigned char *smem, uint64_t *bar,
                             RunCounters *ctr, ChainSmem &cs)
 {
-    if (!stage_bulk(smem, wa.data32, wa.bytes32, bar, &ctr->timeout))
+    if (!stage_bulk(smem, wa.data32, wa.bytes32, bar, &ctr->timeout, &ctr->error))
         return false;
     unsigned *tab = (unsigned *)(smem + wa.bytes32);
     build_chain_tables(sp.dim, wa.n, wa.test_order, tab, cs.t);
@@ -254,11 +254,11 @@ __global__ void __launch_bounds__(256) chain_hits_kernel(SpaceParams sp, WorldAr
     __shared__ uint64_t bar;
     RunCounters *none = nullptr;
     (void)none;
-    __shared__ unsigned timeout;
+    __shared__ unsigned timeout, error;
     if (threadIdx.x == 0)
-        timeout = 0;
+        timeout = error = 0;
     __syncthreads();
-    if (!stage_bulk(smem, wa.data32, wa.bytes32, &bar, &timeout))
+    if (!stage_bulk(smem, wa.data32, wa.bytes32, &bar, &timeout, &error))
         return;
     const ChainSegF32 *w = (const ChainSegF32 *)smem;
     const int lane = threadIdx.x & 31;
@@ -278,6 +278,9 @@ __global__ void __launch_bounds__(256) chain_hits_kernel(SpaceParams sp, WorldAr
 void launch_chain_hits(cudaStream_t s, const SpaceParams &sp, const WorldArgs &wa, const double *states, int n,
                        unsigned *bits, int words)
 {
+    if (wa.bytes32 > 48 * 1024)
+        cudaFuncSetAttribute((const void *)chain_hits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)wa.bytes32);
     chain_hits_kernel<<<64, 256, wa.bytes32, s>>>(sp, wa, states, n, bits, words);
     note_launch();
 }

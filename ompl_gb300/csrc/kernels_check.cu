@@ -79,15 +79,24 @@ __device__ bool setup_world(const WorldArgs &wa, unsigned char *smem, uint64_t *
     unsigned char *p = smem;
     if (PREC == GBO_PRECISION_FP32_GUARDED && (CK == GBO_CHECK_CHAIN_SEGMENTS || CK == GBO_CHECK_DH_SPHERES))
     {
-        if (!stage_bulk(p, wa.data32, wa.bytes32, bar, &ctr->timeout))
-            return false;
-        ev.w32 = (const ChainSegF32 *)p;
-        ev.sph32 = (const float4 *)p;
+        if (wa.stage32)
+        {
+            if (!stage_bulk(p, wa.data32, wa.bytes32, bar, &ctr->timeout, &ctr->error))
+                return false;
+            ev.w32 = (const ChainSegF32 *)p;
+            ev.sph32 = (const float4 *)p;
+        }
+        else
+        {
+            // too large for shared memory: read from global memory (L2 / L1)
+            ev.w32 = (const ChainSegF32 *)wa.data32;
+            ev.sph32 = (const float4 *)wa.data32;
+        }
         ev.w64 = (const double *)wa.data64;  // FP64 re-checks read the world from global memory (L2)
     }
     else if (wa.stage64)
     {
-        if (!stage_bulk(p, wa.data64, wa.bytes64, bar, &ctr->timeout))
+        if (!stage_bulk(p, wa.data64, wa.bytes64, bar, &ctr->timeout, &ctr->error))
             return false;
         ev.w64 = (const double *)p;
     }

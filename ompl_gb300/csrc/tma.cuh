@@ -57,14 +57,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
     return false;
 }
 
+__device__ __forceinline__ unsigned dynamic_smem_bytes()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+    return r;
+}
+
 // Copy `bytes` (multiple of 16, 16-byte aligned on both sides) from global to shared memory with the
-// bulk-copy engine. All threads of the block must call it. Returns false after raising *timeout if the
-// copy did not complete within the wait limit (after a second bounded wait for the copy in flight).
+// bulk-copy engine. All threads of the block must call it. A copy larger than the launch's dynamic
+// shared memory, or an unaligned one, is refused: *error is raised and false returned. Returns false
+// after raising *timeout if the copy did not complete within the wait limit (after a second bounded
+// wait for the copy in flight).
 __device__ __forceinline__ bool stage_bulk(void *dst, const void *src, unsigned bytes, uint64_t *bar,
-                                           unsigned *timeout)
+                                           unsigned *timeout, unsigned *error)
 {
     if (bytes == 0)
         return true;
+    if (bytes > dynamic_smem_bytes() || (bytes & 15u) || (((uintptr_t)src) & 15u) || (smem_addr(dst) & 15u))
+    {
+        if (threadIdx.x == 0)
+            atomicExch(error, 1u);
+        return false;
+    }
     if (threadIdx.x == 0)
         mbar_init(bar, 1);
     __syncthreads();

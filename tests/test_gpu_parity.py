@@ -297,3 +297,26 @@ def test_knn_chain_large_vs_oracle(chain_case, port):
     ri, rd = port.knn(sp, w.states, q, 16)
     assert np.array_equal(idx, ri) and ulp_close(dist, rd)
     assert idx[:, 0].tolist() == [int(np.flatnonzero((w.states == qq).all(1))[0]) for qq in q]
+
+
+def test_dh_arm_large_world_read_from_global_memory(port):
+    """A 16,384-sphere world does not fit the shared-memory staging limit: the FP32 path reads the
+    spheres from global memory. Validity and motion must still equal the oracle's."""
+    w = W.config4(n_world=16_384)
+    sp = SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction)
+    ckd = CheckerDesc(w.checker_kind, w.obstacles, dh=w.dh, spheres_per_link=8, sphere_radius=0.05)
+    rng = np.random.default_rng(13)
+    st = rng.uniform(-math.pi, math.pi, size=(400, 7))
+    port.set_threads(16)
+    vref = port.is_valid(sp, ckd, st).astype(bool)
+    e1, e2 = st[:60], st[60:120] * 0.25
+    mref = port.check_motion(sp, ckd, e1, e2, want_state=False, want_bisect=False)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    mv = B.DiscreteMotionValidator(ck)
+    for p in ("fp32_guarded", "fp64"):
+        ck.setPrecision(p)
+        assert np.array_equal(ck.isValid(st), vref), p
+        assert ck.stats() is not None
+        r = mv.checkMotions(e1, e2, schedule=capi.SCHEDULE_TILE if p == "fp32_guarded" else capi.SCHEDULE_PLAIN)
+        assert np.array_equal(r["ok"], mref["ok"]) and np.array_equal(r["first_j"], mref["first_j"]), p
