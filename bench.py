@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm"],
+    p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve"],
                    help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
     p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks"],
@@ -458,8 +458,144 @@ def prm_bench(args):
                       "checked_states": rm.checked_states}))
 
 
+def serve_bench(args):
+    """Serving: 512 clients, each with its own world (1,024..8,192 spheres, the 7-DoF DH arm) and roadmap
+    (10k..200k joint states, nearestK k=10); Poisson arrivals of motion requests (16..65,536 edges) and
+    nearestK requests (1..4,096 queries). Reports saturation throughput and, at 70% of it, p50/p99."""
+    import threading as th
+
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import capi
+    from ompl_gb300 import serve
+    from ompl_gb300 import workloads as W
+    n_clients = int(os.environ.get("SERVE_CLIENTS", 512))
+    n_req = int(os.environ.get("SERVE_REQUESTS", 3000))
+    rng = np.random.default_rng(3)
+    dh = W.dh_arm(np.random.default_rng(2))
+    lvs_fraction = 1.0 / 2500.0
+    clients = []
+    t_setup = time.perf_counter()
+    for c in range(n_clients):
+        crng = np.random.default_rng(3 + 1000 * (c + 1))
+        world = W.sphere_world(crng, int(crng.integers(1024, 8193)))
+        space = B.RealVectorStateSpace(7, -math.pi, math.pi)
+        space.setLongestValidSegmentFraction(lvs_fraction)
+        ck = B.DHSphereArmValidityChecker(space, dh, world, 8, 0.05)
+        ck.setPrecision("fp32_guarded")
+        nroad = int(np.exp(crng.uniform(np.log(10_000), np.log(200_000))))
+        wspace = B.WrapL2StateSpace(7)
+        nn = B.NearestNeighborsGPU(wspace, capacity=nroad)
+        nn.add(torch.as_tensor(crng.uniform(-math.pi, math.pi, size=(7, nroad)), device="cuda"), soa=True)
+        clients.append((ck, nn, nroad))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    lo, hi = np.full(7, -math.pi), np.full(7, math.pi)
+    e1, e2 = W.arm_edges(rng, 262_144, 2 * math.pi * math.sqrt(7) * lvs_fraction, lo, hi)
+    qpool = rng.uniform(-math.pi, math.pi, size=(262_144, 7))
+    reqs = []
+    for i in range(n_req):
+        c = int(rng.integers(0, n_clients))
+        if rng.random() < 0.5:
+            n = int(np.exp(rng.uniform(np.log(16), np.log(65_536))))
+            o = int(rng.integers(0, len(e1) - n))
+            reqs.append(("motion", c, e1[o:o + n], e2[o:o + n]))
+        else:
+            n = int(np.exp(rng.uniform(np.log(1), np.log(4096))))
+            o = int(rng.integers(0, len(qpool) - n))
+            reqs.append(("knn", c, qpool[o:o + n], None))
+    srv = serve.Server(n_streams=32, arena_bytes=8 << 30)
+
+    def submit(r):
+        kind, c, a, b = r
+        ck, nn, _ = clients[c]
+        if kind == "motion":
+            return srv.submit_motion(ck, a, b, schedule=capi.SCHEDULE_TILE)
+        return srv.submit_knn(nn, a, 10, want_dist=False)
+
+    for r in reqs[:64]:  # warm-up: allocations of every code path
+        srv.wait(submit(r))
+
+    def run(rate):
+        lat = [None] * len(reqs)
+        tickets = [None] * len(reqs)
+        done = th.Event()
+
+        def waiter():
+            for i in range(len(reqs)):
+                while tickets[i] is None:
+                    time.sleep(0.0002)
+                lat[i] = srv.wait(tickets[i])[1]
+            done.set()
+
+        w = th.Thread(target=waiter)
+        w.start()
+        t0 = time.perf_counter()
+        gaps = np.random.default_rng(9).exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+        t_next = t0
+        for i, r in enumerate(reqs):
+            t_next += gaps[i]
+            d = t_next - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets[i] = submit(r)
+        done.wait()
+        wall = time.perf_counter() - t0
+        w.join()
+        return wall, lat
+
+    wall_sat, _ = run(None)
+    edges = sum(len(r[2]) for r in reqs if r[0] == "motion")
+    queries = sum(len(r[2]) for r in reqs if r[0] == "knn")
+    rate = 0.7 * len(reqs) / wall_sat
+    wall, lat = run(rate)
+
+    def pct(kind, q):
+        xs = [l for r, l in zip(reqs, lat) if kind in (None, r[0])]
+        return float(np.percentile(xs, q) * 1e3)
+
+    # plain form: the same requests one at a time, FP64 plain motion schedule and FP64 exact nearestK
+    sample = reqs[:200]
+    t = time.perf_counter()
+    pe = pq = 0
+    for kind, c, a, b in sample:
+        ck, nn, _ = clients[c]
+        if kind == "motion":
+            ck.setPrecision("fp64")
+            B.DiscreteMotionValidator(ck).checkMotions(a, b, schedule=capi.SCHEDULE_PLAIN)
+            ck.setPrecision("fp32_guarded")
+            pe += len(a)
+        else:
+            nn.setPrecision("fp64")
+            nn.nearestK(a, 10, want_dist=False)
+            nn.setPrecision("fp32_guarded")
+            pq += len(a)
+    plain_s = time.perf_counter() - t
+    st = srv.stats()
+    srv.close()
+    print(json.dumps({
+        "metric": "serving: validated edges/s and kNN queries/s, p50/p99 latency", "clients": n_clients,
+        "requests": n_req, "setup_s": setup_s,
+        "saturation": {"wall_s": wall_sat, "edges_per_s": edges / wall_sat, "queries_per_s": queries / wall_sat,
+                       "requests_per_s": n_req / wall_sat},
+        "offered_load_requests_per_s": rate,
+        "at_offered_load": {"wall_s": wall, "edges_per_s": edges / wall, "queries_per_s": queries / wall,
+                            "p50_ms": pct(None, 50), "p99_ms": pct(None, 99),
+                            "motion_p50_ms": pct("motion", 50), "motion_p99_ms": pct("motion", 99),
+                            "knn_p50_ms": pct("knn", 50), "knn_p99_ms": pct("knn", 99)},
+        "plain_sequential_sample": {"requests": len(sample), "wall_s": plain_s,
+                                    "edges_per_s": pe / plain_s if plain_s else None,
+                                    "work_units_per_s": (pe + pq) / plain_s},
+        "served_vs_plain_edges": (edges / wall_sat) / (pe / plain_s) if pe else None,
+        "server": st}))
+
+
 def main():
     args = parse()
+    if args.workload == "serve" and not args.profile and args.impl == "ours":
+        serve_bench(args)
+        return
     if args.workload == "arm" and not args.profile and args.impl == "ours":
         arm_bench(args)
         return

@@ -183,6 +183,42 @@ gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t 
 gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out);
 gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out);
 
+/* ---- serving ----
+ * A request loop for many concurrent planner instances: clients submit validity, motion and nearestK
+ * requests over their own device-resident worlds (checkers) and indices (gbo_nn); the server admits a
+ * request when a stream slot is free and its device footprint (inputs, outputs) fits in the server's
+ * arena, runs admitted requests concurrently on its streams, and frees slots and memory as requests
+ * complete (requests behind a blocked one are admitted when they fit). Inputs and outputs are host
+ * arrays (AoS rows; pinned memory copies fastest). Requests on one nearest-neighbour index run one at
+ * a time (they share its scratch). No OMPL counterpart: OMPL's planners call the plugins one state at
+ * a time from their own threads (SURVEY: ParallelPlan, pRRT, CForest). */
+typedef struct gbo_server gbo_server;
+enum { GBO_REQ_VALIDITY = 0, GBO_REQ_MOTION = 1, GBO_REQ_KNN = 2 };
+typedef struct {
+    int kind;                 /* GBO_REQ_* */
+    gbo_checker *checker;     /* VALIDITY, MOTION */
+    gbo_nn *nn;               /* KNN */
+    const double *states;     /* VALIDITY states / MOTION s1 / KNN queries: n rows of dim doubles */
+    const double *states2;    /* MOTION s2 */
+    int64_t n;
+    int k;                    /* KNN */
+    int schedule;             /* MOTION: GBO_SCHEDULE_* (AUTO resolves to the checker's tuned choice) */
+    uint8_t *ok;              /* VALIDITY / MOTION: n bytes */
+    int32_t *first_j;         /* MOTION, nullable */
+    int32_t *nd;              /* MOTION, nullable */
+    int64_t *idx;             /* KNN: n*k */
+    double *dist;             /* KNN: n*k, nullable */
+} gbo_request;
+gbo_status gbo_server_create(int n_streams, int64_t arena_bytes, gbo_server **out);
+gbo_status gbo_server_destroy(gbo_server *s);
+/* Queue a request; it runs asynchronously. The arrays must stay valid until gbo_server_wait returns. */
+gbo_status gbo_server_submit(gbo_server *s, const gbo_request *req, uint64_t *ticket);
+/* Wait for a request (timeout_s < 0: no limit). latency_s: submit-to-completion time. The request's
+ * own status is returned (GBO_ERR_TIMEOUT if the wait ran out). */
+gbo_status gbo_server_wait(gbo_server *s, uint64_t ticket, double timeout_s, double *latency_s);
+gbo_status gbo_server_stats(gbo_server *s, uint64_t *submitted, uint64_t *completed, int64_t *arena_in_use,
+                            int *max_concurrent);
+
 /* ---- measurement helper ---- FP32 FMA throughput of this GPU (FLOP/s), for roofline denominators. */
 gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
 /* The FP32 cos/sin of the guarded kinematic-chain path for n FP64 angles (device arrays); exposed so

@@ -14,6 +14,15 @@ SPACE_REAL_VECTOR, SPACE_SO2, SPACE_KINEMATIC_CHAIN, SPACE_WRAP_L2 = 0, 1, 2, 3
 CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_FP32_GUARDED = 0, 1
 SCHEDULE_PLAIN, SCHEDULE_TILE, SCHEDULE_WARP, SCHEDULE_AUTO = 0, 1, 2, 3
+REQ_VALIDITY, REQ_MOTION, REQ_KNN = 0, 1, 2
+
+
+class Request(C.Structure):
+    """gbo_request (include/gbompl.h)."""
+    _fields_ = [("kind", C.c_int), ("checker", C.c_void_p), ("nn", C.c_void_p), ("states", C.c_void_p),
+                ("states2", C.c_void_p), ("n", C.c_int64), ("k", C.c_int), ("schedule", C.c_int),
+                ("ok", C.c_void_p), ("first_j", C.c_void_p), ("nd", C.c_void_p), ("idx", C.c_void_p),
+                ("dist", C.c_void_p)]
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -62,6 +71,12 @@ SIGNATURES = {
     "gbo_nn_nearest_r_host": (C.c_int, [_P, _P, C.c_double, _I64, C.POINTER(_I64), _P, _P]),
     "gbo_sample_uniform_host": (C.c_int, [_P, _I64, _P]),
     "gbo_sample_uniform_near_host": (C.c_int, [_P, _P, C.c_double, _I64, _P]),
+    "gbo_server_create": (C.c_int, [C.c_int, _I64, C.POINTER(_P)]),
+    "gbo_server_destroy": (C.c_int, [_P]),
+    "gbo_server_submit": (C.c_int, [_P, _P, C.POINTER(C.c_uint64)]),
+    "gbo_server_wait": (C.c_int, [_P, C.c_uint64, C.c_double, _D]),
+    "gbo_server_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(_I64),
+                                   C.POINTER(C.c_int)]),
     "gbo_measure_fp32_peak": (C.c_int, [_D, _P]),
     "gbo_measure_fp64_peak": (C.c_int, [_D, _P]),
     "gbo_sincos32": (C.c_int, [_P, _I64, _P, _P, _P]),

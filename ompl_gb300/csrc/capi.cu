@@ -1501,6 +1501,21 @@ gbo_status internal_ensure_device(int *sm_count)
     return GBO_OK;
 }
 
+gbo_status internal_request_dim(const gbo_request *r, int *dim)
+{
+    if (r->kind == GBO_REQ_KNN)
+    {
+        if (!r->nn)
+            return GBO_ERR_INVALID_ARGUMENT;
+        *dim = r->nn->sp.dim;
+        return GBO_OK;
+    }
+    if ((r->kind != GBO_REQ_VALIDITY && r->kind != GBO_REQ_MOTION) || !r->checker)
+        return GBO_ERR_INVALID_ARGUMENT;
+    *dim = r->checker->sp.dim;
+    return GBO_OK;
+}
+
 bool internal_nn_view(const gbo_nn *nn, NNArgs *a, SpaceParams *sp, int *precision, int *features)
 {
     if (!nn)
