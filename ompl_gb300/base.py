@@ -58,8 +58,8 @@ class StateSpace:
 
     def __init__(self, dim, low=None, high=None, param=0.0):
         self.dim = dim
-        self.low = None if low is None else np.asarray(low, dtype=np.float64).reshape(dim)
-        self.high = None if high is None else np.asarray(high, dtype=np.float64).reshape(dim)
+        self.low = None if low is None else np.array(np.broadcast_to(np.asarray(low, dtype=np.float64), (dim,)))
+        self.high = None if high is None else np.array(np.broadcast_to(np.asarray(high, dtype=np.float64), (dim,)))
         self.param = param
         self.fraction = 0.01
         self.factor = 1
@@ -130,8 +130,7 @@ class RealVectorStateSpace(StateSpace):
     kind = capi.SPACE_REAL_VECTOR
 
     def __init__(self, dim, low, high):
-        super().__init__(dim, np.broadcast_to(np.asarray(low, dtype=np.float64), (dim,)),
-                         np.broadcast_to(np.asarray(high, dtype=np.float64), (dim,)))
+        super().__init__(dim, low, high)
 
 
 class SO2StateSpace(StateSpace):
