@@ -270,15 +270,24 @@ int persistent_grid(const void *kernel, int block, unsigned smem, const LaunchCf
 {
     static std::mutex mu;
     static std::map<std::pair<const void *, unsigned>, int> occ;
+    static std::map<const void *, bool> raised;
     int per_sm = 0;
     {
         std::lock_guard<std::mutex> lk(mu);
+        if (smem > 48 * 1024 && !raised[kernel])
+        {
+            // raise the kernel's dynamic shared-memory limit once, to the device's opt-in maximum, so
+            // that launches with any world size up to it remain valid
+            int dev = 0, optin = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
+            raised[kernel] = true;
+        }
         auto key = std::make_pair(kernel, smem);
         auto it = occ.find(key);
         if (it == occ.end())
         {
-            if (smem > 48 * 1024)
-                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
             if (per_sm < 1)
                 per_sm = 1;

@@ -279,8 +279,13 @@ void launch_chain_hits(cudaStream_t s, const SpaceParams &sp, const WorldArgs &w
                        unsigned *bits, int words)
 {
     if (wa.bytes32 > 48 * 1024)
+    {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncSetAttribute((const void *)chain_hits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)wa.bytes32);
+                             optin - 1024);
+    }
     chain_hits_kernel<<<64, 256, wa.bytes32, s>>>(sp, wa, states, n, bits, words);
     note_launch();
 }
