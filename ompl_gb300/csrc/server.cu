@@ -240,7 +240,9 @@ void gbo_server::run()
             ++completed;
             cv_done.notify_all();
         }
-        // admit pending requests into free slots, in arrival order, skipping those that do not fit yet
+        // admit pending requests into free slots, in arrival order, skipping those that do not fit yet;
+        // the admitted ones are launched after the lock is released (submit() may append meanwhile)
+        std::vector<Job *> admit;
         for (auto it = pending.begin(); it != pending.end() && inflight < (int)slot_job.size();)
         {
             Job *j = *it;
@@ -268,9 +270,15 @@ void gbo_server::run()
             ++inflight;
             max_inflight = std::max(max_inflight, inflight);
             it = pending.erase(it);
+            admit.push_back(j);
+        }
+        if (!admit.empty())
+        {
             lk.unlock();
-            launch(j);
+            for (Job *j : admit)
+                launch(j);
             lk.lock();
+            continue;  // re-check completions and the queue before sleeping
         }
         if (stop && pending.empty() && inflight == 0)
             break;
