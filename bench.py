@@ -449,13 +449,26 @@ def prm_bench(args):
     rm = prm.construct_roadmap(space, checker, w.extra["sampler_seed"], n)
     total = time.perf_counter() - t
     nm = rm.milestones.shape[1]
+    # the motion phase under each persistent schedule (the autotuner picks one per checker)
+    from ompl_gb300 import capi
+    mv = B.DiscreteMotionValidator(checker)
+    s1 = rm.milestones[:, rm.edge_src[:200_000]].contiguous()
+    s2 = rm.milestones[:, rm.edge_dst[:200_000]].contiguous()
+    sched = {}
+    for name, sch in (("tile", capi.SCHEDULE_TILE), ("warp", capi.SCHEDULE_WARP)):
+        mv.checkMotions(s1, s2, schedule=sch, soa=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mv.checkMotions(s1, s2, schedule=sch, soa=True)
+        torch.cuda.synchronize()
+        sched[name] = s1.shape[1] / (time.perf_counter() - t0)
     comps = prm.connected_components(nm, rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy())
     print(json.dumps({"metric": "PRM roadmap construction (DH arm, 16384 spheres)", "samples": n,
                       "milestones": nm, "candidate_edges": rm.candidate_edges, "edges": int(rm.edge_src.numel()),
                       "components": comps, "total_s": total, "timings_ms": rm.timings_ms,
                       "edges_per_s": rm.candidate_edges / (rm.timings_ms["motion"] * 1e-3),
                       "knn_queries_per_s": nm / (rm.timings_ms["nn add+prefix kNN"] * 1e-3),
-                      "checked_states": rm.checked_states}))
+                      "checked_states": rm.checked_states, "valid_edge_schedules_edges_per_s": sched}))
 
 
 def serve_bench(args):

@@ -145,26 +145,35 @@ struct Pinned
     }
 };
 
+// Per-object device scratch that grows geometrically with the stream-ordered allocator. Outgrown
+// buffers are kept until the object is destroyed: freeing them during a call would synchronise the
+// whole device (cudaFree) and stall every other stream.
 struct DevBuf
 {
     void *p = nullptr;
     size_t bytes = 0;
-    gbo_status reserve(size_t b)
+    std::vector<void *> outgrown;
+    gbo_status reserve(size_t b, cudaStream_t stream = nullptr)
     {
         if (b <= bytes)
             return GBO_OK;
+        const size_t want = std::max(b, 2 * bytes);
+        void *np = nullptr;
+        CUDA_TRY(cudaMallocAsync(&np, want, stream));
         if (p)
-            cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        CUDA_TRY(cudaMalloc(&p, b));
-        bytes = b;
+            outgrown.push_back(p);
+        p = np;
+        bytes = want;
         return GBO_OK;
     }
     ~DevBuf()
     {
+        if (p || !outgrown.empty())
+            cudaDeviceSynchronize();
         if (p)
             cudaFree(p);
+        for (void *q : outgrown)
+            cudaFree(q);
     }
 };
 
@@ -188,6 +197,7 @@ struct gbo_checker
     WorldArgs wa{};
     void *d64 = nullptr, *d32 = nullptr;
     int *cell_start = nullptr, *cell_items = nullptr;
+    float *cell_items4 = nullptr;
     unsigned *test_order = nullptr;
     CounterRing ctr;
     int tuned_schedule = -1;
@@ -205,6 +215,8 @@ struct gbo_checker
             cudaFree(cell_start);
         if (cell_items)
             cudaFree(cell_items);
+        if (cell_items4)
+            cudaFree(cell_items4);
         if (test_order)
             cudaFree(test_order);
         if (host_stream)
@@ -772,7 +784,7 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         }
         wa.data32 = c->d32;
         wa.bytes32 = (unsigned)b32;
-        wa.stage32 = b32 > 0 && b32 <= 160 * 1024;
+        wa.stage32 = 0;  // the FP32 narrow phase reads the spheres listed in the grid cells (cell_items4)
         // FK error bound in FP32 (spectral-norm propagation): |dR_k| <= k (2 eps_t + 16u),
         // |dp| <= sum_k (|dR_k| |pA| + |pA| (eps_t + u) + 4u (|p| + |pA|)); centres add 3u|p|.
         const double u = kU32, eps_t = u * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
@@ -789,8 +801,10 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         const double D = 2.0 * (sphere_radius + rmax);
         const double E = 2.0 * D * dc + dc * dc + 8.0 * u * D * D + 4.0 * u * (D * D);
         wa.dh_e = (float)(2.0 * E);
-        // uniform grid: each sphere goes into every cell its box grown by rs + margin overlaps
-        const int G = 32;
+        // uniform 64^3 grid: a sphere is listed in every cell whose box lies within rs + ro + margin of its
+        // centre (exact sphere-box distance), so the cell holding a robot sphere centre lists every world
+        // sphere that can touch it; cells store the index (FP64 path) and the FP32 sphere itself.
+        const int G = 64;
         const double margin = 1e-3;
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
         for (int64_t i = 0; i < n_world; ++i)
@@ -806,45 +820,66 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
                 lo[r] = -1;
                 hi[r] = 1;
             }
-        double inv[3];
+        double inv[3], cell[3];
         for (int r = 0; r < 3; ++r)
         {
             lo[r] -= margin;
             hi[r] += margin;
             inv[r] = G / (hi[r] - lo[r]);
+            cell[r] = (hi[r] - lo[r]) / G;
             wa.glo64[r] = lo[r];
             wa.ginv64[r] = inv[r];
             wa.glo[r] = (float)lo[r];
             wa.ginv[r] = (float)inv[r];
         }
-        std::vector<std::vector<int>> cells((size_t)G * G * G);
-        for (int64_t i = 0; i < n_world; ++i)
-        {
+        const size_t ncell = (size_t)G * G * G;
+        std::vector<int> start(ncell + 1, 0);
+        auto visit = [&](int64_t i, auto &&emit) {
+            const double ext = world[4 * i + 3] + sphere_radius + margin;
             int c0[3], c1[3];
             for (int r = 0; r < 3; ++r)
             {
-                const double ext = world[4 * i + 3] + sphere_radius + margin;
                 c0[r] = std::max(0, (int)std::floor((world[4 * i + r] - ext - lo[r]) * inv[r]) - 1);
                 c1[r] = std::min(G - 1, (int)std::floor((world[4 * i + r] + ext - lo[r]) * inv[r]) + 1);
             }
             for (int x = c0[0]; x <= c1[0]; ++x)
                 for (int y = c0[1]; y <= c1[1]; ++y)
                     for (int z = c0[2]; z <= c1[2]; ++z)
-                        cells[((size_t)x * G + y) * G + z].push_back((int)i);
-        }
-        std::vector<int> start(cells.size() + 1, 0), items;
-        for (size_t k = 0; k < cells.size(); ++k)
-        {
-            start[k + 1] = start[k] + (int)cells[k].size();
-            items.insert(items.end(), cells[k].begin(), cells[k].end());
-        }
-        if (items.empty())
-            items.push_back(0);
+                    {
+                        const int ix[3] = {x, y, z};
+                        double d2 = 0.0;
+                        for (int r = 0; r < 3; ++r)
+                        {
+                            const double b0 = lo[r] + ix[r] * cell[r], b1 = b0 + cell[r];
+                            const double o = world[4 * i + r];
+                            const double g = o < b0 ? b0 - o : (o > b1 ? o - b1 : 0.0);
+                            d2 += g * g;
+                        }
+                        if (d2 <= ext * ext * (1.0 + 1e-9))
+                            emit(((size_t)x * G + y) * G + z);
+                    }
+        };
+        for (int64_t i = 0; i < n_world; ++i)
+            visit(i, [&](size_t k) { start[k + 1]++; });
+        for (size_t k = 0; k < ncell; ++k)
+            start[k + 1] += start[k];
+        std::vector<int> fill(start.begin(), start.end() - 1), items(std::max(1, start[ncell]));
+        std::vector<float> items4(4 * items.size(), 0.f);
+        for (int64_t i = 0; i < n_world; ++i)
+            visit(i, [&](size_t k) {
+                const int pos = fill[k]++;
+                items[pos] = (int)i;
+                for (int r = 0; r < 4; ++r)
+                    items4[4 * (size_t)pos + r] = (float)world[4 * i + r];
+            });
         if (cudaMalloc(&c->cell_start, start.size() * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&c->cell_items, items.size() * sizeof(int)) != cudaSuccess)
+            cudaMalloc(&c->cell_items, items.size() * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&c->cell_items4, items4.size() * sizeof(float)) != cudaSuccess)
             return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "grid allocation failed"));
         cudaMemcpy(c->cell_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice);
         cudaMemcpy(c->cell_items, items.data(), items.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->cell_items4, items4.data(), items4.size() * sizeof(float), cudaMemcpyHostToDevice);
+        wa.cell_items4 = (const float4 *)c->cell_items4;
         wa.cell_start = c->cell_start;
         wa.cell_items = c->cell_items;
         wa.grid_n = G;
@@ -1012,9 +1047,9 @@ gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, ui
     const size_t bin = (size_t)n * c->sp.dim * sizeof(double);
     if (auto st = c->pin_in.reserve(bin))
         return st;
-    if (auto st = c->dev_in.reserve(bin))
+    if (auto st = c->dev_in.reserve(bin, c->host_stream))
         return st;
-    if (auto st = c->dev_out.reserve((size_t)n))
+    if (auto st = c->dev_out.reserve((size_t)n, c->host_stream))
         return st;
     std::memcpy(c->pin_in.p, states, bin);
     CUDA_TRY(cudaMemcpyAsync(c->dev_in.p, c->pin_in.p, bin, cudaMemcpyHostToDevice, c->host_stream));
@@ -1039,7 +1074,7 @@ gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double 
     // device layout: s1 | s2 | first_j | nd | ok | last_t | last_state
     const size_t off_fj = 2 * bst, off_nd = off_fj + 4 * (size_t)n, off_ok = off_nd + 4 * (size_t)n;
     const size_t off_lt = pad16(off_ok + (size_t)n), off_ls = off_lt + 8 * (size_t)n, total = off_ls + bst;
-    if (auto st = c->dev_in.reserve(total))
+    if (auto st = c->dev_in.reserve(total, c->host_stream))
         return st;
     char *d = (char *)c->dev_in.p;
     // the endpoints go straight from the caller's arrays to the device (no staging copy on the host)
@@ -1260,15 +1295,15 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
     nn->queries += nq;
     if (nn->precision == GBO_PRECISION_FP32_GUARDED && k <= 20)
     {
-        if (auto st = nn->qfeat.reserve(sizeof(float) * nn->F * nq))
+        if (auto st = nn->qfeat.reserve(sizeof(float) * nn->F * nq, lc.stream))
             return st;
-        if (auto st = nn->fb_list.reserve(sizeof(unsigned long long) * nq))
+        if (auto st = nn->fb_list.reserve(sizeof(unsigned long long) * nq, lc.stream))
             return st;
         unsigned long long *fb_n = &ctr->queue;
         const int P = knn_chunks(lc, nq, nn->size);
         const int keep = k <= 12 ? 16 : 24;
         const size_t pl = (size_t)P * nq * keep;
-        if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + 64))
+        if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + 64, lc.stream))
             return st;
         int64_t *part_k = (int64_t *)nn->part.p;
         float *part_d = (float *)(part_k + pl);
@@ -1332,7 +1367,7 @@ gbo_status gbo_nn_add_host(gbo_nn *nn, const double *states, int64_t n, int64_t 
     const size_t b = (size_t)n * nn->sp.dim * sizeof(double);
     if (auto st = nn->pin.reserve(b + 16))
         return st;
-    if (auto st = nn->dev.reserve(b + 16))
+    if (auto st = nn->dev.reserve(b + 16, nn->host_stream))
         return st;
     std::memcpy(nn->pin.p, states, b);
     CUDA_TRY(cudaMemcpyAsync(nn->dev.p, nn->pin.p, b, cudaMemcpyHostToDevice, nn->host_stream));
@@ -1349,7 +1384,7 @@ gbo_status gbo_nn_remove_host(gbo_nn *nn, const int64_t *keys, int64_t n)
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad remove arguments");
     std::lock_guard<std::mutex> lk(nn->mu);
     const size_t b = (size_t)n * sizeof(int64_t);
-    if (auto st = nn->dev.reserve(b + 16))
+    if (auto st = nn->dev.reserve(b + 16, nn->host_stream))
         return st;
     CUDA_TRY(cudaMemcpyAsync(nn->dev.p, keys, b, cudaMemcpyHostToDevice, nn->host_stream));
     if (auto st = gbo_nn_remove(nn, (const int64_t *)nn->dev.p, n, nn->host_stream))
@@ -1366,7 +1401,7 @@ gbo_status gbo_nn_nearest_k_host(gbo_nn *nn, const double *q, int64_t nq, int k,
     const size_t bq = (size_t)nq * nn->sp.dim * sizeof(double), bo = (size_t)nq * k * 8;
     if (auto st = nn->pin.reserve(std::max(bq, 2 * bo) + 16))
         return st;
-    if (auto st = nn->dev.reserve(bq + 2 * bo + 32))
+    if (auto st = nn->dev.reserve(bq + 2 * bo + 32, nn->host_stream))
         return st;
     char *d = (char *)nn->dev.p;
     std::memcpy(nn->pin.p, q, bq);
@@ -1393,7 +1428,7 @@ gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t 
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestR arguments");
     std::lock_guard<std::mutex> lk(nn->mu);
     const int dim = nn->sp.dim;
-    if (auto st = nn->dev.reserve(64 + 16 * (size_t)(nn->size + 1) + 16 * (size_t)dim))
+    if (auto st = nn->dev.reserve(64 + 16 * (size_t)(nn->size + 1) + 16 * (size_t)dim, nn->host_stream))
         return st;
     char *d = (char *)nn->dev.p;
     double *dq = (double *)d;
@@ -1426,7 +1461,7 @@ gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out)
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
     std::lock_guard<std::mutex> lk(s->mu);
     const size_t b = (size_t)n * s->sp.dim * sizeof(double);
-    if (auto st = s->dev.reserve(b + 16))
+    if (auto st = s->dev.reserve(b + 16, s->host_stream))
         return st;
     if (auto st = s->pin.reserve(b + 16))
         return st;
@@ -1444,7 +1479,7 @@ gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, doub
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniformNear arguments");
     std::lock_guard<std::mutex> lk(s->mu);
     const size_t b = (size_t)n * s->sp.dim * sizeof(double);
-    if (auto st = s->dev.reserve(2 * b + 32))
+    if (auto st = s->dev.reserve(2 * b + 32, s->host_stream))
         return st;
     if (auto st = s->pin.reserve(b + 16))
         return st;

@@ -44,6 +44,7 @@ struct WorldArgs
     // uniform grid over the world spheres (cells hold spheres whose box grown by rs + margin overlaps)
     const int *cell_start;
     const int *cell_items;
+    const float4 *cell_items4;  // the listed spheres themselves (FP32), parallel to cell_items
     int grid_n;
     float glo[3], ginv[3];
     double glo64[3], ginv64[3];
@@ -198,8 +199,7 @@ __device__ int dh_valid32(const DHArm &arm, const double *q, const float4 *sph, 
             const int b = __ldg(wa.cell_start + cid), e = __ldg(wa.cell_start + cid + 1);
             for (int it = b; it < e; ++it)
             {
-                const int oi = __ldg(wa.cell_items + it);
-                const float4 o = wa.stage32 ? sph[oi] : __ldg(sph + oi);
+                const float4 o = __ldg(wa.cell_items4 + it);
                 const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
                 const float rr = rs + o.w;
                 const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
