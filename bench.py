@@ -305,13 +305,14 @@ def ours(args, rank, world, local_rank):
         return
     peak_fp32 = B.measure_fp32_peak()
     achieved = mean_checked * FLOP_PER_STATE / (mean_ms * 1e-3)
+    # DRAM read + write bytes of one launch of the timed kernel, from the committed ncu summary
+    # (same 100k-edge batch as one step)
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "motion_tile_chain10_traffic.json")
+    prof = os.path.join(ROOT, "profiles", "chain_motion_warp_kernel_chain10.md")
     if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+        for line in open(prof):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
     # CPU baseline: the oracle port on all host threads, bounded sample of batch 0
     from oracle.oracle import CheckerDesc, Oracle, SpaceDesc
     port = Oracle.port()

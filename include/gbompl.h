@@ -191,7 +191,8 @@ gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, doub
  * complete (requests behind a blocked one are admitted when they fit). Inputs and outputs are host
  * arrays (AoS rows; pinned memory copies fastest). Requests on one nearest-neighbour index run one at
  * a time (they share its scratch). No OMPL counterpart: OMPL's planners call the plugins one state at
- * a time from their own threads (SURVEY: ParallelPlan, pRRT, CForest). */
+ * a time from their own threads (tools/multiplan/ParallelPlan.h, geometric/planners/rrt/pRRT.h,
+ * geometric/planners/cforest/CForest.h). */
 typedef struct gbo_server gbo_server;
 enum { GBO_REQ_VALIDITY = 0, GBO_REQ_MOTION = 1, GBO_REQ_KNN = 2 };
 typedef struct {
