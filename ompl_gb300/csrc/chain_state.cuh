@@ -21,6 +21,17 @@ __device__ __forceinline__ int chain_test_count(int n_links, int nw, int &n_self
     return n_self + m * nw;
 }
 
+// Fields of a table entry: link a (bits 0-7), second segment b (bits 8-30: a link for a link-link
+// pair, else a world segment), link-link flag (bit 31).
+__host__ __device__ __forceinline__ int chain_test_a(unsigned e)
+{
+    return (int)(e & 0xffu);
+}
+__host__ __device__ __forceinline__ int chain_test_b(unsigned e)
+{
+    return (int)((e >> 8) & 0x7fffffu);
+}
+
 // Default order: self pairs row by row, then world-major link-world pairs.
 __host__ __device__ inline unsigned chain_test_entry(int idx, int n_links, int nw)
 {
@@ -119,68 +130,86 @@ __device__ __forceinline__ void chain_segments64_warp(double q, int lane, int n,
     }
 }
 
-// Warp-cooperative state test: kInvalid or kValid (same in all lanes). Tests run 32 per round in
-// table order; a lane whose FP32 comparison is ambiguous re-evaluates its own test with the FP64
-// reference code on the state's FP64 segments (built once per state, on the first ambiguity, from
-// q64(lane) = joint `lane` of the state in FP64). `rechecked` counts states that needed FP64.
+// Per-warp link records: the CTA's shared memory holds, after the world's segments, one block of
+// n_links + 1 ChainSegF32 records per warp, laid out like a world segment (start point, vector,
+// then the link-link error bounds), so that a link-link test reads its second segment exactly as a
+// link-world test reads a world segment. The bounds are written once per CTA; the start point and
+// vector are rewritten for every state the warp evaluates.
+__device__ __forceinline__ void init_chain_links(ChainSegF32 *links, int count, const ChainGuard &g)
+{
+    for (int k = threadIdx.x; k < count; k += blockDim.x)
+        links[k] = ChainSegF32{0.f, 0.f, 0.f, 0.f, g.self_den, g.self_s, g.self_t, g.self_u, g.self_v, 0.f, 0.f, 0.f};
+}
+
+// FP64 re-evaluation of the tests of one round whose FP32 result is ambiguous (reference operation
+// order): builds the state's FP64 segments from q = joint `lane` in FP64 and reruns the lanes whose
+// r is kAmbiguous. Warp-collective. Out of line so that the FP32 loop carries no FP64 values.
+static __device__ __noinline__ int chain_round64(int lane, int n, double L64, double q, unsigned e, int r,
+                                                 const double *w64)
+{
+    double sx0, sy0, sx1, sy1;
+    chain_segments64_warp(q, lane, n, L64, sx0, sy0, sx1, sy1);
+    const int a = chain_test_a(e), b = chain_test_b(e);
+    const double ax0 = __shfl_sync(0xffffffffu, sx0, a), ay0 = __shfl_sync(0xffffffffu, sy0, a);
+    const double ax1 = __shfl_sync(0xffffffffu, sx1, a), ay1 = __shfl_sync(0xffffffffu, sy1, a);
+    const double bx0 = __shfl_sync(0xffffffffu, sx0, b & 31), by0 = __shfl_sync(0xffffffffu, sy0, b & 31);
+    const double bx1 = __shfl_sync(0xffffffffu, sx1, b & 31), by1 = __shfl_sync(0xffffffffu, sy1, b & 31);
+    if (r != kAmbiguous)
+        return r;
+    bool hit;
+    if (e & 0x80000000u)
+        hit = seg_intersect64(ax0, ay0, ax1, ay1, bx0, by0, bx1, by1);
+    else
+    {
+        const double *o = w64 + 4 * (size_t)b;
+        hit = seg_intersect64(ax0, ay0, ax1, ay1, o[0], o[1], o[2], o[3]);
+    }
+    return hit ? kInvalid : kValid;
+}
+
+// Warp-cooperative state test: kInvalid or kValid (same in all lanes). Lane k <= n holds segment k
+// of the state (vector vx, vy; start px, py). `w` is the CTA's shared record array: the world's
+// segments at [0, nw), this warp's link records at [lb, lb + n + 1). Tests run 32 per round in table
+// order; a round with an ambiguous FP32 result re-evaluates those tests with the FP64 reference code
+// (chain_round64) from q64(lane) = joint `lane` of the state in FP64. `rechecked` counts states that
+// needed FP64.
 template <class Q64>
 __device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, float vx, float vy, float px,
-                                                  float py, const ChainSegF32 *w, const double *w64,
-                                                  const unsigned *tab, ChainTables t, ChainGuard g, Q64 q64,
-                                                  unsigned &rechecked)
+                                                  float py, ChainSegF32 *w, int lb, const double *w64,
+                                                  const unsigned *tab, ChainTables t, Q64 q64, unsigned &rechecked)
 {
+    __syncwarp();  // the previous state's records are no longer read
+    if (lane <= n)
+        *(float4 *)&w[lb + lane] = make_float4(px, py, vx, vy);
+    __syncwarp();
     bool have64 = false;
-    double sx0 = 0.0, sy0 = 0.0, sx1 = 0.0, sy1 = 0.0;
     for (int base = 0; base < t.n_tests; base += 32)
     {
         const int idx = base + lane;
         int r = kValid;
-        const unsigned e = idx < t.n_tests ? tab[idx] : 0u;
-        const int a = (int)(e & 0xff), b = (int)((e >> 8) & 0xffffff);
-        const bool self = (e & 0x80000000u) != 0u;
-        const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
-        const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
-        const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);
-        const float bpx = __shfl_sync(0xffffffffu, px, b & 31), bpy = __shfl_sync(0xffffffffu, py, b & 31);
+        unsigned e = 0u;
         if (idx < t.n_tests)
         {
-            if (self)
-                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_den, g.self_s, g.self_t, g.self_u,
-                                    g.self_v);
-            else
-            {
-                const ChainSegF32 ws = w[b];
-                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.e_den, ws.e_s, ws.e_t, ws.e_u,
-                                    ws.e_v);
-            }
+            e = tab[idx];
+            const int a = chain_test_a(e), b = chain_test_b(e);
+            const float4 A = *(const float4 *)&w[lb + a];
+            const ChainSegF32 B = w[(e & 0x80000000u) ? lb + b : b];
+            r = seg_intersect32(A.z, A.w, B.sx, B.sy, A.x - B.x0, A.y - B.y0, B.e_den, B.e_s, B.e_t, B.e_u, B.e_v);
         }
-        if (__any_sync(0xffffffffu, r == kAmbiguous))
+        if (__ballot_sync(0xffffffffu, r != kValid))
         {
-            if (!have64)
+            if (__any_sync(0xffffffffu, r == kAmbiguous))
             {
-                chain_segments64_warp(q64(lane), lane, n, L64, sx0, sy0, sx1, sy1);
-                have64 = true;
-                ++rechecked;
-            }
-            const double ax0 = __shfl_sync(0xffffffffu, sx0, a), ay0 = __shfl_sync(0xffffffffu, sy0, a);
-            const double ax1 = __shfl_sync(0xffffffffu, sx1, a), ay1 = __shfl_sync(0xffffffffu, sy1, a);
-            const double bx0 = __shfl_sync(0xffffffffu, sx0, b & 31), by0 = __shfl_sync(0xffffffffu, sy0, b & 31);
-            const double bx1 = __shfl_sync(0xffffffffu, sx1, b & 31), by1 = __shfl_sync(0xffffffffu, sy1, b & 31);
-            if (r == kAmbiguous)
-            {
-                bool hit;
-                if (self)
-                    hit = seg_intersect64(ax0, ay0, ax1, ay1, bx0, by0, bx1, by1);
-                else
+                if (!have64)
                 {
-                    const double *o = w64 + 4 * (size_t)b;
-                    hit = seg_intersect64(ax0, ay0, ax1, ay1, o[0], o[1], o[2], o[3]);
+                    have64 = true;
+                    ++rechecked;
                 }
-                r = hit ? kInvalid : kValid;
+                r = chain_round64(lane, n, L64, q64(lane), e, r, w64);
             }
+            if (__any_sync(0xffffffffu, r == kInvalid))
+                return kInvalid;
         }
-        if (__any_sync(0xffffffffu, r == kInvalid))
-            return kInvalid;
     }
     return kValid;
 }
@@ -194,7 +223,7 @@ __device__ __forceinline__ void chain_state_hits32(int lane, float vx, float vy,
     {
         const int idx = base + lane;
         const unsigned e = idx < n_tests ? chain_test_entry(idx, n_links, nw) : 0u;
-        const int a = (int)(e & 0xff), b = (int)((e >> 8) & 0xffffff);
+        const int a = chain_test_a(e), b = chain_test_b(e);
         const float ax = __shfl_sync(0xffffffffu, vx, a), ay = __shfl_sync(0xffffffffu, vy, a);
         const float apx = __shfl_sync(0xffffffffu, px, a), apy = __shfl_sync(0xffffffffu, py, a);
         const float bvx = __shfl_sync(0xffffffffu, vx, b & 31), bvy = __shfl_sync(0xffffffffu, vy, b & 31);

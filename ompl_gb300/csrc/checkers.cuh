@@ -123,7 +123,7 @@ __device__ bool chain_valid64(const SpaceParams &s, const double *q, const doubl
 //   x0, y0, sx, sy  : start point and direction vector (s32) rounded to FP32
 //   e_den, e_s, e_t : bounds on |fp32 - fp64| of denom, s_numer and t_numer for a link vs this segment
 //   e_u, e_v        : bounds for s_numer - denom and t_numer - denom
-struct ChainSegF32
+struct __align__(16) ChainSegF32
 {
     float x0, y0, sx, sy, e_den, e_s, e_t, e_u, e_v, pad0, pad1, pad2;
 };
@@ -148,27 +148,25 @@ __device__ __forceinline__ int gt3(float x, float thr, float e)
 __device__ __forceinline__ int seg_intersect32(float s10x, float s10y, float s32x, float s32y, float s02x, float s02y,
                                                float e_den, float e_s, float e_t, float e_u, float e_v)
 {
+    // Branch-free: every clause is classified, then combined. Each clause of
+    // demos/KinematicChain.h:267-274 is "(cmp) == denomPositive => no collision"; one clause that
+    // definitely holds decides "no collision" whatever the others are, a collision needs all four
+    // to fail definitely, and an undecided sign or zero test of the denominator is undecided.
     constexpr float kFlt = 1.1920928955078125e-07f;
-    float den = fmaf(s10x, s32y, -s32x * s10y);
-    if (fabsf(den) <= e_den)
-        return kAmbiguous;  // collinearity / sign of denom not decided in FP32
+    const float den = fmaf(s10x, s32y, -s32x * s10y);
+    const float sn = fmaf(s10x, s02y, -s10y * s02x);
+    const float tn = fmaf(s32x, s02y, -s32y * s02x);
+    const float un = sn - den, vn = tn - den;
     const bool P = den > 0.f;
-    // each clause of demos/KinematicChain.h:267-274 is "(cmp) == denomPositive => no collision"
-    float sn = fmaf(s10x, s02y, -s10y * s02x);
-    int S = lt3(sn, kFlt, e_s);
-    if (S != 2 && (S == 1) == P)
-        return kValid;
-    float tn = fmaf(s32x, s02y, -s32y * s02x);
-    int T = lt3(tn, kFlt, e_t);
-    if (T != 2 && (T == 1) == P)
-        return kValid;
-    int U = gt3(sn - den, -kFlt, e_u);
-    if (U != 2 && (U == 1) == P)
-        return kValid;
-    int V = gt3(tn - den, kFlt, e_v);
-    if (V != 2 && (V == 1) == P)
-        return kValid;
-    return (S == 2 || T == 2 || U == 2 || V == 2) ? kAmbiguous : kInvalid;
+    // definite truth (x_t) and definite falsehood (x_f) of each comparison, as lt3 / gt3 classify them
+    const bool s_t = sn < kFlt - e_s, s_f = sn >= kFlt + e_s;
+    const bool t_t = tn < kFlt - e_t, t_f = tn >= kFlt + e_t;
+    const bool u_t = un > -kFlt + e_u, u_f = un <= -kFlt - e_u;
+    const bool v_t = vn > kFlt + e_v, v_f = vn <= kFlt - e_v;
+    const bool holds = P ? (s_t || t_t || u_t || v_t) : (s_f || t_f || u_f || v_f);
+    const bool undecided = !(s_t || s_f) || !(t_t || t_f) || !(u_t || u_f) || !(v_t || v_f);
+    const bool den_undecided = fabsf(den) <= e_den;
+    return den_undecided ? kAmbiguous : (holds ? kValid : (undecided ? kAmbiguous : kInvalid));
 }
 
 // FP32 link directions from an FP64 angle (thread-per-state forms): the angle is split exactly into

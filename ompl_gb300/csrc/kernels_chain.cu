@@ -17,10 +17,13 @@
 namespace gbo
 {
 
+// Dynamic shared memory of the warp kernels: the world's ChainSegF32 records (bytes32 = 48 * nw),
+// then (dim + 1) link records per warp, then the test table (one u32 per test).
 struct ChainSmem
 {
-    const ChainSegF32 *w32;
+    ChainSegF32 *w32;
     const unsigned *tab;
+    int lb;  // index of this warp's first link record in w32
     ChainTables t;
 };
 
@@ -29,11 +32,15 @@ __device__ bool chain_setup(const SpaceParams &sp, const WorldArgs &wa, unsigned
 {
     if (!stage_bulk(smem, wa.data32, wa.bytes32, bar, &ctr->timeout, &ctr->error))
         return false;
-    unsigned *tab = (unsigned *)(smem + wa.bytes32);
+    ChainSegF32 *w = (ChainSegF32 *)smem;
+    const int per_warp = sp.dim + 1, n_link_recs = (int)(blockDim.x >> 5) * per_warp;
+    init_chain_links(w + wa.n, n_link_recs, wa.guard);
+    unsigned *tab = (unsigned *)(w + wa.n + n_link_recs);
     build_chain_tables(sp.dim, wa.n, wa.test_order, tab, cs.t);
     __syncthreads();
-    cs.w32 = (const ChainSegF32 *)smem;
+    cs.w32 = w;
     cs.tab = tab;
+    cs.lb = wa.n + (int)(threadIdx.x >> 5) * per_warp;
     return true;
 }
 
@@ -86,8 +93,21 @@ __device__ __noinline__ int chain_nd64(const SpaceParams &sp, const StatesView &
     return segment_count_from_distance(sp, distance64<GBO_MAXD>(sp, a, b));
 }
 
-__global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v,
-                                                                  int64_t n, uint8_t *out, RunCounters *ctr)
+// Joint `ln` of checked state j of edge e in FP64, as DiscreteMotionValidator.cpp:63 forms it (j == top
+// is s2 itself). Out of line: inlined, the compiler hoists the loop-invariant FP64 division j / nd out
+// of the rarely taken re-check branch and executes it for every checked state.
+__device__ __noinline__ double motion_joint64(const StatesView &v1, const StatesView &v2, int64_t e, int ln, int j,
+                                              int nd, int top)
+{
+    if (j == top)
+        return v2(e, ln);
+    return interp_angle64(v1(e, ln), v2(e, ln), ddiv((double)j, (double)nd));
+}
+
+__global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(const __grid_constant__ SpaceParams sp,
+                                                                  const __grid_constant__ WorldArgs wa,
+                                                                  const __grid_constant__ StatesView v, int64_t n,
+                                                                  uint8_t *out, RunCounters *ctr)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
@@ -100,7 +120,6 @@ __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams
     const float L = (float)sp.link;
     const double L64 = sp.link;
     const int dim = sp.dim;
-    const ChainGuard g = wa.guard;
     const double *w64 = (const double *)wa.data64;
     unsigned rechecks = 0, evaluated = 0;
     for (int64_t i = warp; i < n; i += nwarps)
@@ -109,7 +128,7 @@ __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams
         float vx, vy, px, py;
         chain_segments32(lane_joint(v, i, lane, dim), lane, dim, L, vx, vy, px, py);
         auto q64 = [&](int ln) { return ln < dim ? v(i, ln) : 0.0; };
-        const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, w64, cs.tab, cs.t, g, q64,
+        const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t, q64,
                                          rechecks);
         if (lane == 0)
             out[i] = r == kValid ? 1 : 0;
@@ -123,9 +142,12 @@ __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(SpaceParams
     }
 }
 
-__global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1,
-                                                                StatesView v2, int64_t n, uint8_t *ok,
-                                                                int32_t *first_j, int32_t *nd_out, RunCounters *ctr)
+__global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(const __grid_constant__ SpaceParams sp,
+                                                                const __grid_constant__ WorldArgs wa,
+                                                                const __grid_constant__ StatesView v1,
+                                                                const __grid_constant__ StatesView v2, int64_t n,
+                                                                uint8_t *ok, int32_t *first_j, int32_t *nd_out,
+                                                                RunCounters *ctr)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
@@ -136,7 +158,6 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
     const int dim = sp.dim;
     const float L = (float)sp.link;
     const double L64 = sp.link;
-    const ChainGuard g = wa.guard;
     const double *w64 = (const double *)wa.data64;
     constexpr float kPiF = 3.14159265358979323846f;
     unsigned evaluated = 0, rechecks = 0;
@@ -210,16 +231,9 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(SpaceParams s
                 }
                 float vx, vy, px, py;
                 chain_segments32(q, lane, dim, L, vx, vy, px, py);
-                // joint `ln` of checked state j in FP64, as DiscreteMotionValidator.cpp:63 forms it
-                auto q64 = [&](int ln) {
-                    if (ln >= dim)
-                        return 0.0;
-                    if (j == top)
-                        return v2(e, ln);
-                    return interp_angle64(v1(e, ln), v2(e, ln), ddiv((double)j, (double)nd));
-                };
-                const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, w64, cs.tab, cs.t, g, q64,
-                                                 rechecks);
+                auto q64 = [&](int ln) { return ln < dim ? motion_joint64(v1, v2, e, ln, j, nd, top) : 0.0; };
+                const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t,
+                                                 q64, rechecks);
                 ++evaluated;
                 if (r == kInvalid)
                 {
@@ -290,11 +304,20 @@ void launch_chain_hits(cudaStream_t s, const SpaceParams &sp, const WorldArgs &w
     note_launch();
 }
 
-static unsigned chain_smem(const SpaceParams &sp, const WorldArgs &wa)
+static unsigned chain_smem(const SpaceParams &sp, const WorldArgs &wa, int block)
 {
     const int m = sp.dim + 1;
     const int n_tests = (m - 1) * (m - 2) / 2 + m * wa.n;
-    return wa.bytes32 + (unsigned)((4 * n_tests + 15) & ~15);
+    return wa.bytes32 + (unsigned)((block / 32) * m * sizeof(ChainSegF32)) + (unsigned)((4 * n_tests + 15) & ~15);
+}
+
+// The dynamic shared memory limit of a persistent kernel is raised to the opt-in maximum - 1 KB.
+static bool chain_smem_fits(unsigned bytes)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return (int64_t)bytes + 1024 <= (int64_t)optin;
 }
 
 bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
@@ -302,7 +325,9 @@ bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, cons
 {
     if (sp.dim > 31 || !wa.stage32)
         return false;
-    const unsigned sm = chain_smem(sp, wa);
+    const unsigned sm = chain_smem(sp, wa, 256);
+    if (!chain_smem_fits(sm))
+        return false;
     const int grid = persistent_grid((const void *)chain_validity_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
     chain_validity_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v, n, out, ctr);
     note_launch();
@@ -314,7 +339,9 @@ bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const 
 {
     if (sp.dim > 31 || !wa.stage32)
         return false;
-    const unsigned sm = chain_smem(sp, wa);
+    const unsigned sm = chain_smem(sp, wa, 256);
+    if (!chain_smem_fits(sm))
+        return false;
     const int grid = persistent_grid((const void *)chain_motion_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
     chain_motion_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v1, v2, n, ok, fj, nd, ctr);
     note_launch();
