@@ -7,9 +7,11 @@
 // Interpolated joints are formed in float-float from exact splits of s1 and s2:
 //   q_i(t) = s1_i + D_i t, D_i the shortest-arc difference of KinematicChain.h:150-176 (the wrap by
 //   2*pi that interpolate applies changes no sine or cosine), t = j / nd in float-float.
-// Anything the FP32 error bounds leave undecided is settled with the FP64 reference-order code:
-// an ambiguous state, an undecided segment count, or an edge whose joint difference lies within
-// 1e-9 of pi (where the interpolation branch itself would be uncertain).
+// Anything the FP32 error bounds leave undecided is settled with the FP64 reference-order code: an
+// ambiguous segment test (chain_round64), an undecided segment count (chain_nd64), and the states of
+// an edge whose joint difference lies within 1e-9 of pi, where the interpolation's own branch is not
+// settled in FP32 (motion_joint64). All FP64 work sits in small out-of-line functions: an inlined or
+// large call inside the edge loop costs the loop registers, and local-memory spills, on every edge.
 #include "chain_state.cuh"
 #include "kernels.cuh"
 #include "tma.cuh"
@@ -61,31 +63,7 @@ __device__ __noinline__ void load_pair64(const StatesView &v1, const StatesView 
     }
 }
 
-// DiscreteMotionValidator.cpp:48-91 for one edge.
-__device__ __noinline__ void chain_motion64(const SpaceParams &sp, const WorldArgs &wa, const StatesView &v1,
-                                           const StatesView &v2, int64_t e, int &nd, int &first)
-{
-    double a[GBO_MAXD], b[GBO_MAXD];
-    load_pair64(v1, v2, e, sp.dim, a, b);
-    nd = segment_count_from_distance(sp, distance64<GBO_MAXD>(sp, a, b));
-    first = -1;
-    const int top = nd > 1 ? nd : 1;
-    for (int j = 1; j <= top; ++j)
-    {
-        double q[GBO_MAXD];
-        if (j == top)
-            for (int d = 0; d < GBO_MAXD; ++d)
-                q[d] = b[d];
-        else
-            interpolate64<GBO_MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
-        if (!chain_valid64<GBO_MAXD>(sp, q, (const double *)wa.data64, wa.n))
-        {
-            first = j == top ? nd : j;
-            return;
-        }
-    }
-}
-
+// StateSpace::validSegmentCount of one edge in FP64 (StateSpace.cpp:851-854).
 __device__ __noinline__ int chain_nd64(const SpaceParams &sp, const StatesView &v1, const StatesView &v2, int64_t e)
 {
     double a[GBO_MAXD], b[GBO_MAXD];
@@ -174,72 +152,67 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(const __grid_
         // decided entirely in FP64 (the reference's branch on fabs(diff) <= pi is not settled here)
         ff diff = two_sum(b.hi, -a.hi);
         diff = fast_two_sum(diff.hi, diff.lo + (b.lo - a.lo));
+        // |diff| - pi in float-float: adh - float(pi) is exact, float(pi) - pi = 8.742278e-08 (the
+        // constant's own error is ~3e-15); the whole is good to ~1e-13, far inside the 1e-9 window
         const float adh = fabsf(diff.hi);
-        const bool near_pi = lane < dim && fabsf((adh - kPiF) + (diff.hi < 0.f ? -diff.lo : diff.lo) -
-                                                 (-8.742278e-08f)) < 1e-9f;
-        int nd = -2, first = -1;
-        if (__any_sync(0xffffffffu, near_pi))
+        const float over_pi = ((adh - kPiF) + (diff.hi < 0.f ? -diff.lo : diff.lo)) + 8.742278e-08f;
+        const bool near_pi = lane < dim && fabsf(over_pi) < 1e-9f;
+        // an edge with a joint difference within 1e-9 of pi builds its states with the FP64 reference
+        // interpolation (motion_joint64): the branch on fabs(diff) <= pi is not settled in FP32
+        const bool exact = __any_sync(0xffffffffu, near_pi);
+        ff D = diff;
+        if (lane < dim && over_pi > 0.f)  // the reference wraps when fabs(diff) > pi
         {
-            if (lane == 0)
-            {
-                chain_motion64(sp, wa, v1, v2, e, nd, first);
-                ++rechecks;
-            }
-            nd = __shfl_sync(0xffffffffu, nd, 0);
-            first = __shfl_sync(0xffffffffu, first, 0);
+            // D = diff - sign(diff) * 2*pi in float-float
+            const float sgn = diff.hi > 0.f ? -1.f : 1.f;
+            const ff t1 = two_sum(diff.hi, sgn * 6.28125f);
+            const ff t2 = two_sum(t1.hi, sgn * (519505.0f / 268435456.0f));
+            D = fast_two_sum(t2.hi, (t1.lo + t2.lo) + (diff.lo + sgn * 2.4308403e-10f));
         }
-        else
+        int nd = chain_segment_count_warp(a, b, lane, dim, L, wa.inv_lvs32, wa.e_dist, sp.factor);
+        const bool nd64 = nd < 0;
+        if (nd64)
         {
-            ff D = diff;
-            if (lane < dim && adh > kPiF)
+            // segment count not decided by the FP32 distance bound: the reference's FP64 count
+            if (lane == 0)
+                nd = chain_nd64(sp, v1, v2, e);
+            nd = __shfl_sync(0xffffffffu, nd, 0);
+        }
+        if (exact || nd64)
+            ++rechecks;
+        const int top = nd > 1 ? nd : 1;
+        // 1/nd in float-float
+        const float ndf = float_of(nd > 0 ? nd : 1);
+        const float inv_hi = __frcp_rn(ndf);
+        const float inv_lo = fmaf(-inv_hi, ndf, 1.0f) * inv_hi;
+        float jf = 0.f;
+        int first = -1;
+        for (int j = 1; j <= top; ++j)
+        {
+            jf += 1.0f;
+            ff q;
+            if (j == top)
+                q = b;
+            else if (exact)
+                q = lane < dim ? split_double(motion_joint64(v1, v2, e, lane, j, nd, top)) : ff{0.f, 0.f};
+            else
             {
-                // D = diff - sign(diff) * 2*pi in float-float
-                const float sgn = diff.hi > 0.f ? -1.f : 1.f;
-                const ff t1 = two_sum(diff.hi, sgn * 6.28125f);
-                const ff t2 = two_sum(t1.hi, sgn * (519505.0f / 268435456.0f));
-                D = fast_two_sum(t2.hi, (t1.lo + t2.lo) + (diff.lo + sgn * 2.4308403e-10f));
+                const float t_hi = jf * inv_hi;
+                const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
+                const float p_hi = D.hi * t_hi;
+                const float p_lo = fmaf(D.hi, t_hi, -p_hi) + fmaf(D.hi, t_lo, D.lo * t_hi);
+                q = lane < dim ? ff_add(a, {p_hi, p_lo}) : ff{0.f, 0.f};
             }
-            nd = chain_segment_count_warp(a, b, lane, dim, L, wa.inv_lvs32, wa.e_dist, sp.factor);
-            if (nd < 0)
+            float vx, vy, px, py;
+            chain_segments32(q, lane, dim, L, vx, vy, px, py);
+            auto q64 = [&](int ln) { return ln < dim ? motion_joint64(v1, v2, e, ln, j, nd, top) : 0.0; };
+            const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t, q64,
+                                             rechecks);
+            ++evaluated;
+            if (r == kInvalid)
             {
-                if (lane == 0)
-                {
-                    nd = chain_nd64(sp, v1, v2, e);
-                    ++rechecks;
-                }
-                nd = __shfl_sync(0xffffffffu, nd, 0);
-            }
-            const int top = nd > 1 ? nd : 1;
-            // 1/nd in float-float
-            const float ndf = float_of(nd > 0 ? nd : 1);
-            const float inv_hi = __frcp_rn(ndf);
-            const float inv_lo = fmaf(-inv_hi, ndf, 1.0f) * inv_hi;
-            float jf = 0.f;
-            for (int j = 1; j <= top; ++j)
-            {
-                jf += 1.0f;
-                ff q;
-                if (j == top)
-                    q = b;
-                else
-                {
-                    const float t_hi = jf * inv_hi;
-                    const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
-                    const float p_hi = D.hi * t_hi;
-                    const float p_lo = fmaf(D.hi, t_hi, -p_hi) + fmaf(D.hi, t_lo, D.lo * t_hi);
-                    q = lane < dim ? ff_add(a, {p_hi, p_lo}) : ff{0.f, 0.f};
-                }
-                float vx, vy, px, py;
-                chain_segments32(q, lane, dim, L, vx, vy, px, py);
-                auto q64 = [&](int ln) { return ln < dim ? motion_joint64(v1, v2, e, ln, j, nd, top) : 0.0; };
-                const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t,
-                                                 q64, rechecks);
-                ++evaluated;
-                if (r == kInvalid)
-                {
-                    first = j == top ? nd : j;
-                    break;
-                }
+                first = j == top ? nd : j;
+                break;
             }
         }
         if (lane == 0)

@@ -219,6 +219,39 @@ def test_chain_motion_valid_endpoints_vs_oracle(chain_case, port):
             assert np.array_equal(r["nd"], ref["nd"])
 
 
+def test_chain_motion_deferred_edges_vs_oracle(chain_case, port):
+    """Edges the FP32 warp kernel hands to its FP64 follow-up kernel: a joint difference within 1e-9
+    of pi (the interpolation's shortest-arc branch), and zero or tiny length (segment count not
+    decided by the FP32 distance bound); mixed with ordinary edges in one batch."""
+    w, sp, ckd, valid = chain_case
+    vs = w.states[valid == 1]
+    rng = np.random.default_rng(5)
+    n = 600
+    s1 = vs[rng.integers(0, len(vs), n)].copy()
+    s2 = vs[rng.integers(0, len(vs), n)].copy()
+    rows = np.arange(200)
+    k = rng.integers(0, w.dim, 200)
+    off = np.array([0.0, 5e-10, -5e-10, 2e-9])[rng.integers(0, 4, 200)]
+    base = s1[rows, k]
+    s2[rows, k] = np.clip(np.where(base > 0, base - math.pi, base + math.pi) + off, -math.pi, math.pi)
+    s2[200:300] = s1[200:300]                       # zero length
+    s2[300:350] = s1[300:350] + 1e-12               # below the FP32 distance bound
+    ref = port.check_motion(sp, ckd, s1, s2, want_state=False, want_bisect=False)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    mv = B.DiscreteMotionValidator(ck)
+    for p in ("fp64", "fp32_guarded"):
+        ck.setPrecision(p)
+        for sch in SCHEDULES:
+            r = mv.checkMotions(s1, s2, schedule=sch)
+            assert np.array_equal(r["ok"], ref["ok"]), (p, sch)
+            assert np.array_equal(r["first_j"], ref["first_j"]), (p, sch)
+            assert np.array_equal(r["nd"], ref["nd"]), (p, sch)
+    ck.setPrecision("fp32_guarded")
+    mv.checkMotions(s1, s2, schedule=capi.SCHEDULE_WARP)
+    assert ck.stats()["rechecked"] >= 200   # the last call's FP64 work: at least the deferred edges
+
+
 def test_dh_arm_motion_vs_oracle(port):
     w = W.config2(n_edges=400, n_world=1024)
     sp = SpaceDesc(w.space_kind, 7, w.low, w.high, lvs_fraction=w.lvs_fraction)
