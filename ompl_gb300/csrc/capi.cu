@@ -343,15 +343,29 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
         return 2.0 * (da * B + db * A + da * db) + 3.0 * u * A * B + 1e-15;
     };
     const double safety = 2.0;
+    // one bound e for the four numerator comparisons (that of s_numer - denom or t_numer - denom,
+    // which include the others), stored as the thresholds FLT_EPSILON -/+ e rounded outward
+    const double flt_eps = std::ldexp(1.0, -23);
+    auto down = [](double x) {
+        float f = (float)x;
+        return (double)f > x ? std::nextafter(f, -INFINITY) : f;
+    };
+    auto up = [](double x) {
+        float f = (float)x;
+        return (double)f < x ? std::nextafter(f, INFINITY) : f;
+    };
+    auto numer_bound = [&](double A, double B, double C, double eden, double es, double et) {
+        const double eu = es + eden + u * 2 * (A * C + A * B), ev = et + eden + u * 2 * (B * C + A * B);
+        return safety * std::max(std::max(es, et), std::max(eu, ev));
+    };
     g.eps_dir = (float)eps_dir;
     {
         const double A = L, B = L, C = 2 * R, dC = 2 * dP + 2 * u * R;
         const double eden = cross(A, B, dV, dV), es = cross(A, C, dV, dC), et = cross(B, C, dV, dC);
-        g.self_den = (float)(safety * eden + 1e-12);
-        g.self_s = (float)(safety * es);
-        g.self_t = (float)(safety * et);
-        g.self_u = (float)(safety * (es + eden + u * 2 * (A * C + A * B)));
-        g.self_v = (float)(safety * (et + eden + u * 2 * (B * C + A * B)));
+        const double e = numer_bound(A, B, C, eden, es, et);
+        g.self_den = up(safety * eden + 1e-12);
+        g.self_lo = down(flt_eps - e);
+        g.self_hi = up(flt_eps + e);
     }
     segs.resize(n);
     for (int j = 0; j < n; ++j)
@@ -368,11 +382,10 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
         s.y0 = (float)y0;
         s.sx = (float)sx;
         s.sy = (float)sy;
-        s.e_den = (float)(safety * eden + 1e-12);
-        s.e_s = (float)(safety * es);
-        s.e_t = (float)(safety * et);
-        s.e_u = (float)(safety * (es + eden + u * 2 * (A * C + A * B)));
-        s.e_v = (float)(safety * (et + eden + u * 2 * (B * C + A * B)));
+        const double e = numer_bound(A, B, C, eden, es, et);
+        s.e_den = up(safety * eden + 1e-12);
+        s.lo = down(flt_eps - e);
+        s.hi = up(flt_eps + e);
         segs[j] = s;
     }
     // workspace distance (segment_count, FP32 form): dx_i accumulates 2i direction errors and i

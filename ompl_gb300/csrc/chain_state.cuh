@@ -138,7 +138,7 @@ __device__ __forceinline__ void chain_segments64_warp(double q, int lane, int n,
 __device__ __forceinline__ void init_chain_links(ChainSegF32 *links, int count, const ChainGuard &g)
 {
     for (int k = threadIdx.x; k < count; k += blockDim.x)
-        links[k] = ChainSegF32{0.f, 0.f, 0.f, 0.f, g.self_den, g.self_s, g.self_t, g.self_u, g.self_v, 0.f, 0.f, 0.f};
+        links[k] = ChainSegF32{0.f, 0.f, 0.f, 0.f, g.self_lo, g.self_hi, g.self_den, 0.f};
 }
 
 // FP64 re-evaluation of the tests of one round whose FP32 result is ambiguous (reference operation
@@ -194,7 +194,7 @@ __device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, f
             const int a = chain_test_a(e), b = chain_test_b(e);
             const float4 A = *(const float4 *)&w[lb + a];
             const ChainSegF32 B = w[(e & 0x80000000u) ? lb + b : b];
-            r = seg_intersect32(A.z, A.w, B.sx, B.sy, A.x - B.x0, A.y - B.y0, B.e_den, B.e_s, B.e_t, B.e_u, B.e_v);
+            r = seg_intersect32(A.z, A.w, B.sx, B.sy, A.x - B.x0, A.y - B.y0, B.lo, B.hi, B.e_den);
         }
         if (__ballot_sync(0xffffffffu, r != kValid))
         {
@@ -232,13 +232,11 @@ __device__ __forceinline__ void chain_state_hits32(int lane, float vx, float vy,
         if (idx < n_tests)
         {
             if (e & 0x80000000u)
-                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_den, g.self_s, g.self_t, g.self_u,
-                                    g.self_v);
+                r = seg_intersect32(ax, ay, bvx, bvy, apx - bpx, apy - bpy, g.self_lo, g.self_hi, g.self_den);
             else
             {
                 const ChainSegF32 ws = w[b];
-                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.e_den, ws.e_s, ws.e_t, ws.e_u,
-                                    ws.e_v);
+                r = seg_intersect32(ax, ay, ws.sx, ws.sy, apx - ws.x0, apy - ws.y0, ws.lo, ws.hi, ws.e_den);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, r == kInvalid);

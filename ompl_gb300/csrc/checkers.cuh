@@ -119,19 +119,21 @@ __device__ bool chain_valid64(const SpaceParams &s, const double *q, const doubl
 }
 
 // ---------------------------------------------------------------- kinematic chain (FP32, guarded)
-// Per world segment, FP32 data plus its error bounds (filled by the host, see chain_bounds in capi.cu):
-//   x0, y0, sx, sy  : start point and direction vector (s32) rounded to FP32
-//   e_den, e_s, e_t : bounds on |fp32 - fp64| of denom, s_numer and t_numer for a link vs this segment
-//   e_u, e_v        : bounds for s_numer - denom and t_numer - denom
+// Per world segment, FP32 data plus its error bounds (filled by the host, see chain_bounds in capi.cu),
+// 32 bytes = two 16-byte loads:
+//   x0, y0, sx, sy : start point and direction vector (s32) rounded to FP32
+//   lo, hi         : FLT_EPSILON - e and FLT_EPSILON + e rounded outward, e a bound on |fp32 - fp64| of
+//                    s_numer, t_numer, s_numer - denom and t_numer - denom for a link vs this segment
+//   e_den          : bound on |fp32 - fp64| of denom
 struct __align__(16) ChainSegF32
 {
-    float x0, y0, sx, sy, e_den, e_s, e_t, e_u, e_v, pad0, pad1, pad2;
+    float x0, y0, sx, sy, lo, hi, e_den, pad;
 };
 
 struct ChainGuard
 {
-    float eps_dir;   // bound on |cos/sin fp32 - fp64| of one link direction
-    float self_den, self_s, self_t, self_u, self_v;  // bounds for link-vs-link tests
+    float eps_dir;                      // bound on |cos/sin fp32 - fp64| of one link direction
+    float self_lo, self_hi, self_den;   // lo, hi, e_den of link-vs-link tests
 };
 
 // 3-valued "x < thr" with |x - x_ref| <= e: returns 1 (true), 0 (false), 2 (ambiguous).
@@ -145,24 +147,27 @@ __device__ __forceinline__ int gt3(float x, float thr, float e)
 }
 
 // Guarded segment test: returns kInvalid (definite collision), kValid (definite none) or kAmbiguous.
+// Branch-free: every clause of demos/KinematicChain.h:267-274 ("(cmp) == denomPositive => no
+// collision") is classified, then combined: one clause that definitely holds decides "no
+// collision" whatever the others are, a collision needs all four to fail definitely, and an
+// undecided zero or sign test of the denominator is undecided. With |x32 - x64| <= e/2 for every
+// numerator x (the bounds carry a safety factor of 2), "x < FLT_EPSILON" is definitely true when
+// x32 < lo = FLT_EPSILON - e and definitely false when x32 >= hi = FLT_EPSILON + e; the clauses on
+// s_numer - denom and t_numer - denom compare against -FLT_EPSILON (thresholds -lo, -hi) and
+// +FLT_EPSILON.
 __device__ __forceinline__ int seg_intersect32(float s10x, float s10y, float s32x, float s32y, float s02x, float s02y,
-                                               float e_den, float e_s, float e_t, float e_u, float e_v)
+                                               float lo, float hi, float e_den)
 {
-    // Branch-free: every clause is classified, then combined. Each clause of
-    // demos/KinematicChain.h:267-274 is "(cmp) == denomPositive => no collision"; one clause that
-    // definitely holds decides "no collision" whatever the others are, a collision needs all four
-    // to fail definitely, and an undecided sign or zero test of the denominator is undecided.
-    constexpr float kFlt = 1.1920928955078125e-07f;
     const float den = fmaf(s10x, s32y, -s32x * s10y);
     const float sn = fmaf(s10x, s02y, -s10y * s02x);
     const float tn = fmaf(s32x, s02y, -s32y * s02x);
     const float un = sn - den, vn = tn - den;
     const bool P = den > 0.f;
-    // definite truth (x_t) and definite falsehood (x_f) of each comparison, as lt3 / gt3 classify them
-    const bool s_t = sn < kFlt - e_s, s_f = sn >= kFlt + e_s;
-    const bool t_t = tn < kFlt - e_t, t_f = tn >= kFlt + e_t;
-    const bool u_t = un > -kFlt + e_u, u_f = un <= -kFlt - e_u;
-    const bool v_t = vn > kFlt + e_v, v_f = vn <= kFlt - e_v;
+    // definite truth (x_t) and definite falsehood (x_f) of each comparison
+    const bool s_t = sn < lo, s_f = sn >= hi;
+    const bool t_t = tn < lo, t_f = tn >= hi;
+    const bool u_t = un > -lo, u_f = un <= -hi;
+    const bool v_t = vn > hi, v_f = vn <= lo;
     const bool holds = P ? (s_t || t_t || u_t || v_t) : (s_f || t_f || u_f || v_f);
     const bool undecided = !(s_t || s_f) || !(t_t || t_f) || !(u_t || u_f) || !(v_t || v_f);
     const bool den_undecided = fabsf(den) <= e_den;
@@ -215,8 +220,8 @@ __device__ int chain_valid32(const SpaceParams &s, const double *q, const ChainS
         for (int j = i + 2; j < MAXD + 1; ++j)
             if (j < m)
             {
-                int r = seg_intersect32(VX[i], VY[i], VX[j], VY[j], X[i] - X[j], Y[i] - Y[j], g.self_den, g.self_s,
-                                        g.self_t, g.self_u, g.self_v);
+                int r = seg_intersect32(VX[i], VY[i], VX[j], VY[j], X[i] - X[j], Y[i] - Y[j], g.self_lo, g.self_hi,
+                                        g.self_den);
                 if (r == kInvalid)
                     return kInvalid;
                 amb |= (r == kAmbiguous);
@@ -228,8 +233,8 @@ __device__ int chain_valid32(const SpaceParams &s, const double *q, const ChainS
         for (int i = 0; i < MAXD + 1; ++i)
             if (i < m)
             {
-                int r = seg_intersect32(VX[i], VY[i], ws.sx, ws.sy, X[i] - ws.x0, Y[i] - ws.y0, ws.e_den, ws.e_s,
-                                        ws.e_t, ws.e_u, ws.e_v);
+                int r = seg_intersect32(VX[i], VY[i], ws.sx, ws.sy, X[i] - ws.x0, Y[i] - ws.y0, ws.lo, ws.hi,
+                                        ws.e_den);
                 if (r == kInvalid)
                     return kInvalid;
                 amb |= (r == kAmbiguous);

@@ -19,7 +19,7 @@
 namespace gbo
 {
 
-// Dynamic shared memory of the warp kernels: the world's ChainSegF32 records (bytes32 = 48 * nw),
+// Dynamic shared memory of the warp kernels: the world's ChainSegF32 records (bytes32 = 32 * nw),
 // then (dim + 1) link records per warp, then the test table (one u32 per test).
 struct ChainSmem
 {
