@@ -1050,6 +1050,20 @@ gbo_status gbo_check_motion_states(gbo_checker *c, const double *states, int64_t
     return GBO_OK;
 }
 
+// Device address of a page-locked host array (cudaMallocHost / cudaHostRegister), or null for
+// pageable or device memory. Kernels read and write such arrays in place over the coherent host
+// link, so the transfer overlaps with the work inside the launch instead of preceding it.
+static void *mapped_host(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, uint8_t *out)
 {
     if (!c || n < 0 || (n > 0 && (!states || !out)))
@@ -1058,18 +1072,28 @@ gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, ui
         return GBO_OK;
     std::lock_guard<std::mutex> lk(c->mu);
     const size_t bin = (size_t)n * c->sp.dim * sizeof(double);
-    if (auto st = c->pin_in.reserve(bin))
-        return st;
-    if (auto st = c->dev_in.reserve(bin, c->host_stream))
-        return st;
-    if (auto st = c->dev_out.reserve((size_t)n, c->host_stream))
-        return st;
-    std::memcpy(c->pin_in.p, states, bin);
-    CUDA_TRY(cudaMemcpyAsync(c->dev_in.p, c->pin_in.p, bin, cudaMemcpyHostToDevice, c->host_stream));
-    if (auto st = gbo_is_valid(c, (const double *)c->dev_in.p, n, c->sp.dim, GBO_LAYOUT_AOS, (uint8_t *)c->dev_out.p,
+    const double *din = (const double *)mapped_host(states);
+    uint8_t *dout = (uint8_t *)mapped_host(out);
+    if (!din)
+    {
+        if (auto st = c->pin_in.reserve(bin))
+            return st;
+        if (auto st = c->dev_in.reserve(bin, c->host_stream))
+            return st;
+        std::memcpy(c->pin_in.p, states, bin);
+        CUDA_TRY(cudaMemcpyAsync(c->dev_in.p, c->pin_in.p, bin, cudaMemcpyHostToDevice, c->host_stream));
+        din = (const double *)c->dev_in.p;
+    }
+    if (!dout)
+    {
+        if (auto st = c->dev_out.reserve((size_t)n, c->host_stream))
+            return st;
+    }
+    if (auto st = gbo_is_valid(c, din, n, c->sp.dim, GBO_LAYOUT_AOS, dout ? dout : (uint8_t *)c->dev_out.p,
                                c->host_stream))
         return st;
-    CUDA_TRY(cudaMemcpyAsync(out, c->dev_out.p, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+    if (!dout)
+        CUDA_TRY(cudaMemcpyAsync(out, c->dev_out.p, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
     CUDA_TRY(cudaStreamSynchronize(c->host_stream));
     return GBO_OK;
 }
@@ -1084,34 +1108,44 @@ gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double 
     std::lock_guard<std::mutex> lk(c->mu);
     const int dim = c->sp.dim;
     const size_t bst = (size_t)n * dim * sizeof(double);
-    // device layout: s1 | s2 | first_j | nd | ok | last_t | last_state
-    const size_t off_fj = 2 * bst, off_nd = off_fj + 4 * (size_t)n, off_ok = off_nd + 4 * (size_t)n;
+    // page-locked arrays are used in place (mapped_host); the others go through device buffers
+    const double *m1 = (const double *)mapped_host(s1), *m2 = (const double *)mapped_host(s2);
+    const bool in_place = m1 && m2;
+    uint8_t *mok = (uint8_t *)mapped_host(ok);
+    double *mlt = (double *)mapped_host(last_t), *mls = (double *)mapped_host(last_state);
+    // device layout: [s1 | s2 (copy path)] | first_j | nd | ok | last_t | last_state
+    const size_t off_fj = in_place ? 0 : 2 * bst, off_nd = off_fj + 4 * (size_t)n, off_ok = off_nd + 4 * (size_t)n;
     const size_t off_lt = pad16(off_ok + (size_t)n), off_ls = off_lt + 8 * (size_t)n, total = off_ls + bst;
     if (auto st = c->dev_in.reserve(total, c->host_stream))
         return st;
     char *d = (char *)c->dev_in.p;
-    // the endpoints go straight from the caller's arrays to the device (no staging copy on the host)
-    CUDA_TRY(cudaMemcpyAsync(d, s1, bst, cudaMemcpyHostToDevice, c->host_stream));
-    CUDA_TRY(cudaMemcpyAsync(d + bst, s2, bst, cudaMemcpyHostToDevice, c->host_stream));
+    if (!in_place)
+    {
+        // straight from the caller's arrays to the device (no staging copy on the host)
+        CUDA_TRY(cudaMemcpyAsync(d, s1, bst, cudaMemcpyHostToDevice, c->host_stream));
+        CUDA_TRY(cudaMemcpyAsync(d + bst, s2, bst, cudaMemcpyHostToDevice, c->host_stream));
+        m1 = (const double *)d;
+        m2 = (const double *)(d + bst);
+    }
+    uint8_t *okd = mok ? mok : (uint8_t *)(d + off_ok);
+    int32_t *fj = (int32_t *)(d + off_fj), *ndv = (int32_t *)(d + off_nd);
     const int sched = c->precision == GBO_PRECISION_FP64 ? GBO_SCHEDULE_PLAIN : GBO_SCHEDULE_AUTO;
-    if (auto st = gbo_check_motion(c, (const double *)d, (const double *)(d + bst), n, dim, GBO_LAYOUT_AOS, sched,
-                                   (uint8_t *)(d + off_ok), (int32_t *)(d + off_fj), (int32_t *)(d + off_nd),
-                                   c->host_stream))
+    if (auto st = gbo_check_motion(c, m1, m2, n, dim, GBO_LAYOUT_AOS, sched, okd, fj, ndv, c->host_stream))
         return st;
+    double *ltd = mlt ? mlt : (double *)(d + off_lt), *lsd = mls ? mls : (double *)(d + off_ls);
     if (last_t || last_state)
     {
-        StatesView v1 = make_view((const double *)d, dim, GBO_LAYOUT_AOS);
-        StatesView v2 = make_view((const double *)(d + bst), dim, GBO_LAYOUT_AOS);
-        launch_last_valid(lcfg(c->host_stream), c->sp, v1, v2, (const int32_t *)(d + off_fj),
-                          (const int32_t *)(d + off_nd), n, (double *)(d + off_lt),
-                          MutStatesView{last_state ? (double *)(d + off_ls) : nullptr, dim, 1});
+        launch_last_valid(lcfg(c->host_stream), c->sp, make_view(m1, dim, GBO_LAYOUT_AOS),
+                          make_view(m2, dim, GBO_LAYOUT_AOS), fj, ndv, n, ltd,
+                          MutStatesView{last_state ? lsd : nullptr, dim, 1});
         CHECK_LAUNCH();
     }
-    CUDA_TRY(cudaMemcpyAsync(ok, d + off_ok, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
-    if (last_t)
-        CUDA_TRY(cudaMemcpyAsync(last_t, d + off_lt, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
-    if (last_state)
-        CUDA_TRY(cudaMemcpyAsync(last_state, d + off_ls, bst, cudaMemcpyDeviceToHost, c->host_stream));
+    if (!mok)
+        CUDA_TRY(cudaMemcpyAsync(ok, okd, (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+    if (last_t && !mlt)
+        CUDA_TRY(cudaMemcpyAsync(last_t, ltd, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->host_stream));
+    if (last_state && !mls)
+        CUDA_TRY(cudaMemcpyAsync(last_state, lsd, bst, cudaMemcpyDeviceToHost, c->host_stream));
     CUDA_TRY(cudaStreamSynchronize(c->host_stream));
     return GBO_OK;
 }

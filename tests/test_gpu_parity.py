@@ -252,6 +252,46 @@ def test_chain_motion_deferred_edges_vs_oracle(chain_case, port):
     assert ck.stats()["rechecked"] >= 200   # the last call's FP64 work: at least the deferred edges
 
 
+def test_motion_host_pinned_and_pageable_vs_oracle(chain_case, port):
+    """The host entry point reads and writes page-locked arrays in place (mapped over the host link)
+    and copies pageable ones; both must equal the oracle for every edge, with and without lastValid,
+    and with mixed pinned / pageable arguments."""
+    import ctypes as C
+    w, sp, ckd, valid = chain_case
+    vs = w.states[valid == 1]
+    rng = np.random.default_rng(17)
+    n = 70_001
+    s1, s2 = vs[rng.integers(0, len(vs), n)], vs[rng.integers(0, len(vs), n)]
+    ref = port.check_motion(sp, ckd, s1, s2, want_state=True, want_bisect=False)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    ck.setPrecision("fp32_guarded")
+    mv = B.DiscreteMotionValidator(ck)
+    ok, lt, ls = mv.checkMotionHost(s1, s2)                      # pageable
+    assert np.array_equal(ok, ref["ok"].astype(bool))
+    assert same_bits(lt, ref["last_t"]) and same_bits(ls, ref["last_state"])
+    ok2, _, _ = mv.checkMotionHost(s1, s2, last_valid=False)
+    assert np.array_equal(ok2, ok)
+    p1, p2 = torch.as_tensor(s1).pin_memory(), torch.as_tensor(s2).pin_memory()
+    for pinned_out in (True, False):
+        okp = torch.zeros(n, dtype=torch.uint8)
+        ltp = torch.zeros(n, dtype=torch.float64)
+        lsp = torch.zeros((n, w.dim), dtype=torch.float64)
+        if pinned_out:
+            okp, ltp, lsp = okp.pin_memory(), ltp.pin_memory(), lsp.pin_memory()
+        vp = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+        capi.check(capi.lib().gbo_check_motion_host(ck._h, vp(p1), vp(p2), n, vp(okp), vp(ltp), vp(lsp)))
+        assert np.array_equal(okp.numpy().astype(bool), ref["ok"].astype(bool)), pinned_out
+        assert same_bits(ltp.numpy(), ref["last_t"]) and same_bits(lsp.numpy(), ref["last_state"]), pinned_out
+    # validity through the host entry point, pinned in place and pageable
+    st = w.states[:50_000]
+    ref_v = valid[:50_000].astype(bool)
+    assert np.array_equal(ck.isValidHost(st), ref_v)
+    pst, pout = torch.as_tensor(st).pin_memory(), torch.zeros(len(st), dtype=torch.uint8).pin_memory()
+    capi.check(capi.lib().gbo_is_valid_host(ck._h, C.c_void_p(pst.data_ptr()), len(st), C.c_void_p(pout.data_ptr())))
+    assert np.array_equal(pout.numpy().astype(bool), ref_v)
+
+
 def test_dh_arm_motion_vs_oracle(port):
     w = W.config2(n_edges=400, n_world=1024)
     sp = SpaceDesc(w.space_kind, 7, w.low, w.high, lvs_fraction=w.lvs_fraction)
