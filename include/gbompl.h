@@ -96,6 +96,13 @@ gbo_status gbo_space_distance(const gbo_space *s, const double *a, const double 
                               double *out, gbo_stream stream);
 gbo_status gbo_space_interpolate(const gbo_space *s, const double *a, const double *b, const double *t, int64_t n,
                                  int64_t ld, int layout, double *out, gbo_stream stream);
+/* SpaceInformation::getMotionStates(s1, s2, states, count, endpoints, alloc = true)
+ * (src/ompl/base/src/SpaceInformation.cpp:215-286) over a batch of edges: edge i yields
+ * m = count + 2 states with endpoints (s1, interpolate(s1, s2, j / (count + 1)) for j = 1..count, s2)
+ * or m = count without, as rows i*m .. i*m + m - 1 of out (n*m rows, out_ld, same layout). */
+gbo_status gbo_get_motion_states(const gbo_space *s, const double *s1, const double *s2, int64_t n, int64_t ld,
+                                 int layout, unsigned count, int endpoints, double *out, int64_t out_ld,
+                                 gbo_stream stream);
 
 /* ---- validity checkers ----
  * world: n_world rows of 3 (circles) or 4 (segments, spheres) doubles, host memory, copied to the device.
@@ -139,6 +146,13 @@ gbo_status gbo_sampler_destroy(gbo_sampler *s);
 gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream);
 gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double distance, int64_t n, int64_t ld,
                                    int layout, double *out, gbo_stream stream);
+/* UniformValidStateSampler::sample (src/ompl/base/samplers/src/UniformValidStateSampler.cpp:46-57)
+ * called n times: call i draws sampleUniform states from s until c reports one valid or `attempts`
+ * were drawn (MAX_VALID_SAMPLE_ATTEMPTS = 100 in OMPL); row i of out = the state it ended on,
+ * ok[i] = 1 when valid. The stream of s advances by exactly the draws the n calls make, as OMPL's
+ * would. Device arrays; returns when done (the host decides how many states each round draws). */
+gbo_status gbo_sample_valid(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out, int64_t ld,
+                            int layout, uint8_t *ok, gbo_stream stream);
 
 /* ---- nearest neighbours ---- (NearestNeighbors<T>; element key = insertion index) */
 gbo_status gbo_nn_create(const gbo_space *space, int64_t capacity, gbo_nn **out);

@@ -125,6 +125,18 @@ class StateSpace:
                                           _stream(stream)))
         return out if isinstance(a, torch.Tensor) else _host(out)
 
+    def getMotionStates(self, s1, s2, count, endpoints=True, stream=None):
+        """SpaceInformation::getMotionStates(s1, s2, states, count, endpoints, alloc=true) for a batch
+        of edges (AoS rows): returns (n, m, dim) with m = count + 2 (endpoints) or count."""
+        t1, n, ld, lay = _batch(s1, self.dim, False)
+        t2, _, _, _ = _batch(s2, self.dim, False)
+        m = count + 2 if endpoints else count
+        out = torch.empty((n * m, self.dim), dtype=torch.float64, device="cuda")
+        check(lib().gbo_get_motion_states(self.handle(), _ptr(t1), _ptr(t2), n, ld, lay, int(count),
+                                          1 if endpoints else 0, _ptr(out), self.dim, _stream(stream)))
+        out = out.reshape(n, m, self.dim)
+        return out if isinstance(s1, torch.Tensor) else _host(out)
+
 
 class RealVectorStateSpace(StateSpace):
     kind = capi.SPACE_REAL_VECTOR
@@ -340,6 +352,16 @@ class StateSampler:
         check(lib().gbo_sample_uniform_near(self._h, _ptr(t), float(distance), n, ld, lay, _ptr(out),
                                             _stream(stream)))
         return out if isinstance(near, torch.Tensor) else _host(out)
+
+
+    def sampleValid(self, checker, n, attempts=100, stream=None, host=True):
+        """UniformValidStateSampler::sample called n times on this sampler's stream: (states, ok)."""
+        dim = self.space.dim
+        out = torch.empty((n, dim), dtype=torch.float64, device="cuda")
+        ok = torch.empty(n, dtype=torch.uint8, device="cuda")
+        check(lib().gbo_sample_valid(self._h, checker._h, n, int(attempts), _ptr(out), dim, capi.LAYOUT_AOS,
+                                     _ptr(ok), _stream(stream)))
+        return (_host(out), _host(ok).astype(bool)) if host else (out, ok)
 
 
 RealVectorStateSampler = StateSampler

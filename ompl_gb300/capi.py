@@ -39,6 +39,7 @@ SIGNATURES = {
     "gbo_space_info": (C.c_int, [_P, _D, _D]),
     "gbo_space_distance": (C.c_int, [_P, _P, _P, _I64, _I64, C.c_int, _P, _P]),
     "gbo_space_interpolate": (C.c_int, [_P, _P, _P, _P, _I64, _I64, C.c_int, _P, _P]),
+    "gbo_get_motion_states": (C.c_int, [_P, _P, _P, _I64, _I64, C.c_int, C.c_uint, C.c_int, _P, _I64, _P]),
     "gbo_checker_create": (C.c_int, [_P, C.c_int, _D, _I64, _D, C.c_int, C.c_int, C.c_double, C.POINTER(_P)]),
     "gbo_checker_destroy": (C.c_int, [_P]),
     "gbo_checker_set_precision": (C.c_int, [_P, C.c_int]),
@@ -53,6 +54,7 @@ SIGNATURES = {
     "gbo_sampler_destroy": (C.c_int, [_P]),
     "gbo_sample_uniform": (C.c_int, [_P, _I64, _P, _I64, C.c_int, _P]),
     "gbo_sample_uniform_near": (C.c_int, [_P, _P, C.c_double, _I64, _I64, C.c_int, _P, _P]),
+    "gbo_sample_valid": (C.c_int, [_P, _P, _I64, C.c_uint, _P, _I64, C.c_int, _P, _P]),
     "gbo_nn_create": (C.c_int, [_P, _I64, C.POINTER(_P)]),
     "gbo_nn_destroy": (C.c_int, [_P]),
     "gbo_nn_set_precision": (C.c_int, [_P, C.c_int]),

@@ -686,6 +686,25 @@ gbo_status gbo_space_interpolate(const gbo_space *s, const double *a, const doub
     return GBO_OK;
 }
 
+gbo_status gbo_get_motion_states(const gbo_space *s, const double *s1, const double *s2, int64_t n, int64_t ld,
+                                 int layout, unsigned count, int endpoints, double *out, int64_t out_ld,
+                                 gbo_stream stream)
+{
+    const int64_t m = endpoints ? (int64_t)count + 2 : (int64_t)count;
+    if (!s || n < 0 || (n > 0 && (!s1 || !s2 || (m > 0 && !out))) || !valid_layout(layout, n, ld, s->sp.dim) ||
+        !valid_layout(layout, n * m, out_ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad getMotionStates arguments");
+    if (n == 0 || m == 0)
+        return GBO_OK;
+    if (auto st = ensure_device())
+        return st;
+    StatesView ov = make_view(out, out_ld, layout);
+    launch_motion_states(lcfg(stream), s->sp, make_view(s1, ld, layout), make_view(s2, ld, layout), n, count,
+                         endpoints ? 1 : 0, MutStatesView{out, ov.si, ov.sd});
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
 // ---------------------------------------------------------------- checkers
 gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *world, int64_t n_world,
                               const double *dh, int n_joints, int spheres_per_link, double sphere_radius,
@@ -1205,6 +1224,94 @@ gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double di
     launch_sample_uniform(lcfg(stream), s->st, s->sp, near, make_view(near, ld, layout), distance, n,
                           MutStatesView{out, ov.si, ov.sd});
     CHECK_LAUNCH();
+    return GBO_OK;
+}
+
+// UniformValidStateSampler::sample, n calls. A call draws until a valid state or `attempts` draws;
+// the stream must end where OMPL's would, so no draw is made that no call consumes. Each round draws
+// one state per unresolved call (every such call consumes at least one more), checks them, and walks
+// the flags on the host; after 8 rounds the rest is drawn speculatively up to its upper bound
+// (attempts per call) from a saved copy of the generator, which is then restored and advanced by
+// exactly the draws consumed.
+gbo_status gbo_sample_valid(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out, int64_t ld,
+                            int layout, uint8_t *ok, gbo_stream stream)
+{
+    if (!s || !c || n < 0 || (n > 0 && (!out || !ok)) || !valid_layout(layout, n, ld, s->sp.dim) ||
+        c->sp.dim != s->sp.dim)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleValid arguments");
+    if (n == 0)
+        return GBO_OK;
+    const int64_t A = attempts > 0 ? attempts : 1;  // do { ... } while: one draw at least
+    const int dim = s->sp.dim;
+    cudaStream_t st = (cudaStream_t)stream;
+    const StatesView ov = make_view(out, ld, layout);
+    const LaunchCfg lc = lcfg(st);
+    std::vector<uint8_t> flags, okh;
+    std::vector<int64_t> src;
+    int64_t done = 0, open = 0;  // calls resolved; draws of the unresolved call so far
+    constexpr int64_t kSpeculativeCap = 1ll << 26;
+    for (int round = 0; done < n; ++round)
+    {
+        const int64_t r = n - done;
+        const bool spec = round >= 8 && r * A - open <= kSpeculativeCap;
+        const int64_t gen = spec ? r * A - open : r;
+        double *buf = nullptr;
+        uint8_t *fl = nullptr;
+        int64_t *idx = nullptr;
+        SamplerState *ckpt = nullptr;
+        CUDA_TRY(cudaMallocAsync((void **)&buf, (size_t)gen * dim * sizeof(double), st));
+        CUDA_TRY(cudaMallocAsync((void **)&fl, (size_t)gen, st));
+        CUDA_TRY(cudaMallocAsync((void **)&idx, (size_t)r * sizeof(int64_t), st));
+        if (spec)
+        {
+            CUDA_TRY(cudaMallocAsync((void **)&ckpt, sizeof(SamplerState), st));
+            CUDA_TRY(cudaMemcpyAsync(ckpt, s->st, sizeof(SamplerState), cudaMemcpyDeviceToDevice, st));
+        }
+        if (auto e = gbo_sample_uniform(s, gen, buf, dim, GBO_LAYOUT_AOS, stream))
+            return e;
+        if (auto e = gbo_is_valid(c, buf, gen, dim, GBO_LAYOUT_AOS, fl, stream))
+            return e;
+        flags.resize((size_t)gen);
+        CUDA_TRY(cudaMemcpyAsync(flags.data(), fl, (size_t)gen, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        src.clear();
+        okh.clear();
+        int64_t q = 0;
+        while (done + (int64_t)src.size() < n && q < gen)
+        {
+            ++open;
+            if (flags[(size_t)q] || open == A)
+            {
+                src.push_back(q);
+                okh.push_back(flags[(size_t)q] ? 1 : 0);
+                open = 0;
+            }
+            ++q;
+        }
+        if (spec)
+        {
+            // back to the saved generator, advanced by exactly the q draws consumed (same values)
+            CUDA_TRY(cudaMemcpyAsync(s->st, ckpt, sizeof(SamplerState), cudaMemcpyDeviceToDevice, st));
+            if (auto e = gbo_sample_uniform(s, q, buf, dim, GBO_LAYOUT_AOS, stream))
+                return e;
+        }
+        const int64_t m = (int64_t)src.size();
+        if (m)
+        {
+            CUDA_TRY(cudaMemcpyAsync(idx, src.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaMemcpyAsync(ok + done, okh.data(), (size_t)m, cudaMemcpyHostToDevice, st));
+            launch_gather_rows(lc, StatesView{buf, dim, 1}, idx, m, dim,
+                               MutStatesView{out + done * ov.si, ov.si, ov.sd});
+            CHECK_LAUNCH();
+        }
+        cudaFreeAsync(buf, st);
+        cudaFreeAsync(fl, st);
+        cudaFreeAsync(idx, st);
+        if (ckpt)
+            cudaFreeAsync(ckpt, st);
+        CUDA_TRY(cudaStreamSynchronize(st));  // src / okh are reused by the next round
+        done += m;
+    }
     return GBO_OK;
 }
 

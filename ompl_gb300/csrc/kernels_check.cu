@@ -11,6 +11,8 @@
 //
 // The checked states and the reported first invalid index follow DiscreteMotionValidator.cpp:48-91:
 // states j/nd for j = 1..nd-1 in order, then s2 itself (index nd); nd = validSegmentCount(s1, s2).
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "tma.cuh"
 
@@ -473,6 +475,48 @@ __global__ void interpolate_kernel(SpaceParams sp, StatesView va, StatesView vb,
         out(i, d) = q[d];
 }
 
+// SpaceInformation::getMotionStates(s1, s2, states, count, endpoints, alloc = true)
+// (SpaceInformation.cpp:215-286) for a batch of edges: edge e yields m rows e*m .. e*m + m - 1:
+// [s1,] interpolate(s1, s2, j / (count + 1)) for j = 1..count[, s2]. Thread per output row.
+template <int MAXD>
+__global__ void motion_states_kernel(SpaceParams sp, StatesView v1, StatesView v2, int64_t n, unsigned count,
+                                     int endpoints, MutStatesView out)
+{
+    const int64_t m = endpoints ? (int64_t)count + 2 : (int64_t)count;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n * m; r += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t e = r / m, k = r - e * m;
+        double a[MAXD], b[MAXD], q[MAXD];
+        load_state<MAXD>(v1, e, sp.dim, a);
+        load_state<MAXD>(v2, e, sp.dim, b);
+        if (endpoints && k == 0)
+            for (int d = 0; d < sp.dim; ++d)
+                out(r, d) = a[d];
+        else if (endpoints && k == m - 1)
+            for (int d = 0; d < sp.dim; ++d)
+                out(r, d) = b[d];
+        else
+        {
+            const unsigned j = (unsigned)(endpoints ? k : k + 1);
+            interpolate64<MAXD>(sp, a, b, ddiv((double)j, (double)(count + 1u)), q);
+            for (int d = 0; d < sp.dim; ++d)
+                out(r, d) = q[d];
+        }
+    }
+}
+
+// Row gather: out row i = src row idx[i] (UniformValidStateSampler results).
+template <int MAXD>
+__global__ void gather_rows_kernel(StatesView src, const int64_t *idx, int64_t n, int dim, MutStatesView out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t j = idx[i];
+        for (int d = 0; d < dim; ++d)
+            out(i, d) = src(j, d);
+    }
+}
+
 // SpaceInformation::checkMotion(states, count, firstInvalid) (SpaceInformation.cpp:288-299): first
 // invalid index of an ordered chain, by a grid-stride scan with an atomicMin.
 template <int CK, int MAXD>
@@ -651,6 +695,27 @@ void launch_distance(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, S
     if (grid == 0)
         return;
     distance_kernel<GBO_MAXD><<<grid, 256, 0, lc.stream>>>(sp, a, b, n, out);
+    note_launch();
+}
+
+void launch_motion_states(const LaunchCfg &lc, const SpaceParams &sp, StatesView v1, StatesView v2, int64_t n,
+                          unsigned count, int endpoints, MutStatesView out)
+{
+    const int64_t rows = n * (endpoints ? (int64_t)count + 2 : (int64_t)count);
+    const int64_t grid = std::min<int64_t>((rows + 255) / 256, (int64_t)lc.sm_count * 16);
+    if (grid == 0)
+        return;
+    motion_states_kernel<GBO_MAXD><<<(int)grid, 256, 0, lc.stream>>>(sp, v1, v2, n, count, endpoints, out);
+    note_launch();
+}
+
+void launch_gather_rows(const LaunchCfg &lc, StatesView src, const int64_t *idx, int64_t n, int dim,
+                        MutStatesView out)
+{
+    const int64_t grid = std::min<int64_t>((n + 255) / 256, (int64_t)lc.sm_count * 16);
+    if (grid == 0)
+        return;
+    gather_rows_kernel<GBO_MAXD><<<(int)grid, 256, 0, lc.stream>>>(src, idx, n, dim, out);
     note_launch();
 }
 

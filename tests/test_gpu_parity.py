@@ -180,6 +180,65 @@ def test_motion_states_vs_ompl(golden):
             assert fi == g["first_invalid"][i]
 
 
+def test_get_motion_states_vs_ompl(golden):
+    """SpaceInformation::getMotionStates (alloc = true) per fixture edge, bitwise against OMPL; and the
+    same edges batched per (count, endpoints)."""
+    g = golden("motion_states")
+    s = gpu_space(g)
+    off = 0
+    groups = {}
+    for i in range(len(g["count"])):
+        n = int(g["lengths"][i])
+        want = g["states"][off:off + n]
+        off += n
+        cnt, ep = int(g["count"][i]), bool(g["endpoints"][i])
+        got = s.getMotionStates(g["a"][i:i + 1], g["b"][i:i + 1], cnt, endpoints=ep)[0]
+        assert same_bits(got, want), i
+        groups.setdefault((cnt, ep), []).append((i, want))
+    for (cnt, ep), items in groups.items():
+        rows = [i for i, _ in items]
+        got = s.getMotionStates(g["a"][rows], g["b"][rows], cnt, endpoints=ep)
+        for j, (_, want) in enumerate(items):
+            assert same_bits(got[j], want)
+
+
+def _valid_sampler_walk(flags, n, attempts):
+    """UniformValidStateSampler::sample n times over a stream with validity flags: (index, ok) per call
+    and the number of draws consumed."""
+    A = max(attempts, 1)
+    out, q = [], 0
+    for _ in range(n):
+        for a in range(A):
+            if flags[q] or a == A - 1:
+                out.append((q, bool(flags[q])))
+                q += 1
+                break
+            q += 1
+    return out, q
+
+
+@pytest.mark.parametrize("name,attempts", [("circles_seeded", 100), ("chain_seeded", 100), ("chain_seeded", 3)])
+def test_sample_valid_vs_oracle(golden, port, name, attempts):
+    g = golden(name)
+    sd, ckd = space_of(g), checker_of(g)
+    s = gpu_space(g)
+    ck = gpu_checker(s, ckd)
+    seed, n = 1234, 3000
+    stream = port.sample_uniform(sd, seed, n * max(attempts, 1) + 64)
+    flags = port.is_valid(sd, ckd, stream).astype(bool)
+    calls, used = _valid_sampler_walk(flags, n, attempts)
+    sampler = B.StateSampler(s, seed)
+    for prec in ("fp32_guarded",):
+        ck.setPrecision(prec)
+        st, ok = sampler.sampleValid(ck, n, attempts=attempts)
+        idx = np.array([i for i, _ in calls])
+        assert np.array_equal(ok, np.array([v for _, v in calls]))
+        assert same_bits(st, stream[idx])
+        # the stream continues exactly where OMPL's would
+        nxt = sampler.sampleUniform(5)
+        assert same_bits(nxt, stream[used:used + 5])
+
+
 # ------------------------------------------------------------------ larger seeded cases vs the oracle
 @pytest.fixture(scope="module")
 def chain_case(port):
