@@ -196,6 +196,8 @@ gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t 
 /* Host-memory sampling (AoS rows; synchronous). */
 gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out);
 gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out);
+gbo_status gbo_sample_valid_host(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out,
+                                 uint8_t *ok);
 
 /* ---- serving ----
  * A request loop for many concurrent planner instances: clients submit validity, motion and nearestK

@@ -18,6 +18,7 @@
 #include <ompl/base/SpaceInformation.h>
 #include <ompl/base/StateSampler.h>
 #include <ompl/base/StateValidityChecker.h>
+#include <ompl/base/ValidStateSampler.h>
 #include <ompl/datastructures/NearestNeighbors.h>
 #include <ompl/util/Exception.h>
 
@@ -248,6 +249,50 @@ public:
         throwIf(gbo_sample_uniform_host(s_, (int64_t)states.size(), rows.data()), "sampleUniform");
         for (size_t i = 0; i < states.size(); ++i)
             ctx_->fromRow(rows.data() + i * d, states[i]);
+    }
+
+private:
+    GpuContextPtr ctx_;
+    gbo_sampler *s_ = nullptr;
+};
+
+/* UniformValidStateSampler (base/samplers/UniformValidStateSampler.h) on the GPU: sampleUniform draws
+ * from the GPU stream of RNG::setLocalSeed(localSeed) until the context's checker reports a valid
+ * state or getNrAttempts() draws were made; the stream is consumed exactly as OMPL's sampler would
+ * consume it. sampleBatch makes n such calls in one go. */
+class GpuUniformValidStateSampler : public ompl::base::ValidStateSampler
+{
+public:
+    GpuUniformValidStateSampler(const ompl::base::SpaceInformation *si, GpuContextPtr ctx, uint32_t localSeed)
+      : ompl::base::ValidStateSampler(si), ctx_(std::move(ctx))
+    {
+        name_ = "uniform";
+        throwIf(gbo_sampler_create(ctx_->space(), localSeed, &s_), "sampler");
+    }
+    ~GpuUniformValidStateSampler() override { gbo_sampler_destroy(s_); }
+    bool sample(ompl::base::State *state) override
+    {
+        std::vector<double> row(ctx_->dim());
+        uint8_t ok = 0;
+        throwIf(gbo_sample_valid_host(s_, ctx_->checker(), 1, attempts_, row.data(), &ok), "sample");
+        ctx_->fromRow(row.data(), state);
+        return ok != 0;
+    }
+    bool sampleNear(ompl::base::State *, const ompl::base::State *, double) override
+    {
+        throw ompl::Exception("gbompl: sampleNear is not provided by the GPU valid-state sampler");
+    }
+    /* states.size() consecutive sample() calls; ok[i] is call i's result. */
+    void sampleBatch(std::vector<ompl::base::State *> &states, std::vector<bool> &ok)
+    {
+        const unsigned d = ctx_->dim();
+        std::vector<double> rows(states.size() * d);
+        std::vector<uint8_t> r(states.size());
+        throwIf(gbo_sample_valid_host(s_, ctx_->checker(), (int64_t)states.size(), attempts_, rows.data(), r.data()),
+                "sample");
+        for (size_t i = 0; i < states.size(); ++i)
+            ctx_->fromRow(rows.data() + i * d, states[i]);
+        ok.assign(r.begin(), r.end());
     }
 
 private:

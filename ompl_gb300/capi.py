@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbo_sample_uniform": (C.c_int, [_P, _I64, _P, _I64, C.c_int, _P]),
     "gbo_sample_uniform_near": (C.c_int, [_P, _P, C.c_double, _I64, _I64, C.c_int, _P, _P]),
     "gbo_sample_valid": (C.c_int, [_P, _P, _I64, C.c_uint, _P, _I64, C.c_int, _P, _P]),
+    "gbo_sample_valid_host": (C.c_int, [_P, _P, _I64, C.c_uint, _P, _P]),
     "gbo_nn_create": (C.c_int, [_P, _I64, C.POINTER(_P)]),
     "gbo_nn_destroy": (C.c_int, [_P]),
     "gbo_nn_set_precision": (C.c_int, [_P, C.c_int]),

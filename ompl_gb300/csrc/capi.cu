@@ -1627,6 +1627,27 @@ gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out)
     return GBO_OK;
 }
 
+gbo_status gbo_sample_valid_host(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out,
+                                 uint8_t *ok)
+{
+    if (!s || !c || n < 0 || (n > 0 && (!out || !ok)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleValid arguments");
+    if (n == 0)
+        return GBO_OK;
+    std::lock_guard<std::mutex> lk(s->mu);
+    const size_t b = (size_t)n * s->sp.dim * sizeof(double);
+    if (auto st = s->dev.reserve(b + (size_t)n + 16, s->host_stream))
+        return st;
+    double *d = (double *)s->dev.p;
+    uint8_t *dok = (uint8_t *)s->dev.p + b;
+    if (auto st = gbo_sample_valid(s, c, n, attempts, d, s->sp.dim, GBO_LAYOUT_AOS, dok, s->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(out, d, b, cudaMemcpyDeviceToHost, s->host_stream));
+    CUDA_TRY(cudaMemcpyAsync(ok, dok, (size_t)n, cudaMemcpyDeviceToHost, s->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(s->host_stream));
+    return GBO_OK;
+}
+
 gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out)
 {
     if (!s || n < 0 || (n > 0 && (!out || !near)))

@@ -3,6 +3,7 @@
 // SpaceInformation. Without a GPU it checks that construction fails with ompl::Exception.
 #include <ompl/base/DiscreteMotionValidator.h>
 #include <ompl/base/SpaceInformation.h>
+#include <ompl/base/samplers/UniformValidStateSampler.h>
 #include <ompl/base/spaces/RealVectorStateSpace.h>
 #include <ompl/datastructures/NearestNeighborsLinear.h>
 
@@ -28,6 +29,15 @@ struct Circles : ob::StateValidityChecker
         return true;
     }
     std::vector<double> c_;
+};
+
+// OMPL's own sampler with its stream seeded like RNG::setLocalSeed(seed)
+struct SeededSampler : ob::RealVectorStateSampler
+{
+    SeededSampler(const ob::StateSpace *s, std::uint_fast32_t seed) : ob::RealVectorStateSampler(s)
+    {
+        rng_.setLocalSeed(seed);
+    }
 };
 
 int main()
@@ -100,6 +110,25 @@ int main()
         mism += n1 != n2;
     }
     mism += gnn.size() != lnn.size();
+    // UniformValidStateSampler: same seed, same calls, same results (a few with 2 attempts)
+    space->setStateSamplerAllocator([](const ob::StateSpace *s) { return std::make_shared<SeededSampler>(s, 77); });
+    ob::UniformValidStateSampler rvs(si.get());
+    gbompl::GpuUniformValidStateSampler gvs(si.get(), ctx, 77);
+    for (int i = 0; i < 300; ++i)
+    {
+        const unsigned att = i % 50 < 10 ? 2 : 100;
+        rvs.setNrAttempts(att);
+        gvs.setNrAttempts(att);
+        const bool r1 = rvs.sample(a), r2 = gvs.sample(b);
+        mism += r1 != r2 || !space->equalStates(a, b);
+    }
+    std::vector<ob::State *> batch(500);
+    for (auto &p : batch)
+        p = si->allocState();
+    std::vector<bool> bok;
+    gvs.sampleBatch(batch, bok);
+    for (size_t i = 0; i < batch.size(); ++i)
+        mism += rvs.sample(a) != bok[i] || !space->equalStates(a, batch[i]);
     std::printf("%s mismatches=%d valid=%u invalid=%u\n", mism ? "MISMATCH" : "MATCH", mism,
                 gmv.getValidMotionCount(), gmv.getInvalidMotionCount());
     return mism ? 1 : 0;

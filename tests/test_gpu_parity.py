@@ -237,6 +237,13 @@ def test_sample_valid_vs_oracle(golden, port, name, attempts):
         # the stream continues exactly where OMPL's would
         nxt = sampler.sampleUniform(5)
         assert same_bits(nxt, stream[used:used + 5])
+    # host-memory form on a fresh sampler with the same seed
+    import ctypes as C
+    h = B.StateSampler(s, seed)
+    out, okh = np.empty((n, sd.dim)), np.empty(n, dtype=np.uint8)
+    capi.check(capi.lib().gbo_sample_valid_host(h._h, ck._h, n, attempts, out.ctypes.data_as(C.c_void_p),
+                                                okh.ctypes.data_as(C.c_void_p)))
+    assert np.array_equal(okh.astype(bool), ok) and same_bits(out, st)
 
 
 # ------------------------------------------------------------------ larger seeded cases vs the oracle
