@@ -438,6 +438,40 @@ def test_knn_chain_large_vs_oracle(chain_case, port):
     assert idx[:, 0].tolist() == [int(np.flatnonzero((w.states == qq).all(1))[0]) for qq in q]
 
 
+@pytest.mark.parametrize("kind", ["chain10", "wrap7", "rv7"])
+def test_knn_large_batch_vs_exact_scan(kind):
+    """Large batches (4,500 queries over 60,000 elements) through the FP32 scan with FP64 re-check:
+    index sets and FP64 distances must equal the exact FP64 scan's, with and without PRM prefix
+    limits, for fresh and self queries, and after removals."""
+    rng = np.random.default_rng(21)
+    n, dim = 60_000, (10 if kind == "chain10" else 7)
+    if kind == "chain10":
+        space = B.KinematicChainSpace(10, 0.1)
+    elif kind == "wrap7":
+        space = B.WrapL2StateSpace(7)
+    else:
+        space = B.RealVectorStateSpace(7, np.full(7, -math.pi), np.full(7, math.pi))
+    pts = rng.uniform(-math.pi, math.pi, size=(n, dim))
+    queries = np.concatenate([pts[:3000], rng.uniform(-math.pi, math.pi, size=(1500, dim))])
+    nn = B.NearestNeighborsGPU(space, capacity=n)
+    nn.add(pts)
+
+    def both(k, prefix=None):
+        nn.setPrecision("fp32_guarded")
+        i32, d32 = nn.nearestK(queries, k, prefix=prefix)
+        nn.setPrecision("fp64")
+        i64, d64 = nn.nearestK(queries, k, prefix=prefix)
+        assert np.array_equal(i32, i64), (kind, k)
+        assert same_bits(d32, d64), (kind, k)
+
+    for k in (10, 16):
+        both(k)
+    both(10, prefix=np.minimum(np.arange(len(queries)) * 13, n))
+    nn.remove(np.arange(0, n, 7))
+    both(16)
+    assert nn.stats()["queries"] > 0
+
+
 def test_dh_arm_large_world_read_from_global_memory(port):
     """A 16,384-sphere world does not fit the shared-memory staging limit: the FP32 path reads the
     spheres from global memory. Validity and motion must still equal the oracle's."""
