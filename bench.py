@@ -253,6 +253,26 @@ def ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         sched_eps[name] = N_BATCHES * N_EDGES / (a0.elapsed_time(a1) * 1e-3)
 
+    # the same steps replayed from CUDA graphs (one graph per batch, captured after the autotuner ran):
+    # the persistent launch and its counter reset are stream work and capture as they are
+    graphs = []
+    for i in range(N_BATCHES):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            run(i, capi.SCHEDULE_AUTO)
+        graphs.append(g)
+    for g in graphs:
+        g.replay()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for i in range(args.steps):
+        graphs[i % N_BATCHES].replay()
+    g1.record()
+    torch.cuda.synchronize()
+    graph_eps = N_EDGES * args.steps / (g0.elapsed_time(g1) * 1e-3)
+    del graphs
+
     # plain one-launch-per-batch FP64 form on the same batches
     checker.setPrecision("fp64")
     run(0, capi.SCHEDULE_PLAIN)
@@ -343,6 +363,8 @@ def ours(args, rank, world, local_rank):
         "plain_fp64_edges_per_s": plain_eps,
         "batched_vs_plain": value / world / plain_eps,
         "schedule_edges_per_s": sched_eps,
+        "graph_replay_edges_per_s": graph_eps,
+        "recheck_rate": stats["rechecked"] / max(stats["evaluated"], 1),
         "states_per_s": states_per_s,
         "knn_queries_per_s": knn_qps,
         "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},
