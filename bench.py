@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve"],
                    help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
-    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks"],
+    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm"],
                    help="launch one kernel kind twice on the chain workload (for ncu) and exit")
     return p.parse_args()
 
@@ -380,6 +380,22 @@ def profile(kind):
 
     from ompl_gb300 import base as B
     from ompl_gb300 import capi
+    if kind == "arm":
+        # DH arm (4,096 spheres): 64k of the 256k edges, tile schedule, two launches
+        from ompl_gb300 import workloads as W
+        wa = W.config2()
+        space = B.RealVectorStateSpace(7, wa.low, wa.high)
+        space.setLongestValidSegmentFraction(wa.lvs_fraction)
+        checker = B.DHSphereArmValidityChecker(space, wa.dh, wa.obstacles, 8, 0.05)
+        checker.setPrecision("fp32_guarded")
+        mv = B.DiscreteMotionValidator(checker)
+        a = torch.as_tensor(wa.s1[:65536].T.copy(), device="cuda")
+        b = torch.as_tensor(wa.s2[:65536].T.copy(), device="cuda")
+        for _ in range(2):
+            mv.checkMotions(a, b, schedule=capi.SCHEDULE_TILE, soa=True)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": kind, "ok": True}))
+        return
     w = workload()
     space = B.KinematicChainSpace(w.dim, w.link_length)
     space.setLongestValidSegmentFraction(w.lvs_fraction)
