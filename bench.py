@@ -381,7 +381,7 @@ def profile(kind):
     from ompl_gb300 import base as B
     from ompl_gb300 import capi
     if kind == "arm":
-        # DH arm (4,096 spheres): 64k of the 256k edges, tile schedule, two launches
+        # DH arm (4,096 spheres): the 256k edges of the arm workload, tile schedule, two launches
         from ompl_gb300 import workloads as W
         wa = W.config2()
         space = B.RealVectorStateSpace(7, wa.low, wa.high)
@@ -389,8 +389,8 @@ def profile(kind):
         checker = B.DHSphereArmValidityChecker(space, wa.dh, wa.obstacles, 8, 0.05)
         checker.setPrecision("fp32_guarded")
         mv = B.DiscreteMotionValidator(checker)
-        a = torch.as_tensor(wa.s1[:65536].T.copy(), device="cuda")
-        b = torch.as_tensor(wa.s2[:65536].T.copy(), device="cuda")
+        a = torch.as_tensor(wa.s1.T.copy(), device="cuda")
+        b = torch.as_tensor(wa.s2.T.copy(), device="cuda")
         for _ in range(2):
             mv.checkMotions(a, b, schedule=capi.SCHEDULE_TILE, soa=True)
         torch.cuda.synchronize()

@@ -819,7 +819,17 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         wa.stage32 = 0;  // the FP32 narrow phase reads the spheres listed in the grid cells (cell_items4)
         // FK error bound in FP32 (spectral-norm propagation): |dR_k| <= k (2 eps_t + 16u),
         // |dp| <= sum_k (|dR_k| |pA| + |pA| (eps_t + u) + 4u (|p| + |pA|)); centres add 3u|p|.
-        const double u = kU32, eps_t = u * kPiH * 1.01 + 2.0 * std::ldexp(1.0, -23);
+        // angles: |q| <= qmax (the space's bounds; states beyond them are re-checked in FP64), rounded to
+        // FP32 (u |q|, +1% for the float-float interpolation), sincosf within 2 ulp
+        double qmax = kPiH;
+        if (sp.kind == GBO_SPACE_REAL_VECTOR)
+        {
+            qmax = 0.0;
+            for (int d = 0; d < sp.dim; ++d)
+                qmax = std::max(qmax, std::max(std::fabs(sp.low[d]), std::fabs(sp.high[d])));
+        }
+        wa.dh_qmax = (float)qmax;
+        const double u = kU32, eps_t = u * qmax * 1.01 + 2.0 * std::ldexp(1.0, -23);
         double dR = 0.0, dp = 0.0, reach = 0.0;
         for (int i = 0; i < n_joints; ++i)
         {

@@ -49,6 +49,7 @@ struct WorldArgs
     float glo[3], ginv[3];
     double glo64[3], ginv64[3];
     float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere test near contact
+    float dh_qmax;  // largest |joint angle| the FP32 guard covers (larger: FP64)
     const unsigned *test_order;  // kinematic chain: segment-test order (likely intersections first)
 };
 
@@ -154,10 +155,85 @@ __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, c
     return true;
 }
 
+// FP64 form of one state, warp-cooperative (warp-uniform call; q and pos in shared memory, q holding the
+// state): every lane runs the forward kinematics above (identical values, so one warp instruction per
+// step), lane 0 records the joint positions in pos[0..joints], and the spheres are spread over the
+// lanes, each centre and each pair test in the operation order of dh_valid64. Same boolean as
+// dh_valid64 on the same state. Out of line: the callers' FP32 loops keep their registers.
+static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const double *q, const double *w,
+                                                    const WorldArgs &wa, double (*pos)[3], int lane)
+{
+    double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double p[3] = {0, 0, 0};
+    const int G = wa.grid_n;
+    if (lane == 0)
+        pos[0][0] = pos[0][1] = pos[0][2] = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < arm.joints; ++i)
+    {
+        double cq, sq;
+        sincos(q[i], &sq, &cq);
+        const double ca = (double)arm.ca[i], sa = (double)arm.sa[i];
+        const double A[3][3] = {{cq, dmul(-sq, ca), dmul(sq, sa)}, {sq, dmul(cq, ca), dmul(-cq, sa)}, {0.0, sa, ca}};
+        const double pA[3] = {dmul(arm.a[i], cq), dmul(arm.a[i], sq), arm.d[i]};
+        double Rn[3][3], pn[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                Rn[r][k] = dadd(dadd(dmul(R[r][0], A[0][k]), dmul(R[r][1], A[1][k])), dmul(R[r][2], A[2][k]));
+            pn[r] = dadd(dadd(dadd(dmul(R[r][0], pA[0]), dmul(R[r][1], pA[1])), dmul(R[r][2], pA[2])), p[r]);
+        }
+        if (lane == 0)
+            for (int r = 0; r < 3; ++r)
+                pos[i + 1][r] = pn[r];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+            p[r] = pn[r];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                R[r][k] = Rn[r][k];
+        }
+    }
+    __syncwarp();
+    bool hit = false;
+    for (int s = lane; s < arm.joints * arm.spl && !hit; s += 32)
+    {
+        const int i = s / arm.spl, k = s - i * arm.spl;
+        const double f = ddiv(dadd((double)k, 0.5), (double)arm.spl);
+        double c[3];
+        int cell[3];
+        bool inside = true;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+        {
+            c[r] = dadd(pos[i][r], dmul(f, dsub(pos[i + 1][r], pos[i][r])));
+            const double g = floor((c[r] - wa.glo64[r]) * wa.ginv64[r]);
+            inside &= (g >= 0.0 && g < (double)G);
+            cell[r] = (int)g;
+        }
+        if (!inside)
+            continue;
+        const int cid = (cell[0] * G + cell[1]) * G + cell[2];
+        const int b = wa.cell_start[cid], e = wa.cell_start[cid + 1];
+        for (int it = b; it < e && !hit; ++it)
+        {
+            const double *o = w + 4 * wa.cell_items[it];
+            const double dx = dsub(c[0], o[0]), dy = dsub(c[1], o[1]), dz = dsub(c[2], o[2]);
+            const double rr = dadd(arm.rs, o[3]);
+            hit = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < dmul(rr, rr);
+        }
+    }
+    return __any_sync(0xffffffffu, hit);
+}
+
 // FP32 form: FK, centres and the narrow phase in FP32; a pair whose d^2 - (rs+ro)^2 lies within
-// +-dh_e is ambiguous (dh_e bounds the FP32 error of that difference near contact).
+// +-dh_e is ambiguous (dh_e bounds the FP32 error of that difference near contact). q: the joint
+// angles as FP32 values within u|q| (+1e-12) of the reference's FP64 angles.
 template <int MAXD>
-__device__ int dh_valid32(const DHArm &arm, const double *q, const float4 *sph, const WorldArgs &wa)
+__device__ int dh_valid32(const DHArm &arm, const float *q, const float4 *sph, const WorldArgs &wa)
 {
     float R[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
     float p[3] = {0.f, 0.f, 0.f};
@@ -168,8 +244,10 @@ __device__ int dh_valid32(const DHArm &arm, const double *q, const float4 *sph, 
 #pragma unroll 1
     for (int i = 0; i < arm.joints; ++i)
     {
+        if (!(fabsf(q[i]) <= wa.dh_qmax))
+            return kAmbiguous;  // outside the angle range the error bound was derived for
         float cq, sq;
-        sincosf((float)q[i], &sq, &cq);
+        sincosf(q[i], &sq, &cq);
         const float ca = arm.ca[i], sa = arm.sa[i];
         const float A[3][3] = {{cq, -sq * ca, sq * sa}, {sq, cq * ca, -cq * sa}, {0.f, sa, ca}};
         const float pA[3] = {arm.af[i] * cq, arm.af[i] * sq, arm.dfl[i]};

@@ -19,6 +19,59 @@
 namespace gbo
 {
 
+// Checked state j of an edge in a RealVectorStateSpace (interpolate, RealVectorStateSpace.cpp:257-265)
+// as FP32 values, computed in float-float with no FP64 instruction: within ~1e-13 of the reference's
+// FP64 state before the final rounding, i.e. within u|q| + 1e-13 of it, which the FP32 guard bounds
+// cover. j == top is s2 itself.
+template <int MAXD>
+__device__ __forceinline__ void state_at_rv32(const double *a, const double *b, int dim, int j, int nd, int top,
+                                              float *q)
+{
+    if (j == top)
+    {
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d)
+            if (d < dim)
+            {
+                const ff v = split_double(b[d]);
+                q[d] = v.hi + v.lo;
+            }
+        return;
+    }
+    const float ndf = float_of(nd);
+    const float inv_hi = __frcp_rn(ndf);
+    const float inv_lo = fmaf(-inv_hi, ndf, 1.0f) * inv_hi;
+    const float jf = float_of(j);
+    const float t_hi = jf * inv_hi;
+    const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
+#pragma unroll
+    for (int d = 0; d < MAXD; ++d)
+        if (d < dim)
+        {
+            const ff A = split_double(a[d]), Bv = split_double(b[d]);
+            ff D = two_sum(Bv.hi, -A.hi);
+            D = fast_two_sum(D.hi, D.lo + (Bv.lo - A.lo));
+            const float p_hi = D.hi * t_hi;
+            const float p_lo = fmaf(D.hi, t_hi, -p_hi) + fmaf(D.hi, t_lo, D.lo * t_hi);
+            const ff r = ff_add(A, ff{p_hi, p_lo});
+            q[d] = r.hi + r.lo;
+        }
+}
+
+template <int MAXD>
+__device__ __forceinline__ void state_at(const SpaceParams &sp, const double *a, const double *b, int j, int nd,
+                                         int top, double *q)
+{
+    if (j == top)
+    {
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d)
+            q[d] = b[d];
+    }
+    else
+        interpolate64<MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
+}
+
 template <int CK, int MAXD>
 struct Eval
 {
@@ -47,9 +100,36 @@ struct Eval
         if constexpr (CK == GBO_CHECK_CHAIN_SEGMENTS)
             return chain_valid32<MAXD>(s, q, w32, nw, g);
         else if constexpr (CK == GBO_CHECK_DH_SPHERES)
-            return dh_valid32<MAXD>(*arm, q, sph32, *wa);
+        {
+            float qf[MAXD];
+#pragma unroll
+            for (int d = 0; d < MAXD; ++d)
+                qf[d] = d < s.dim ? split_double(q[d]).hi + split_double(q[d]).lo : 0.f;
+            return dh_valid32<MAXD>(*arm, qf, sph32, *wa);
+        }
         else
             return valid64(s, q) ? kValid : kInvalid;
+    }
+    // Verdict on checked state j of the edge (a, b) (j == top is b). The DH arm in a RealVectorStateSpace
+    // evaluates the FP32 form on float-float interpolated angles and may return kAmbiguous: the caller
+    // resolves those lanes warp-cooperatively (dh_resolve_warp). The other forms return kValid or
+    // kInvalid, re-checked per lane.
+    template <int PREC>
+    __device__ int eval_at(const SpaceParams &s, const double *a, const double *b, int j, int nd, int top,
+                           unsigned &rechecks) const
+    {
+        if constexpr (PREC == GBO_PRECISION_FP32_GUARDED && CK == GBO_CHECK_DH_SPHERES)
+        {
+            if (s.kind == GBO_SPACE_REAL_VECTOR)
+            {
+                float qf[MAXD];
+                state_at_rv32<MAXD>(a, b, s.dim, j, nd, top, qf);
+                return dh_valid32<MAXD>(*arm, qf, sph32, *wa);
+            }
+        }
+        double q[MAXD];
+        state_at<MAXD>(s, a, b, j, nd, top, q);
+        return valid<PREC>(s, q, rechecks) ? kValid : kInvalid;
     }
     template <int PREC>
     __device__ bool valid(const SpaceParams &s, const double *q, unsigned &rechecks) const
@@ -198,18 +278,30 @@ __device__ int segment_count(const SpaceParams &sp, const WorldArgs &wa, const d
     return segment_count_from_distance(sp, distance64<MAXD>(sp, a, b));
 }
 
-template <int MAXD>
-__device__ __forceinline__ void state_at(const SpaceParams &sp, const double *a, const double *b, int j, int nd,
-                                         int top, double *q)
+// Resolve the lanes whose verdict r is kAmbiguous with the warp-cooperative FP64 test, one state at a
+// time (warp-uniform call): the lane writes its FP64 state to the warp's buffer wq (state_of), then the
+// whole warp evaluates it.
+template <int CK, int MAXD, class StateFn>
+__device__ __forceinline__ int resolve_warp(const Eval<CK, MAXD> &ev, int r, int lane, double *wq, double (*wpos)[3],
+                                            StateFn state_of, unsigned &rechecks)
 {
-    if (j == top)
+    unsigned A = __ballot_sync(0xffffffffu, r == kAmbiguous);
+    while (A)
     {
-#pragma unroll
-        for (int d = 0; d < MAXD; ++d)
-            q[d] = b[d];
+        const int src = __ffs(A) - 1;
+        A &= A - 1;
+        if (lane == src)
+            state_of(wq);
+        __syncwarp();
+        const bool hit = dh_valid64_warp(*ev.arm, wq, ev.w64, *ev.wa, wpos, lane);
+        if (lane == src)
+        {
+            r = hit ? kInvalid : kValid;
+            ++rechecks;
+        }
+        __syncwarp();
     }
-    else
-        interpolate64<MAXD>(sp, a, b, ddiv((double)j, (double)nd), q);
+    return r;
 }
 
 template <int CK, int MAXD>
@@ -266,7 +358,7 @@ __global__ void __launch_bounds__(256) motion_plain_kernel(SpaceParams sp, World
 }
 
 template <int CK, int MAXD, int PREC>
-__global__ void __launch_bounds__(256) motion_tile_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
+__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 3 : 1) motion_tile_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
                                                           int64_t n, uint8_t *ok, int32_t *first_j, int32_t *nd_out,
                                                           RunCounters *ctr)
 {
@@ -308,16 +400,30 @@ __global__ void __launch_bounds__(256) motion_tile_kernel(SpaceParams sp, WorldA
             const int o_top = __shfl_sync(0xffffffffu, top, owner);
             const int o_nd = __shfl_sync(0xffffffffu, nd, owner);
             const int j = o_next + rep;
-            bool bad = false;
+            int verdict = kValid;
             if (j <= o_top)
             {
-                double a[MAXD], b[MAXD], q[MAXD];
+                double a[MAXD], b[MAXD];
                 load_state<MAXD>(v1, e0 + owner, sp.dim, a);
                 load_state<MAXD>(v2, e0 + owner, sp.dim, b);
-                state_at<MAXD>(sp, a, b, j, o_nd, o_top, q);
-                bad = !ev.template valid<PREC>(sp, q, rechecks);
+                verdict = ev.template eval_at<PREC>(sp, a, b, j, o_nd, o_top, rechecks);
                 ++evaluated;
             }
+            if constexpr (CK == GBO_CHECK_DH_SPHERES && PREC == GBO_PRECISION_FP32_GUARDED)
+            {
+                __shared__ double dh_q[8][GBO_MAXD];
+                __shared__ double dh_pos[8][9][3];
+                const int w = threadIdx.x >> 5;
+                verdict = resolve_warp(ev, verdict, lane, dh_q[w], dh_pos[w],
+                                       [&](double *q) {
+                                           double a[MAXD], b[MAXD];
+                                           load_state<MAXD>(v1, e0 + owner, sp.dim, a);
+                                           load_state<MAXD>(v2, e0 + owner, sp.dim, b);
+                                           state_at<MAXD>(sp, a, b, j, o_nd, o_top, q);
+                                       },
+                                       rechecks);
+            }
+            const bool bad = verdict == kInvalid;
             const unsigned B = __ballot_sync(0xffffffffu, bad);
             if (live)
             {
@@ -356,7 +462,7 @@ __global__ void __launch_bounds__(256) motion_tile_kernel(SpaceParams sp, WorldA
 }
 
 template <int CK, int MAXD, int PREC>
-__global__ void __launch_bounds__(256) motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
+__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 3 : 1) motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
                                                           int64_t n, uint8_t *ok, int32_t *first_j, int32_t *nd_out,
                                                           RunCounters *ctr)
 {
@@ -375,11 +481,14 @@ __global__ void __launch_bounds__(256) motion_warp_kernel(SpaceParams sp, WorldA
         const int64_t e = (int64_t)__shfl_sync(0xffffffffu, ei, 0);
         if (e >= n)
             break;
-        double a[MAXD], b[MAXD];
-        load_state<MAXD>(v1, e, sp.dim, a);
-        load_state<MAXD>(v2, e, sp.dim, b);
         unsigned rc = 0;
-        const int nd = segment_count<MAXD, PREC>(sp, wa, a, b, rc);
+        int nd;
+        {
+            double a[MAXD], b[MAXD];
+            load_state<MAXD>(v1, e, sp.dim, a);
+            load_state<MAXD>(v2, e, sp.dim, b);
+            nd = segment_count<MAXD, PREC>(sp, wa, a, b, rc);
+        }
         if (lane == 0)
             rechecks += rc;
         const int top = nd > 1 ? nd : 1;
@@ -387,14 +496,32 @@ __global__ void __launch_bounds__(256) motion_warp_kernel(SpaceParams sp, WorldA
         for (int base = 1; base <= top; base += 32)
         {
             const int j = base + lane;
-            bool bad = false;
+            int verdict = kValid;
             if (j <= top)
             {
-                double q[MAXD];
-                state_at<MAXD>(sp, a, b, j, nd, top, q);
-                bad = !ev.template valid<PREC>(sp, q, rechecks);
+                // the endpoints are re-read per state (same edge in every lane: broadcast L1 hits), so
+                // that they do not hold 2 x MAXD doubles of registers across the state loop
+                double a[MAXD], b[MAXD];
+                load_state<MAXD>(v1, e, sp.dim, a);
+                load_state<MAXD>(v2, e, sp.dim, b);
+                verdict = ev.template eval_at<PREC>(sp, a, b, j, nd, top, rechecks);
                 ++evaluated;
             }
+            if constexpr (CK == GBO_CHECK_DH_SPHERES && PREC == GBO_PRECISION_FP32_GUARDED)
+            {
+                __shared__ double dh_q[8][GBO_MAXD];
+                __shared__ double dh_pos[8][9][3];
+                const int w = threadIdx.x >> 5;
+                verdict = resolve_warp(ev, verdict, lane, dh_q[w], dh_pos[w],
+                                       [&](double *q) {
+                                           double a[MAXD], b[MAXD];
+                                           load_state<MAXD>(v1, e, sp.dim, a);
+                                           load_state<MAXD>(v2, e, sp.dim, b);
+                                           state_at<MAXD>(sp, a, b, j, nd, top, q);
+                                       },
+                                       rechecks);
+            }
+            const bool bad = verdict == kInvalid;
             const unsigned m = __ballot_sync(0xffffffffu, bad);
             if (m)
             {
