@@ -165,6 +165,18 @@ def reference_arm(args, rank, world):
     }))
 
 
+def replica_totals(edges_per_step, steps, dev_s, wall_s, world, device):
+    """Whole-job figures of `world` replicas (one per GPU, no exchange: every rank checks its own
+    batches): the job processed world * edges_per_step * steps edges in the slowest rank's time (max
+    over ranks of the device time and of the wall time). Returns (edges/s, device s, wall s)."""
+    import torch
+    t = torch.tensor([dev_s, wall_s], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    dev_s, wall_s = t.tolist()
+    return world * edges_per_step * steps / dev_s, dev_s, wall_s
+
+
 def ours(args, rank, world, local_rank):
     import torch
 
@@ -231,12 +243,7 @@ def ours(args, rank, world, local_rank):
     launches = B.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     stats = checker.stats()  # states evaluated / re-checked in FP64 by the last timed step
-    dev_s = sum(step_ms) * 1e-3
-    t_local = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
-    dev_s, wall = t_local.tolist()
-    value = world * N_EDGES * args.steps / dev_s
+    value, dev_s, wall = replica_totals(N_EDGES, args.steps, sum(step_ms) * 1e-3, wall, world, dev)
     mean_ms = statistics.mean(step_ms)
     mean_checked = statistics.mean(checked[i % N_BATCHES] for i in range(args.steps))
 
