@@ -131,6 +131,14 @@ def cpu_edges_per_s(port, sd, cd, s1, s2, threads):
     return len(s1) / (time.perf_counter() - t)
 
 
+def bench_config():
+    """The workload both arms report (the reference arm times a bounded sample of each step)."""
+    return {"workload": "kinematic_chain10: 10 links x 0.1, 32 segments, 1M states, 100k edges/step between "
+                        "valid states, segment fraction 0.005, FP32 bulk + FP64 re-check, autotuned persistent "
+                        "schedule", "edges_per_step": N_EDGES, "batches_rotated": N_BATCHES,
+            "l2": "inputs larger than L2 (12 x 16 MB batches rotate)", "parallelism": "replicas"}
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -157,8 +165,7 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "edges/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "kinematic_chain10: 1M states, 32 segments, edges between valid states, "
-                               "segment fraction 0.005", "edges_per_step": sample},
+        "config": {**bench_config(), "reference_sample_edges_per_step": sample},
         "cpu_baseline": {"value": v, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} edges per step of each 100k-edge batch, all host threads"},
         "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -353,10 +360,7 @@ def ours(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic (seeded)",
-        "config": {"workload": "kinematic_chain10: 10 links x 0.1, 32 segments, 1M states, 100k edges/step between "
-                               "valid states, segment fraction 0.005, FP32 bulk + FP64 re-check, autotuned "
-                               "persistent schedule", "edges_per_step": N_EDGES, "batches_rotated": N_BATCHES,
-                   "l2": "inputs larger than L2 (12 x 16 MB batches rotate)", "parallelism": "replicas"},
+        "config": bench_config(),
         "e2e": {"value": e2e, "unit": "edges/s", "h2d_bytes_per_step": 2 * N_EDGES * 10 * 8,
                 "d2h_bytes_per_step": N_EDGES * (1 + 8)},
         "gpu_launches": launches,
