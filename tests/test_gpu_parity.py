@@ -285,6 +285,66 @@ def test_chain_motion_valid_endpoints_vs_oracle(chain_case, port):
             assert np.array_equal(r["nd"], ref["nd"])
 
 
+def _chain_points(q, L=0.1):
+    """Joint positions in the reference's operation order (KinematicChain.h:214-228)."""
+    th, x, y, pts = 0.0, 0.0, 0.0, [(0.0, 0.0)]
+    for a in q:
+        th += a
+        x += math.cos(th) * L
+        y += math.sin(th) * L
+        pts.append((x, y))
+    return pts, th
+
+
+def _boundary_world(q):
+    """World segments on the reference test's boundaries for the chain at q: collinear with links 2-4,
+    through joint 7 (2e-6 long), ending on joint 5, parallel to the chain 1e-9 away (plus 1e-12 tilt)."""
+    pts, th = _chain_points(q)
+    (x2, y2), (x5, y5), (x7, y7) = pts[2], pts[5], pts[7]
+    c, s_ = math.cos(th), math.sin(th)
+    return np.array([[x2, y2, x5, y5],
+                     [x7 - 1e-6 * s_, y7 + 1e-6 * c, x7 + 1e-6 * s_, y7 - 1e-6 * c],
+                     [x5, y5, x5 + 0.3 * s_, y5 - 0.3 * c],
+                     [x2 + 1e-12, y2 + 1e-9, x7, y7 + 1e-9 + 1e-12],
+                     [-1.5, 1.4, 1.5, 1.4], [1.4, -1.5, 1.4, 1.5]])  # axis-aligned, clear of the chain
+
+
+def test_chain_boundary_configurations_vs_oracle(port):
+    """States and worlds on the reference test's own boundaries (demos/KinematicChain.h:251-276):
+    world segments collinear with links, through a joint point, ending on a joint, parallel within
+    1e-9, axis-aligned (exact zero cross products); straight and folded chains perturbed by 0 to 1e-5.
+    The FP32 path must send every undecided comparison to FP64 and agree with the oracle exactly."""
+    rng = np.random.default_rng(12)
+    n = 10
+    bases = [np.r_[0.3, np.zeros(n - 1)], np.r_[0.0, np.zeros(n - 1)], np.r_[math.pi / 2, np.zeros(n - 1)],
+             np.r_[-2.0, np.full(n - 1, 0.25)]]
+    sd = SpaceDesc(capi.SPACE_KINEMATIC_CHAIN, n, link_length=0.1, lvs_fraction=0.005)
+    s = gpu_space(sd)
+    n_valid = n_invalid = 0
+    for q in bases:
+        ckd = CheckerDesc(capi.CHECK_CHAIN_SEGMENTS, _boundary_world(q))
+        states = np.concatenate([q + rng.standard_normal((40, n)) * scale
+                                 for scale in (0.0, 1e-15, 1e-12, 1e-9, 1e-7, 1e-5, 1e-3)])
+        ref = port.is_valid(sd, ckd, states).astype(bool)
+        n_valid += int(ref.sum())
+        n_invalid += int((~ref).sum())
+        ck = gpu_checker(s, ckd)
+        for p in ("fp64", "fp32_guarded"):
+            ck.setPrecision(p)
+            assert np.array_equal(ck.isValid(states), ref), p
+        # motions between the boundary states
+        i, j = rng.integers(0, len(states), 300), rng.integers(0, len(states), 300)
+        mref = port.check_motion(sd, ckd, states[i], states[j], want_state=False, want_bisect=False)
+        mv = B.DiscreteMotionValidator(ck)
+        for p in ("fp64", "fp32_guarded"):
+            ck.setPrecision(p)
+            for sch in SCHEDULES:
+                r = mv.checkMotions(states[i], states[j], schedule=sch)
+                assert np.array_equal(r["ok"], mref["ok"]), (p, sch)
+                assert np.array_equal(r["first_j"], mref["first_j"]), (p, sch)
+    assert n_valid > 0 and n_invalid > 0
+
+
 def test_chain_motion_deferred_edges_vs_oracle(chain_case, port):
     """Edges the FP32 warp kernel hands to its FP64 follow-up kernel: a joint difference within 1e-9
     of pi (the interpolation's shortest-arc branch), and zero or tiny length (segment count not
