@@ -251,7 +251,7 @@ struct gbo_nn
     float *feat32 = nullptr;
     unsigned char *alive = nullptr;
     float eps32 = 0.f;
-    DevBuf qfeat, fb_list, part;
+    DevBuf qfeat, fb_list, part, qorder;
     CounterRing ctr;
     unsigned long long queries = 0;
     std::mutex mu;
@@ -1472,8 +1472,21 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         int64_t *part_k = (int64_t *)nn->part.p;
         float *part_d = (float *)(part_k + pl);
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
+        // large batches without prefix limits run in spatial order (the lanes of a warp then prune the
+        // same elements); with PRM prefix limits the given order keeps each CTA's scan range short
+        const int64_t *order = nullptr;
+        if (!prefix && nq >= 1024)
+        {
+            const size_t wb = ((size_t)3 * kQueryKeys + nq) * sizeof(int);
+            if (auto st = nn->qorder.reserve(wb + (size_t)nq * sizeof(int64_t) + 16, lc.stream))
+                return st;
+            int *work = (int *)nn->qorder.p;
+            int64_t *ord = (int64_t *)((char *)nn->qorder.p + pad16(wb));
+            launch_query_order(lc, nn->sp, (const float *)nn->qfeat.p, nq, work, ord);
+            order = ord;
+        }
         if (launch_knn_fp32(lc, a, nn->sp, qv, (const float *)nn->qfeat.p, nq, k, prefix, idx, dist,
-                            (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P))
+                            (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P, order))
         {
             // queries whose FP32 band overflowed: exact FP64 scan (count read on the device)
             launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist, (const unsigned long long *)nn->fb_list.p,

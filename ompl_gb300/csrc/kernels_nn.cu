@@ -202,11 +202,13 @@ __device__ __forceinline__ float chain_dist32(const float *a, const float *b, in
 }
 
 // Partial scan: CTA (x = block of 128 queries, y = chunk of elements). Each thread keeps the K_KEEP
-// smallest FP32 distances (squared for box/wrapped kinds) of its query within the chunk.
+// smallest FP32 distances (squared for box/wrapped kinds) of its query within the chunk. qorder
+// (nullable): thread qs takes query qorder[qs] (queries in spatial order, so that the lanes of a warp
+// prune the same elements); its list is kept at position qs.
 template <int KIND, int MAXF, int K_KEEP>
 __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp, const float *qf, int64_t nq,
                                                        const int64_t *prefix, int64_t chunk, float *part_d,
-                                                       int64_t *part_k)
+                                                       int64_t *part_k, const int64_t *qorder)
 {
     constexpr int TILE = 128;
     constexpr int FP = (MAXF + 3) / 4 * 4;
@@ -214,8 +216,9 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
     __shared__ unsigned char tile_alive[TILE];
     __shared__ unsigned long long s_limit;
     const int F = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 2 * sp.dim : sp.dim;
-    const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = qi < nq;
+    const int64_t qs = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = qs < nq;
+    const int64_t qi = active && qorder ? qorder[qs] : qs;
     const int64_t c0 = (int64_t)blockIdx.y * chunk;
     const int64_t c1 = min(c0 + chunk, nn.size);
     float qfe[FP];
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
     }
     if (!active)
         return;
-    const int64_t o = ((int64_t)blockIdx.y * nq + qi) * K_KEEP;
+    const int64_t o = ((int64_t)blockIdx.y * nq + qs) * K_KEEP;
 #pragma unroll
     for (int j = 0; j < K_KEEP; ++j)
     {
@@ -304,15 +307,18 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
 // Merge the per-chunk lists, then decide in FP64: every element within 2*eps of the k-th FP32
 // distance is re-evaluated with the reference-order FP64 distance and the final order is
 // (FP64 distance, key). If the band may hold more than K_KEEP elements the query goes to the FP64 scan.
+// qorder (nullable): the lists are kept per position qs of the query order, query qorder[qs].
 template <int KIND, int MAXD, int K_KEEP>
 __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams sp, StatesView qv, int64_t nq, int k,
                                                          int P, const float *part_d, const int64_t *part_k,
                                                          int64_t *idx, double *dist, unsigned long long *fb_list,
-                                                         unsigned long long *fb_n, RunCounters *ctr)
+                                                         unsigned long long *fb_n, RunCounters *ctr,
+                                                         const int64_t *qorder)
 {
-    const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= nq)
+    const int64_t qs = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qs >= nq)
         return;
+    const int64_t qi = qorder ? qorder[qs] : qs;
     float dk[K_KEEP];
     int64_t ik[K_KEEP];
 #pragma unroll
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
     // dropped: smallest distance of an element that fell out of some chunk's list (bounds the rest)
     for (int c = 0; c < P; ++c)
     {
-        const int64_t o = ((int64_t)c * nq + qi) * K_KEEP;
+        const int64_t o = ((int64_t)c * nq + qs) * K_KEEP;
         for (int j = 0; j < K_KEEP; ++j)
         {
             const int64_t key = part_k[o + j];
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
     bool overflow = ik[K_KEEP - 1] >= 0 && !(dk[K_KEEP - 1] > band);
     for (int c = 0; c < P && !overflow; ++c)
     {
-        const int64_t o = ((int64_t)c * nq + qi) * K_KEEP;
+        const int64_t o = ((int64_t)c * nq + qs) * K_KEEP;
         overflow = part_k[o + K_KEEP - 1] >= 0 && !(part_d[o + K_KEEP - 1] > band);
     }
     if (overflow)
@@ -553,13 +559,13 @@ template <int KIND, int MAXD, int MAXF, int K_KEEP>
 static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                           int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist,
                           unsigned long long *fb_list, unsigned long long *fb_n, RunCounters *ctr, float *part_d,
-                          int64_t *part_k, int P, int64_t chunk)
+                          int64_t *part_k, int P, int64_t chunk, const int64_t *qorder)
 {
     const int qb = (int)((nq + 127) / 128);
     knn_scan_kernel<KIND, MAXF, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix, chunk, part_d,
-                                                                           part_k);
+                                                                           part_k, qorder);
     knn_finish_kernel<KIND, MAXD, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,
-                                                                    fb_list, fb_n, ctr);
+                                                                    fb_list, fb_n, ctr, qorder);
     note_launch();
     note_launch();
 }
@@ -574,7 +580,8 @@ int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size)
 
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
+                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
+                     const int64_t *qorder)
 {
     if (k > 20 || nq == 0)
         return false;
@@ -584,10 +591,10 @@ bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &s
     {                                                                                                                 \
         if (k <= 12)                                                                                                  \
             launch_fp32_t<KIND, MAXD, MAXF, 16>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
-                                                part_d, part_k, P, chunk);                                            \
+                                                part_d, part_k, P, chunk, qorder);                                            \
         else                                                                                                          \
             launch_fp32_t<KIND, MAXD, MAXF, 24>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
-                                                part_d, part_k, P, chunk);                                            \
+                                                part_d, part_k, P, chunk, qorder);                                            \
     } while (0)
     if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN && sp.dim <= 10)
         GBO_FP32(GBO_SPACE_KINEMATIC_CHAIN, 10, 20);
@@ -639,6 +646,96 @@ void launch_radius(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp,
     else
         radius_kernel<16><<<grid, 256, 0, lc.stream>>>(nn, sp, qv, nq, r, counts, offsets, idx, dist);
     note_launch();
+}
+
+// ---------------------------------------------------------------- query order (large batches)
+// A cell key per query from a few quantised features: chain metric, the tip and middle-joint points
+// (X_i, Y_i in units of the link length: roughly mean 0 and variance (i + 1) / 2 for uniform joints,
+// 8 levels over +-2.5 standard deviations each); box and wrapped kinds, the first four coordinates over
+// their bounds (8 levels each). A counting sort by key gives the processing order.
+__device__ __forceinline__ int query_level(float v, float lo, float hi)
+{
+    int l = (int)floorf((v - lo) * (8.0f / (hi - lo)));
+    return l < 0 ? 0 : (l > 7 ? 7 : l);
+}
+
+__global__ void query_key_kernel(SpaceParams sp, const float *qf, int64_t nq, int *key, int *count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        int c = 0;
+        if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN)
+        {
+            const int links[2] = {sp.dim - 1, sp.dim / 2 - 1 > 0 ? sp.dim / 2 - 1 : 0};
+            for (int t = 0; t < 2; ++t)
+            {
+                const float r = 2.5f * sqrtf(0.5f * (float)(links[t] + 1));
+                c = c * 64 + query_level(qf[(int64_t)(2 * links[t]) * nq + i], -r, r) * 8 +
+                    query_level(qf[(int64_t)(2 * links[t] + 1) * nq + i], -r, r);
+            }
+        }
+        else
+        {
+            for (int d = 0; d < 4; ++d)
+            {
+                int l = 0;
+                if (d < sp.dim)
+                {
+                    const float lo = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.low[d] : -3.14159265f;
+                    const float hi = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.high[d] : 3.14159265f;
+                    l = hi > lo ? query_level(qf[(int64_t)d * nq + i], lo, hi) : 0;
+                }
+                c = c * 8 + l;
+            }
+        }
+        key[i] = c;
+        atomicAdd(&count[c], 1);
+    }
+}
+
+// exclusive scan of the 4096 key counts (one CTA of 1024 threads, 4 keys each); fill[] cleared
+__global__ void __launch_bounds__(1024) query_scan_kernel(const int *count, int *start, int *fill)
+{
+    __shared__ int part[1024];
+    const int i0 = threadIdx.x * 4;
+    const int s0 = count[i0], s1 = count[i0 + 1], s2 = count[i0 + 2], s3 = count[i0 + 3];
+    part[threadIdx.x] = s0 + s1 + s2 + s3;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    const int run = part[threadIdx.x] - (s0 + s1 + s2 + s3);
+    start[i0] = run;
+    start[i0 + 1] = run + s0;
+    start[i0 + 2] = run + s0 + s1;
+    start[i0 + 3] = run + s0 + s1 + s2;
+    fill[i0] = fill[i0 + 1] = fill[i0 + 2] = fill[i0 + 3] = 0;
+}
+
+__global__ void query_scatter_kernel(const int *key, int64_t nq, const int *start, int *fill, int64_t *order)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int c = key[i];
+        order[start[c] + atomicAdd(&fill[c], 1)] = i;
+    }
+}
+
+void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float *qf, int64_t nq, int *work,
+                        int64_t *order)
+{
+    int *count = work, *start = work + kQueryKeys, *fill = work + 2 * kQueryKeys, *key = work + 3 * kQueryKeys;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nq + 255) / 256, (int64_t)lc.sm_count * 8));
+    cudaMemsetAsync(count, 0, kQueryKeys * sizeof(int), lc.stream);
+    query_key_kernel<<<grid, 256, 0, lc.stream>>>(sp, qf, nq, key, count);
+    query_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, start, fill);
+    query_scatter_kernel<<<grid, 256, 0, lc.stream>>>(key, nq, start, fill, order);
+    for (int i = 0; i < 3; ++i)
+        note_launch();
 }
 
 }  // namespace gbo

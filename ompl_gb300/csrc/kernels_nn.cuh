@@ -20,7 +20,13 @@ void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &
                       const unsigned long long *list_n, int64_t max_items);
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P);
+                     unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
+                     const int64_t *qorder);
+// Spatial processing order of a query batch (counting sort by a cell key of its FP32 features):
+// work holds 3 * kQueryKeys + nq ints, order nq entries.
+constexpr int kQueryKeys = 4096;
+void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float *qf, int64_t nq, int *work,
+                        int64_t *order);
 int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size);
 void launch_features(const LaunchCfg &lc, const SpaceParams &sp, StatesView v, int64_t n, float *out, int64_t ld_out);
 void launch_store_points(const LaunchCfg &lc, StatesView v, int64_t n, int dim, double *pts, int64_t cap,
