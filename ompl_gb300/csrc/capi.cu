@@ -231,7 +231,7 @@ struct gbo_sampler
     std::mutex mu;
     cudaStream_t host_stream = nullptr;
     Pinned pin;
-    DevBuf dev;
+    DevBuf dev, words;  // words: the word-stream scratch of the device calls
     ~gbo_sampler()
     {
         if (host_stream)
@@ -1215,12 +1215,24 @@ gbo_status gbo_sampler_destroy(gbo_sampler *s)
     return GBO_OK;
 }
 
+// Word-stream scratch of a sampling call of n states (stream-ordered growth): 2 words per value, at
+// most 16M words (larger calls run in chunks).
+static gbo_status sampler_words(gbo_sampler *s, int64_t n, gbo_stream stream, int64_t &cap)
+{
+    cap = std::max<int64_t>(2, std::min<int64_t>(2 * n * s->sp.dim, (int64_t)1 << 24));
+    return s->words.reserve((size_t)cap * sizeof(unsigned), (cudaStream_t)stream);
+}
+
 gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream)
 {
     if (!s || n < 0 || (n > 0 && !out) || !valid_layout(layout, n, ld, s->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
     StatesView ov = make_view(out, ld, layout);
-    launch_sample_uniform(lcfg(stream), s->st, s->sp, nullptr, StatesView{}, 0.0, n, MutStatesView{out, ov.si, ov.sd});
+    int64_t cap = 0;
+    if (auto st = sampler_words(s, n, stream, cap))
+        return st;
+    launch_sample_uniform(lcfg(stream), s->st, s->sp, nullptr, StatesView{}, 0.0, n, MutStatesView{out, ov.si, ov.sd},
+                          (unsigned *)s->words.p, cap);
     CHECK_LAUNCH();
     return GBO_OK;
 }
@@ -1231,8 +1243,11 @@ gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double di
     if (!s || n < 0 || (n > 0 && (!out || !near)) || !valid_layout(layout, n, ld, s->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniformNear arguments");
     StatesView ov = make_view(out, ld, layout);
+    int64_t cap = 0;
+    if (auto st = sampler_words(s, n, stream, cap))
+        return st;
     launch_sample_uniform(lcfg(stream), s->st, s->sp, near, make_view(near, ld, layout), distance, n,
-                          MutStatesView{out, ov.si, ov.sd});
+                          MutStatesView{out, ov.si, ov.sd}, (unsigned *)s->words.p, cap);
     CHECK_LAUNCH();
     return GBO_OK;
 }

@@ -42,8 +42,10 @@ struct SamplerState
     unsigned int pos;     // next word index in mt (624 = twist needed)
     unsigned int pad[3];
 };
+// words: scratch of cap_words (even, >= 2) 32-bit words; calls above cap_words / 2 values run in chunks
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
-                           StatesView nearv, double distance, int64_t n, MutStatesView out);
+                           StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *words,
+                           int64_t cap_words);
 double measure_fp32_peak(const LaunchCfg &lc);
 double measure_fp64_peak(const LaunchCfg &lc);
 void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s);

@@ -4,9 +4,11 @@
 // The stream is OMPL's RNG (RandomNumbers.h:66-76): std::mt19937 -> libstdc++
 // generate_canonical<double, 53> (two 32-bit draws w0, w1: (w0 + w1 * 2^32) / 2^64, values >= 1
 // replaced by the largest double below 1) -> uniformReal(lo, hi) = (hi - lo) * U + lo.
-// mt19937 (Matsumoto & Nishimura 1998) is sequential across 624-word blocks, so one CTA owns one
-// stream: the block regeneration runs in the three dependency-free chunks [0,227), [227,454),
-// [454,623) plus word 623, then all threads temper and convert the block's words.
+// mt19937 (Matsumoto & Nishimura 1998) is sequential across 624-word blocks, so one CTA produces a
+// sampler's word stream (mt_words_kernel) and the whole GPU converts word pairs into coordinates
+// (words_to_states_kernel); large calls alternate the two over chunks of the stream.
+#include <algorithm>
+
 #include "kernels_nn.cuh"
 
 namespace gbo
@@ -27,36 +29,6 @@ __device__ __forceinline__ unsigned twist_word(unsigned cur, unsigned next, unsi
     return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
 }
 
-__device__ void regenerate(unsigned *mt)
-{
-    const int t = threadIdx.x;
-    // chunk 1: k in [0, 227): mt[k + 397] still old
-    unsigned v = 0;
-    if (t < 227)
-        v = twist_word(mt[t], mt[t + 1], mt[t + 397]);
-    __syncthreads();
-    if (t < 227)
-        mt[t] = v;
-    __syncthreads();
-    // chunk 2: k in [227, 454): mt[k - 227] new (chunk 1), mt[k + 1] old
-    if (t < 227)
-        v = twist_word(mt[t + 227], mt[t + 228], mt[t]);
-    __syncthreads();
-    if (t < 227)
-        mt[t + 227] = v;
-    __syncthreads();
-    // chunk 3: k in [454, 623): mt[k - 227] new (chunk 2), mt[k + 1] old
-    if (t < 169)
-        v = twist_word(mt[t + 454], mt[t + 455], mt[t + 227]);
-    __syncthreads();
-    if (t < 169)
-        mt[t + 454] = v;
-    __syncthreads();
-    if (t == 0)
-        mt[623] = twist_word(mt[623], mt[0], mt[396]);
-    __syncthreads();
-}
-
 __device__ __forceinline__ double canonical53(unsigned w0, unsigned w1)
 {
     double sum = (double)w0;
@@ -67,123 +39,133 @@ __device__ __forceinline__ double canonical53(unsigned w0, unsigned w1)
     return r;
 }
 
-// One CTA: n states of sp.dim values, value v = (state v / dim, coordinate v % dim) drawn from the
-// word pair (2v, 2v+1) of the stream continuing at st->pos.
-__global__ void __launch_bounds__(256) sample_kernel(SamplerState *st, SpaceParams sp, StatesView nearv, int use_near,
-                                                     double distance, int64_t n, MutStatesView out)
+// The word stream: one CTA continues the stream at st->pos and writes its next W tempered words to
+// out, then saves the generator. A block's regeneration runs in the three dependency-free chunks
+// [0,227), [227,454), [454,623) and word 623 into a second buffer (4 barriers per block), and each
+// word is tempered and stored as soon as its chunk produces it.
+__global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t W, unsigned *out)
 {
-    __shared__ unsigned mt[624];
-    __shared__ unsigned tw[624];
-    __shared__ unsigned s_pending;
-    __shared__ int s_has_pending;
-    for (int i = threadIdx.x; i < 624; i += blockDim.x)
-        mt[i] = st->mt[i];
-    unsigned pos = st->pos;
-    if (threadIdx.x == 0)
-        s_has_pending = 0;
+    __shared__ unsigned buf[2][624];
+    unsigned *cur = buf[0], *nxt = buf[1];
+    const int t = threadIdx.x;
+    for (int i = t; i < 624; i += blockDim.x)
+        cur[i] = st->mt[i];
+    int pos = (int)st->pos;  // next unused word of cur (624: none)
     __syncthreads();
-    const int64_t total = n * sp.dim;
-    int64_t v0 = 0;  // next value index
-    while (v0 < total)
+    int64_t w = min((int64_t)(624 - pos), W);  // the rest of the current block
+    for (int i = t; i < (int)w; i += blockDim.x)
+        out[i] = temper(cur[pos + i]);
+    pos += (int)w;
+    while (w < W)
     {
-        if (pos >= 624)
+        const int m = (int)min((int64_t)624, W - w);  // words of the new block that are used
+        unsigned *o = out + w;
+        if (t < 227)
         {
-            regenerate(mt);
-            pos = 0;
-        }
-        for (int i = threadIdx.x; i < 624; i += blockDim.x)
-            tw[i] = temper(mt[i]);
-        __syncthreads();
-        // words [pos, 624) of this block; a pending word from the previous block pairs with tw[pos]
-        int start = pos;
-        const int has_pending = s_has_pending;
-        const unsigned pending = s_pending;
-        if (has_pending)
-            start += 1;
-        const int avail_pairs = (624 - start) / 2;
-        const int64_t nv = min((int64_t)avail_pairs + (has_pending ? 1 : 0), total - v0);
-        for (int64_t m = threadIdx.x; m < nv; m += blockDim.x)
-        {
-            unsigned w0, w1;
-            if (has_pending && m == 0)
-            {
-                w0 = pending;
-                w1 = tw[pos];
-            }
-            else
-            {
-                const int off = start + 2 * (int)(m - (has_pending ? 1 : 0));
-                w0 = tw[off];
-                w1 = tw[off + 1];
-            }
-            const double U = canonical53(w0, w1);
-            const int64_t v = v0 + m;
-            const int64_t i = v / sp.dim;
-            const int d = (int)(v - i * sp.dim);
-            double lo, hi;
-            if (use_near)
-            {
-                const double c = nearv(i, d);
-                if (sp.kind == GBO_SPACE_SO2)
-                {
-                    lo = __dsub_rn(c, distance);
-                    hi = __dadd_rn(c, distance);
-                }
-                else
-                {
-                    lo = fmax(sp.low[d], __dsub_rn(c, distance));
-                    hi = fmin(sp.high[d], __dadd_rn(c, distance));
-                }
-            }
-            else
-            {
-                lo = sp.low[d];
-                hi = sp.high[d];
-            }
-            double x = __dadd_rn(__dmul_rn(__dsub_rn(hi, lo), U), lo);
-            if (use_near && sp.kind == GBO_SPACE_SO2)
-            {
-                // SO2StateSpace::enforceBounds (SO2StateSpace.cpp:79-87)
-                double y = fmod(x, 2.0 * kPi);
-                if (y < -kPi)
-                    y = __dadd_rn(y, 2.0 * kPi);
-                else if (y >= kPi)
-                    y = __dsub_rn(y, 2.0 * kPi);
-                x = y;
-            }
-            out(i, d) = x;
-        }
-        // advance the stream position
-        int used = 2 * (int)nv - (has_pending ? 1 : 0);
-        const int newpos = pos + used;
-        __syncthreads();
-        if (threadIdx.x == 0)
-        {
-            s_has_pending = 0;
-            if (v0 + nv < total && newpos == 623)
-            {
-                s_pending = tw[623];
-                s_has_pending = 1;
-            }
+            const unsigned v = twist_word(cur[t], cur[t + 1], cur[t + 397]);
+            nxt[t] = v;
+            if (t < m)
+                o[t] = temper(v);
         }
         __syncthreads();
-        v0 += nv;
-        pos = s_has_pending ? 624 : newpos;
+        if (t < 227)
+        {
+            const unsigned v = twist_word(cur[t + 227], cur[t + 228], nxt[t]);
+            nxt[t + 227] = v;
+            if (t + 227 < m)
+                o[t + 227] = temper(v);
+        }
+        __syncthreads();
+        if (t < 169)
+        {
+            const unsigned v = twist_word(cur[t + 454], cur[t + 455], nxt[t + 227]);
+            nxt[t + 454] = v;
+            if (t + 454 < m)
+                o[t + 454] = temper(v);
+        }
+        __syncthreads();
+        if (t == 0)
+        {
+            const unsigned v = twist_word(cur[623], nxt[0], nxt[396]);
+            nxt[623] = v;
+            if (623 < m)
+                o[623] = temper(v);
+        }
+        __syncthreads();
+        unsigned *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        w += m;
+        pos = m;
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 624; i += blockDim.x)
-        st->mt[i] = mt[i];
-    if (threadIdx.x == 0)
-        st->pos = pos;
+    for (int i = t; i < 624; i += blockDim.x)
+        st->mt[i] = cur[i];
+    if (t == 0)
+        st->pos = (unsigned)pos;
+}
+
+// Values v0 .. v0 + nv - 1 of a sampling call (value v = coordinate v % dim of state v / dim) from the
+// word pairs (2m, 2m + 1), m = v - v0, of the word stream: generate_canonical<double, 53> and
+// uniformReal (or the near bounds), across the whole GPU.
+__global__ void __launch_bounds__(256) words_to_states_kernel(const unsigned *words, int64_t v0, int64_t nv,
+                                                              SpaceParams sp, StatesView nearv, int use_near,
+                                                              double distance, MutStatesView out)
+{
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < nv; m += (int64_t)gridDim.x * blockDim.x)
+    {
+        const double U = canonical53(words[2 * m], words[2 * m + 1]);
+        const int64_t v = v0 + m;
+        const int64_t i = v / sp.dim;
+        const int d = (int)(v - i * sp.dim);
+        double lo, hi;
+        if (use_near)
+        {
+            const double c = nearv(i, d);
+            if (sp.kind == GBO_SPACE_SO2)
+            {
+                lo = __dsub_rn(c, distance);
+                hi = __dadd_rn(c, distance);
+            }
+            else
+            {
+                lo = fmax(sp.low[d], __dsub_rn(c, distance));
+                hi = fmin(sp.high[d], __dadd_rn(c, distance));
+            }
+        }
+        else
+        {
+            lo = sp.low[d];
+            hi = sp.high[d];
+        }
+        double x = __dadd_rn(__dmul_rn(__dsub_rn(hi, lo), U), lo);
+        if (use_near && sp.kind == GBO_SPACE_SO2)
+        {
+            // SO2StateSpace::enforceBounds (SO2StateSpace.cpp:79-87)
+            double y = fmod(x, 2.0 * kPi);
+            if (y < -kPi)
+                y = __dadd_rn(y, 2.0 * kPi);
+            else if (y >= kPi)
+                y = __dsub_rn(y, 2.0 * kPi);
+            x = y;
+        }
+        out(i, d) = x;
+    }
 }
 
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
-                           StatesView nearv, double distance, int64_t n, MutStatesView out)
+                           StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *words,
+                           int64_t cap_words)
 {
-    if (n == 0)
-        return;
-    sample_kernel<<<1, 256, 0, lc.stream>>>(st, sp, nearv, near != nullptr, distance, n, out);
-    note_launch();
+    const int64_t total = n * sp.dim, chunk = cap_words / 2;
+    for (int64_t v0 = 0; v0 < total; v0 += chunk)
+    {
+        const int64_t nv = std::min(chunk, total - v0);
+        mt_words_kernel<<<1, 256, 0, lc.stream>>>(st, 2 * nv, words);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t)lc.sm_count * 8));
+        words_to_states_kernel<<<grid, 256, 0, lc.stream>>>(words, v0, nv, sp, nearv, near != nullptr, distance, out);
+        note_launch();
+        note_launch();
+    }
 }
 
 // FP32 FMA throughput probe: independent FMA chains, no memory traffic in the loop.

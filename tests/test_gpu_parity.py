@@ -113,6 +113,22 @@ def test_sampler_large_stream_vs_oracle(port):
     assert same_bits(a.T, ref[:100_000]) and same_bits(b, ref[100_000:])
 
 
+def test_sampler_stream_across_word_chunks_vs_oracle(port):
+    """A call of 9M values (18M words of the stream, more than one chunk of the word scratch) and the
+    calls around it continue one stream exactly as OMPL's sampler draws it, odd-length calls included."""
+    d = SpaceDesc(capi.SPACE_REAL_VECTOR, 2, np.array([-1.0, 0.0]), np.array([1.0, 3.0]))
+    s = gpu_space(d)
+    smp = B.StateSampler(s, 29)
+    a = smp.sampleUniform(311)
+    b = smp.sampleUniform(4_500_000, host=False)
+    c = smp.sampleUniform(5)
+    ref = port.sample_uniform(d, 29, 311 + 4_500_000 + 5)
+    assert same_bits(a, ref[:311]) and same_bits(c, ref[-5:])
+    bb = b.cpu().numpy()
+    assert same_bits(bb[:1000], ref[311:1311]) and same_bits(bb[-1000:], ref[-1005:-5])
+    assert same_bits(bb, ref[311:-5])
+
+
 # ------------------------------------------------------------------ validity / motion vs OMPL fixtures
 CASES = ["circles_seeded", "circles_ompl_tests", "chain_seeded", "chain_horn", "dh_arm"]
 
