@@ -241,6 +241,16 @@ struct gbo_sampler
     }
 };
 
+// Cell index of a gbo_nn over a RealVector / wrapped space (kernels_nn.cu): built by the first large
+// batch after a change of the element set (add / remove / clear clear `valid`).
+struct NNBoxCells
+{
+    bool valid = false;
+    int L = 0, C = 0;
+    DevBuf cell, count, start, fill, skey, pts8, box;
+    DevBuf qcell, qcount, qstart, qfill, qorder;
+};
+
 struct gbo_nn
 {
     SpaceParams sp{};
@@ -251,6 +261,7 @@ struct gbo_nn
     float *feat32 = nullptr;
     unsigned char *alive = nullptr;
     float eps32 = 0.f;
+    NNBoxCells cells;
     DevBuf qfeat, fb_list, part, qorder;
     CounterRing ctr;
     unsigned long long queries = 0;
@@ -1402,6 +1413,7 @@ gbo_status gbo_nn_add(gbo_nn *nn, const double *states, int64_t n, int64_t ld, i
     CHECK_LAUNCH();
     nn->size += n;
     nn->alive_count += n;
+    nn->cells.valid = false;
     return GBO_OK;
 }
 
@@ -1412,6 +1424,7 @@ gbo_status gbo_nn_remove(gbo_nn *nn, const int64_t *keys, int64_t n, gbo_stream 
     launch_remove(lcfg(stream), keys, n, nn->size, nn->alive);
     CHECK_LAUNCH();
     nn->alive_count = -1;  // recounted on demand
+    nn->cells.valid = false;
     return GBO_OK;
 }
 
@@ -1423,6 +1436,7 @@ gbo_status gbo_nn_clear(gbo_nn *nn)
     CUDA_TRY(cudaMemset(nn->alive, 0, nn->cap));
     nn->size = 0;
     nn->alive_count = 0;
+    nn->cells.valid = false;
     return GBO_OK;
 }
 
@@ -1458,6 +1472,31 @@ static NNArgs nn_args(const gbo_nn *nn)
     return a;
 }
 
+// (Re)build the cell index of a RealVector / wrapped gbo_nn in stream order.
+static gbo_status ensure_box_cells(gbo_nn *nn, const LaunchCfg &lc)
+{
+    NNBoxCells &c = nn->cells;
+    if (c.valid)
+        return GBO_OK;
+    c.L = bcell_levels(nn->sp.dim, nn->size);
+    c.C = 1;
+    for (int d = 0; d < nn->sp.dim; ++d)
+        c.C *= c.L;
+    const int64_t n = std::max<int64_t>(nn->size, 1);
+    const cudaStream_t s = lc.stream;
+    for (auto r : {c.cell.reserve((size_t)n * sizeof(int), s), c.count.reserve((size_t)c.C * sizeof(int), s),
+                   c.start.reserve((size_t)(c.C + 1) * sizeof(int), s), c.fill.reserve((size_t)c.C * sizeof(int), s),
+                   c.skey.reserve((size_t)n * sizeof(int64_t), s), c.pts8.reserve((size_t)n * 2 * sizeof(float4), s),
+                   c.box.reserve((size_t)c.C * 4 * sizeof(float4), s)})
+        if (r)
+            return r;
+    launch_bcell_build(lc, nn_args(nn), nn->sp, c.L, c.C, (int *)c.cell.p, (int *)c.count.p, (int *)c.start.p,
+                       (int *)c.fill.p, (int64_t *)c.skey.p, (float4 *)c.pts8.p, (float4 *)c.box.p);
+    CHECK_LAUNCH();
+    c.valid = true;
+    return GBO_OK;
+}
+
 gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
                             const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream)
 {
@@ -1487,6 +1526,37 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         int64_t *part_k = (int64_t *)nn->part.p;
         float *part_d = (float *)(part_k + pl);
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
+        // large batches over a large RealVector / wrapped index: cell index (PRM's prefix kNN)
+        if ((nn->sp.kind == GBO_SPACE_WRAP_L2 || nn->sp.kind == GBO_SPACE_REAL_VECTOR) && nn->sp.dim <= 8 &&
+            nn->size >= 65536 && nn->size < (1ll << 31) && nq >= 4096)
+        {
+            if (auto st = ensure_box_cells(nn, lc))
+                return st;
+            NNBoxCells &c = nn->cells;
+            const int bands = prefix ? 4 : 1, keys = bands * c.C;
+            for (auto r : {c.qcell.reserve((size_t)nq * sizeof(int), lc.stream),
+                           c.qcount.reserve((size_t)keys * sizeof(int), lc.stream),
+                           c.qstart.reserve((size_t)(keys + 1) * sizeof(int), lc.stream),
+                           c.qfill.reserve((size_t)keys * sizeof(int), lc.stream),
+                           c.qorder.reserve((size_t)nq * sizeof(int64_t), lc.stream)})
+                if (r)
+                    return r;
+            launch_bcell_query_order(lc, nn->sp, c.L, c.C, (const float *)nn->qfeat.p, nq, prefix, nn->size, bands,
+                                     (int *)c.qcell.p, (int *)c.qcount.p, (int *)c.qstart.p, (int *)c.qfill.p,
+                                     (int64_t *)c.qorder.p);
+            BoxCellArgs ci{(const int *)c.start.p, (const int64_t *)c.skey.p, (const float4 *)c.pts8.p,
+                           (const float4 *)c.box.p, c.C};
+            const int Pc = std::max(1, std::min(P, c.C));
+            if (launch_knn_bcell(lc, a, ci, nn->sp, qv, (const float *)nn->qfeat.p, nq, (const int64_t *)c.qorder.p,
+                                 (const int *)c.qcell.p, k, prefix, idx, dist, (unsigned long long *)nn->fb_list.p,
+                                 fb_n, ctr, part_d, part_k, Pc))
+            {
+                launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist,
+                                 (const unsigned long long *)nn->fb_list.p, fb_n, std::min<int64_t>(nq, 4096));
+                CHECK_LAUNCH();
+                return GBO_OK;
+            }
+        }
         // large batches without prefix limits run in spatial order (the lanes of a warp then prune the
         // same elements); with PRM prefix limits the given order keeps each CTA's scan range short
         const int64_t *order = nullptr;

@@ -14,6 +14,8 @@
 //                     distance is re-evaluated in FP64 and the final order is decided in FP64. If the
 //                     band may hold more than K_KEEP elements the query is queued for knn_exact_kernel.
 //   radius kernels    FP64 count / fill (CSR), sorted by (distance, key).
+#include <climits>
+
 #include "kernels_nn.cuh"
 
 namespace gbo
@@ -205,10 +207,13 @@ __device__ __forceinline__ float chain_dist32(const float *a, const float *b, in
 // smallest FP32 distances (squared for box/wrapped kinds) of its query within the chunk. qorder
 // (nullable): thread qs takes query qorder[qs] (queries in spatial order, so that the lanes of a warp
 // prune the same elements); its list is kept at position qs.
+// qkey (nullable): only the queries with qkey < key_limit are this launch's (the others' lists are
+// written by the cell kernel).
 template <int KIND, int MAXF, int K_KEEP>
 __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp, const float *qf, int64_t nq,
                                                        const int64_t *prefix, int64_t chunk, float *part_d,
-                                                       int64_t *part_k, const int64_t *qorder)
+                                                       int64_t *part_k, const int64_t *qorder, const int *qkey,
+                                                       int key_limit)
 {
     constexpr int TILE = 128;
     constexpr int FP = (MAXF + 3) / 4 * 4;
@@ -217,8 +222,8 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
     __shared__ unsigned long long s_limit;
     const int F = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 2 * sp.dim : sp.dim;
     const int64_t qs = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = qs < nq;
-    const int64_t qi = active && qorder ? qorder[qs] : qs;
+    const int64_t qi = qs < nq && qorder ? qorder[qs] : qs;
+    const bool active = qs < nq && (!qkey || qkey[qi] < key_limit);
     const int64_t c0 = (int64_t)blockIdx.y * chunk;
     const int64_t c1 = min(c0 + chunk, nn.size);
     float qfe[FP];
@@ -563,7 +568,7 @@ static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpacePara
 {
     const int qb = (int)((nq + 127) / 128);
     knn_scan_kernel<KIND, MAXF, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix, chunk, part_d,
-                                                                           part_k, qorder);
+                                                                           part_k, qorder, nullptr, 0);
     knn_finish_kernel<KIND, MAXD, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,
                                                                     fb_list, fb_n, ctr, qorder);
     note_launch();
@@ -736,6 +741,393 @@ void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float 
     query_scatter_kernel<<<grid, 256, 0, lc.stream>>>(key, nq, start, fill, order);
     for (int i = 0; i < 3; ++i)
         note_launch();
+}
+
+// ---------------------------------------------------------------- cell index for box and wrapped spaces
+// Large batches over a large RealVector / wrapped index (PRM's prefix kNN): the alive elements are
+// bucketed by a uniform grid of L levels per coordinate (counting sort); each cell keeps its elements'
+// FP32 coordinates (two float4 per element, sorted by cell) and their bounding box. Queries are
+// processed in (band of their prefix limit, cell) order, one warp per 32 of them: each lane seeds its
+// threshold T with the k-th FP32 distance among the eligible elements of its own cell (an upper bound on
+// its k-th overall), and the warp skips a cell when, for every lane, the distance from the query to the
+// cell's box is at least min(T, the lane's current K_KEEP-th). Elements beyond T are left out of the
+// lists; the FP64 band of the finish kernel lies below T, so its decisions are unchanged.
+
+__device__ __forceinline__ void bcell_range(const SpaceParams &sp, int d, float &lo, float &hi)
+{
+    if (sp.kind == GBO_SPACE_REAL_VECTOR)
+    {
+        lo = (float)sp.low[d];
+        hi = (float)sp.high[d];
+    }
+    else
+    {
+        lo = -3.14159265358979f;
+        hi = 3.14159265358979f;
+    }
+}
+
+__device__ __forceinline__ int bcell_of(const SpaceParams &sp, int L, const float *f, int64_t ld, int64_t i)
+{
+    int c = 0;
+    for (int d = sp.dim - 1; d >= 0; --d)
+    {
+        float lo, hi;
+        bcell_range(sp, d, lo, hi);
+        int l = hi > lo ? (int)floorf((f[(int64_t)d * ld + i] - lo) * ((float)L / (hi - lo))) : 0;
+        l = l < 0 ? 0 : (l >= L ? L - 1 : l);
+        c = c * L + l;
+    }
+    return c;
+}
+
+__global__ void bcell_assign_kernel(SpaceParams sp, int L, const float *feat, int64_t cap,
+                                    const unsigned char *alive, int64_t n, int *cell, int *count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        if (!alive[i])
+        {
+            cell[i] = -1;
+            continue;
+        }
+        const int c = bcell_of(sp, L, feat, cap, i);
+        cell[i] = c;
+        atomicAdd(&count[c], 1);
+    }
+}
+
+// Exclusive scan of C counts (one CTA of 1024 threads): start[0..C], fill[] cleared.
+__global__ void __launch_bounds__(1024) bcell_scan_kernel(const int *count, int C, int *start, int *fill)
+{
+    __shared__ int part[1024];
+    const int per = (C + 1023) / 1024, i0 = threadIdx.x * per, i1 = min(i0 + per, C);
+    int s = 0;
+    for (int i = i0; i < i1; ++i)
+        s += count[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = part[threadIdx.x] - s;
+    for (int i = i0; i < i1; ++i)
+    {
+        start[i] = run;
+        fill[i] = 0;
+        run += count[i];
+    }
+    if (threadIdx.x == 1023)
+        start[C] = part[1023];
+}
+
+// out[start[c] + arrival order] = i for every row i with c = cell[i] >= 0
+__global__ void bcell_scatter_kernel(const int *cell, int64_t n, const int *start, int *fill, int64_t *out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int c = cell[i];
+        if (c >= 0)
+            out[start[c] + atomicAdd(&fill[c], 1)] = i;
+    }
+}
+
+// sorted coordinates: pts8[2p], pts8[2p + 1] = element skey[p] (unused coordinates 0), p < start[C]
+__global__ void bcell_gather_kernel(const int64_t *skey, const int *start, int C, const float *feat, int64_t cap,
+                                    int dim, float4 *pts8)
+{
+    const int64_t total = start[C];
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t key = skey[p];
+        float v[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+            v[d] = d < dim ? feat[(int64_t)d * cap + key] : 0.f;
+        pts8[2 * p] = make_float4(v[0], v[1], v[2], v[3]);
+        pts8[2 * p + 1] = make_float4(v[4], v[5], v[6], v[7]);
+    }
+}
+
+// box[c] = 4 float4: min of coordinates 0-3, 4-7, then max (warp per cell)
+__global__ void bcell_box_kernel(const float4 *pts8, const int *start, int C, float4 *box)
+{
+    const int lane = threadIdx.x & 31;
+    for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < C; c += (int)((gridDim.x * blockDim.x) >> 5))
+    {
+        float mn[8], mx[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+        {
+            mn[d] = __int_as_float(0x7f800000);
+            mx[d] = -__int_as_float(0x7f800000);
+        }
+        for (int p = start[c] + lane; p < start[c + 1]; p += 32)
+        {
+            const float4 a = pts8[2 * p], b = pts8[2 * p + 1];
+            const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int d = 0; d < 8; ++d)
+            {
+                mn[d] = fminf(mn[d], v[d]);
+                mx[d] = fmaxf(mx[d], v[d]);
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            }
+        if (lane == 0)
+        {
+            box[4 * c] = make_float4(mn[0], mn[1], mn[2], mn[3]);
+            box[4 * c + 1] = make_float4(mn[4], mn[5], mn[6], mn[7]);
+            box[4 * c + 2] = make_float4(mx[0], mx[1], mx[2], mx[3]);
+            box[4 * c + 3] = make_float4(mx[4], mx[5], mx[6], mx[7]);
+        }
+    }
+}
+
+// query key: band then cell. Without prefix limits one band. With them, band 0 holds the queries whose
+// limit is below a quarter of the index (left to the prefix scan: few eligible elements, no useful
+// threshold), bands 1 .. bands - 1 split the rest evenly.
+__global__ void bcell_query_key_kernel(SpaceParams sp, int L, int C, const float *qf, int64_t nq,
+                                       const int64_t *prefix, int64_t index_n, int bands, int *key, int *count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        int band = 0;
+        if (prefix && bands > 1)
+        {
+            const int64_t lim = prefix[i] < 0 ? 0 : (prefix[i] > index_n ? index_n : prefix[i]);
+            const int64_t q4 = index_n / 4, rest = index_n - q4;
+            band = lim < q4 ? 0 : 1 + (int)min((int64_t)bands - 2, (lim - q4) * (bands - 1) / (rest > 0 ? rest : 1));
+        }
+        const int c = band * C + bcell_of(sp, L, qf, nq, i);
+        key[i] = c;
+        atomicAdd(&count[c], 1);
+    }
+}
+
+// distance from query q to the box (lo, hi per coordinate), squared, scaled down by (1 - 1e-5) against
+// the rounding of both sides
+template <int KIND, int MAXF>
+__device__ __forceinline__ float bcell_lb(const float4 *b, const float *q, int dim)
+{
+    const float4 l0 = b[0], l1 = b[1], h0 = b[2], h1 = b[3];
+    const float lo[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+    const float hi[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < MAXF; ++i)
+        if (i < dim)
+        {
+            const float x = q[i];
+            float d;
+            if constexpr (KIND == GBO_SPACE_WRAP_L2 || KIND == GBO_SPACE_SO2)
+            {
+                // nearest point of [lo, hi] on the circle: 0 inside, else the nearer end
+                const float a = fabsf(x - lo[i]), c = fabsf(x - hi[i]);
+                const float wa = fminf(a, 6.28318530717958647692f - a), wc = fminf(c, 6.28318530717958647692f - c);
+                d = (x >= lo[i] && x <= hi[i]) ? 0.f : fminf(wa, wc);
+            }
+            else
+                d = fmaxf(fmaxf(lo[i] - x, x - hi[i]), 0.f);
+            s = fmaf(d, d, s);
+        }
+    return s * (1.0f - 1e-5f);
+}
+
+template <int KIND, int MAXF, int K_KEEP>
+__global__ void __launch_bounds__(128) knn_bcell_kernel(BoxCellArgs ci, SpaceParams sp, float eps, const float *qf,
+                                                        int64_t nq, const int64_t *qorder, const int *qcell,
+                                                        const int64_t *prefix, int k, int cells_per_chunk,
+                                                        float *part_d, int64_t *part_k)
+{
+    const int64_t qs = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t qi = qs < nq ? qorder[qs] : 0;
+    // with prefix limits, band 0 (key < C) belongs to the prefix scan
+    const bool active = qs < nq && (!prefix || qcell[qi] >= ci.C);
+    float qfe[8];
+#pragma unroll
+    for (int f = 0; f < 8; ++f)
+        qfe[f] = (active && f < sp.dim) ? qf[(int64_t)f * nq + qi] : 0.f;
+    const int64_t limit = active ? (prefix ? prefix[qi] : INT64_MAX) : 0;
+    float dk[K_KEEP];
+    int ik[K_KEEP];
+#pragma unroll
+    for (int j = 0; j < K_KEEP; ++j)
+    {
+        dk[j] = __int_as_float(0x7f800000);
+        ik[j] = -1;
+    }
+    auto dist = [&](int64_t p) {
+        const float4 a = ci.pts8[2 * p], b = ci.pts8[2 * p + 1];
+        const float pf[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        return box_dist2<KIND, MAXF>(pf, qfe, sp.dim);
+    };
+    // seed: the k-th distance among the eligible elements of the query's own cell
+    float T = __int_as_float(0x7f800000);
+    if (active)
+    {
+        const int oc = qcell[qi] % ci.C;  // the query key is band * C + cell
+        for (int p = ci.start[oc]; p < ci.start[oc + 1]; ++p)
+        {
+            if (ci.skey[p] >= limit)
+                continue;  // not yet in the roadmap (PRM prefix)
+            const float d = dist(p);
+            if (d < dk[k - 1])
+                topk_insert<K_KEEP>(dk, ik, d, p);
+        }
+        if (dk[k - 1] < __int_as_float(0x7f800000))
+        {
+            const float r = sqrtf(dk[k - 1]) + 2.f * eps;
+            T = r * r * (1.0f + 1e-5f);
+        }
+#pragma unroll
+        for (int j = 0; j < K_KEEP; ++j)
+        {
+            dk[j] = __int_as_float(0x7f800000);
+            ik[j] = -1;
+        }
+    }
+    const int c0 = blockIdx.y * cells_per_chunk, c1 = min(c0 + cells_per_chunk, ci.C);
+    for (int c = c0; c < c1; ++c)
+    {
+        const int s0 = ci.start[c], s1 = ci.start[c + 1];
+        if (s0 == s1)
+            continue;
+        const bool need = active && bcell_lb<KIND, MAXF>(ci.box + 4 * (int64_t)c, qfe, sp.dim) < fminf(T, dk[K_KEEP - 1]);
+        if (!__any_sync(0xffffffffu, need))
+            continue;
+        if (!need)
+            continue;
+        for (int p = s0; p < s1; ++p)
+        {
+            const int64_t key = ci.skey[p];
+            if (key >= limit)
+                continue;
+            const float d = dist(p);
+            if (d < dk[K_KEEP - 1] && d <= T)
+                topk_insert<K_KEEP>(dk, ik, d, (int)key);
+        }
+    }
+    if (!active)
+        return;
+    const int64_t o = ((int64_t)blockIdx.y * nq + qs) * K_KEEP;
+#pragma unroll
+    for (int j = 0; j < K_KEEP; ++j)
+    {
+        part_d[o + j] = dk[j];
+        part_k[o + j] = ik[j];
+    }
+}
+
+int bcell_levels(int dim, int64_t n)
+{
+    // about 40 elements per cell, at most 65536 cells
+    int L = 2;
+    while (true)
+    {
+        int64_t c = 1;
+        for (int d = 0; d < dim; ++d)
+            c *= L + 1;
+        if (c > 65536 || c * 40 > n)
+            break;
+        ++L;
+    }
+    return L;
+}
+
+static int grid_for(const LaunchCfg &lc, int64_t n)
+{
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)lc.sm_count * 8));
+}
+
+void launch_bcell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int L, int C, int *cell,
+                        int *count, int *start, int *fill, int64_t *skey, float4 *pts8, float4 *box)
+{
+    cudaMemsetAsync(count, 0, (size_t)C * sizeof(int), lc.stream);
+    bcell_assign_kernel<<<grid_for(lc, nn.size), 256, 0, lc.stream>>>(sp, L, nn.feat32, nn.cap, nn.alive, nn.size,
+                                                                      cell, count);
+    bcell_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, C, start, fill);
+    bcell_scatter_kernel<<<grid_for(lc, nn.size), 256, 0, lc.stream>>>(cell, nn.size, start, fill, skey);
+    bcell_gather_kernel<<<grid_for(lc, nn.size), 256, 0, lc.stream>>>(skey, start, C, nn.feat32, nn.cap, sp.dim,
+                                                                      pts8);
+    bcell_box_kernel<<<grid_for(lc, (int64_t)C * 32), 256, 0, lc.stream>>>(pts8, start, C, box);
+    for (int i = 0; i < 5; ++i)
+        note_launch();
+}
+
+void launch_bcell_query_order(const LaunchCfg &lc, const SpaceParams &sp, int L, int C, const float *qf, int64_t nq,
+                              const int64_t *prefix, int64_t index_n, int bands, int *qcell, int *count, int *start,
+                              int *fill, int64_t *qorder)
+{
+    const int keys = bands * C;
+    cudaMemsetAsync(count, 0, (size_t)keys * sizeof(int), lc.stream);
+    bcell_query_key_kernel<<<grid_for(lc, nq), 256, 0, lc.stream>>>(sp, L, C, qf, nq, prefix, index_n, bands, qcell,
+                                                                    count);
+    bcell_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, keys, start, fill);
+    bcell_scatter_kernel<<<grid_for(lc, nq), 256, 0, lc.stream>>>(qcell, nq, start, fill, qorder);
+    for (int i = 0; i < 3; ++i)
+        note_launch();
+}
+
+template <int KIND, int K_KEEP>
+static void launch_bcell_t(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
+                           StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
+                           const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
+                           unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
+{
+    const int qb = (int)((nq + 127) / 128);
+    const int per = (ci.C + P - 1) / P;
+    knn_bcell_kernel<KIND, 8, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qcell,
+                                                                         prefix, k, per, part_d, part_k);
+    if (prefix)
+    {
+        // band 0 (limits below a quarter of the index) through the prefix scan, same P lists
+        knn_scan_kernel<KIND, 8, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix,
+                                                                            (nn.size + P - 1) / P, part_d, part_k,
+                                                                            qorder, qcell, ci.C);
+        note_launch();
+    }
+    knn_finish_kernel<KIND, 8, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,
+                                                                 fb_list, fb_n, ctr, qorder);
+    note_launch();
+    note_launch();
+}
+
+bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
+                      StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
+                      const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
+                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
+{
+    if (k > 20 || nq == 0 || sp.dim > 8)
+        return false;
+#define GBO_BCELL(KIND)                                                                                                \
+    do                                                                                                                \
+    {                                                                                                                 \
+        if (k <= 12)                                                                                                  \
+            launch_bcell_t<KIND, 16>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, \
+                                     ctr, part_d, part_k, P);                                                         \
+        else                                                                                                          \
+            launch_bcell_t<KIND, 24>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, \
+                                     ctr, part_d, part_k, P);                                                         \
+    } while (0)
+    if (sp.kind == GBO_SPACE_WRAP_L2)
+        GBO_BCELL(GBO_SPACE_WRAP_L2);
+    else if (sp.kind == GBO_SPACE_REAL_VECTOR)
+        GBO_BCELL(GBO_SPACE_REAL_VECTOR);
+    else
+        return false;
+#undef GBO_BCELL
+    return true;
 }
 
 }  // namespace gbo

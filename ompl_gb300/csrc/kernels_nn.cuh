@@ -22,6 +22,26 @@ bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &s
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
                      const int64_t *qorder);
+// Cell index of a RealVector / wrapped nearest-neighbour index (large batches, PRM prefix kNN).
+struct BoxCellArgs
+{
+    const int *start;      // [C + 1] first sorted position of each cell
+    const int64_t *skey;   // element key at each sorted position
+    const float4 *pts8;    // two float4 (8 coordinates) per sorted position
+    const float4 *box;     // four float4 per cell: min of coordinates 0-3, 4-7, max 0-3, 4-7
+    int C;
+};
+int bcell_levels(int dim, int64_t n);
+void launch_bcell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int L, int C, int *cell,
+                        int *count, int *start, int *fill, int64_t *skey, float4 *pts8, float4 *box);
+void launch_bcell_query_order(const LaunchCfg &lc, const SpaceParams &sp, int L, int C, const float *qf, int64_t nq,
+                              const int64_t *prefix, int64_t index_n, int bands, int *qcell, int *count, int *start,
+                              int *fill, int64_t *qorder);
+bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
+                      StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
+                      const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
+                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P);
+
 // Spatial processing order of a query batch (counting sort by a cell key of its FP32 features):
 // work holds 3 * kQueryKeys + nq ints, order nq entries.
 constexpr int kQueryKeys = 4096;

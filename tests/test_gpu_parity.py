@@ -516,11 +516,12 @@ def test_knn_chain_large_vs_oracle(chain_case, port):
 
 @pytest.mark.parametrize("kind", ["chain10", "wrap7", "rv7"])
 def test_knn_large_batch_vs_exact_scan(kind):
-    """Large batches (4,500 queries over 60,000 elements) through the FP32 scan with FP64 re-check:
-    index sets and FP64 distances must equal the exact FP64 scan's, with and without PRM prefix
-    limits, for fresh and self queries, and after removals."""
+    """Large batches (4,500 queries over 70,000 elements; RealVector and wrapped spaces go through the
+    cell index) with FP32 distances and FP64 re-check: index sets and FP64 distances must equal the
+    exact FP64 scan's, with and without PRM prefix limits, for fresh and self queries, and after
+    removals (which invalidate the cell index)."""
     rng = np.random.default_rng(21)
-    n, dim = 60_000, (10 if kind == "chain10" else 7)
+    n, dim = 70_000, (10 if kind == "chain10" else 7)
     if kind == "chain10":
         space = B.KinematicChainSpace(10, 0.1)
     elif kind == "wrap7":
