@@ -341,12 +341,14 @@ def ours(args, rank, world, local_rank):
     achieved = mean_checked * FLOP_PER_STATE / (mean_ms * 1e-3)
     # DRAM read + write bytes of one launch of the timed kernel, from the committed ncu summary
     # (same 100k-edge batch as one step)
-    traffic = None
+    traffic = issue = None
     prof = os.path.join(ROOT, "profiles", "chain_motion_warp_kernel_chain10.md")
     if os.path.exists(prof):
         for line in open(prof):
             if line.startswith("traffic_bytes_per_launch:"):
                 traffic = int(line.split(":")[1])
+            elif line.startswith("issue_active_frac:"):
+                issue = float(line.split(":")[1])
     # CPU baseline: the oracle port on all host threads, bounded sample of batch 0
     from oracle.oracle import CheckerDesc, Oracle, SpaceDesc
     port = Oracle.port()
@@ -367,6 +369,9 @@ def ours(args, rank, world, local_rank):
         "wall_s": wall,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_fp32 / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak_fp32, "traffic": traffic,
+                     "issue_active_frac": issue,
+                     "note": "the limiter is instruction issue (guard-band compares, shuffles), not FP32 FMA: "
+                             "issue_active_frac is ncu's smsp__issue_active of the same launch",
                      "peak_source": "FP32 FMA throughput measured in this run (gbo_measure_fp32_peak)",
                      "work": f"{FLOP_PER_STATE} flop x checked states ({mean_checked:.0f} per step)"},
         "cpu_baseline": {"value": cpu_v, "unit": "edges/s", "cores": threads, "kind": "port",
