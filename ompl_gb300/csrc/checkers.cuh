@@ -136,16 +136,6 @@ struct ChainGuard
     float self_lo, self_hi, self_den;   // lo, hi, e_den of link-vs-link tests
 };
 
-// 3-valued "x < thr" with |x - x_ref| <= e: returns 1 (true), 0 (false), 2 (ambiguous).
-__device__ __forceinline__ int lt3(float x, float thr, float e)
-{
-    return x < thr - e ? 1 : (x >= thr + e ? 0 : 2);
-}
-__device__ __forceinline__ int gt3(float x, float thr, float e)
-{
-    return x > thr + e ? 1 : (x <= thr - e ? 0 : 2);
-}
-
 // Guarded segment test: returns kInvalid (definite collision), kValid (definite none) or kAmbiguous.
 // Branch-free: every clause of demos/KinematicChain.h:267-274 ("(cmp) == denomPositive => no
 // collision") is classified, then combined: one clause that definitely holds decides "no
