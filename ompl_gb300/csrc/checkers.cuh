@@ -3,7 +3,9 @@
 // FP64 forms reproduce the reference's arithmetic operation for operation (exact _rn intrinsics):
 //   circles          tests/resources/circles2D.h:141-151
 //   kinematic chain  demos/KinematicChain.h:209-276
-//   DH sphere arm    the arm definition shared with the oracle (no OMPL counterpart)
+//   DH sphere arm    no OMPL counterpart: standard DH forward kinematics, spheres evenly spaced along
+//                    each link, a pair collides when |c_robot - c_world|^2 < (r_robot + r_world)^2
+//                    (kernels.cuh: dh_valid64 fixes the operation order)
 //
 // FP32_GUARDED forms evaluate every comparison in FP32 together with a bound E on
 // |value_fp32 - value_fp64_reference| and classify it as definitely-true, definitely-false or

@@ -86,8 +86,9 @@ void launch_gather_rows(const LaunchCfg &lc, StatesView src, const int64_t *idx,
                         MutStatesView out);
 
 // ---------------------------------------------------------------- DH sphere arm
-// FP64 form: the arm definition (sphere centres in the exact operation order of the oracle's
-// definition), candidates from the uniform grid (a superset of every colliding sphere), exact test.
+// FP64 form: the arm definition (this operation order for the sphere centres is the definition the
+// test oracle restates), candidates from the uniform grid (a superset of every colliding sphere),
+// exact test.
 template <int MAXD>
 __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, const WorldArgs &wa)
 {
