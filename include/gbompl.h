@@ -245,6 +245,12 @@ gbo_status gbo_sincos32(const double *theta, int64_t n, float *cos_out, float *s
 gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
 /* Number of kernels this library launched since load (for launch accounting). */
 uint64_t gbo_launch_count(void);
+/* Self-test of the bounded device waits (no OMPL counterpart): a kernel waits limit_ns nanoseconds
+ * (at most 2 s) on a barrier that nothing completes, gives up, and reports it; returns GBO_ERR_TIMEOUT
+ * (the expected outcome) with *elapsed_ms the time the wait took. Every device wait of the library
+ * (world staging) is bounded the same way (one second) and reports GBO_ERR_TIMEOUT instead of hanging;
+ * the context stays usable. */
+gbo_status gbo_selftest_bounded_wait(int64_t limit_ns, double *elapsed_ms);
 
 #ifdef __cplusplus
 }

@@ -12,8 +12,11 @@
 
 #include <random>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "chain_state.cuh"
 #include "kernels_nn.cuh"
+#include "tma.cuh"
 
 using namespace gbo;
 
@@ -281,6 +284,16 @@ struct gbo_nn
             cudaFree(alive);
     }
 };
+
+namespace
+{
+// NVTX range over a C-ABI call (visible to ncu / Nsight; no cost without an attached tool)
+struct Trace
+{
+    explicit Trace(const char *name) { nvtxRangePushA(name); }
+    ~Trace() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace gbo
 {
@@ -557,6 +570,25 @@ const char *gbo_last_error(void)
 uint64_t gbo_launch_count(void)
 {
     return g_launches.load();
+}
+
+gbo_status gbo_selftest_bounded_wait(int64_t limit_ns, double *elapsed_ms)
+{
+    if (limit_ns <= 0 || limit_ns > 2000000000ll)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "wait limit must be in (0, 2 s]");
+    if (auto st = ensure_device())
+        return st;
+    unsigned long long *d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    launch_wait_probe((unsigned long long)limit_ns, d);
+    unsigned long long h[2] = {0, 0};
+    const cudaError_t e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return fail(GBO_ERR_CUDA, std::string("bounded-wait self-test: ") + cudaGetErrorString(e));
+    if (elapsed_ms)
+        *elapsed_ms = (double)h[1] * 1e-6;
+    return h[0] ? fail(GBO_ERR_TIMEOUT, "the probe's wait ran out, as intended") : GBO_OK;
 }
 
 gbo_status gbo_device_check(int *sm_count, int *cc_major, int *cc_minor)
@@ -982,6 +1014,7 @@ gbo_status gbo_checker_stats(const gbo_checker *c, uint64_t *evaluated, uint64_t
 gbo_status gbo_is_valid(gbo_checker *c, const double *states, int64_t n, int64_t ld, int layout, uint8_t *out,
                         gbo_stream stream)
 {
+    Trace trace("gbo_is_valid");
     if (!c || n < 0 || (n > 0 && (!states || !out)) || !valid_layout(layout, n, ld, c->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad isValid arguments");
     if (n == 0)
@@ -1007,6 +1040,7 @@ static gbo_status motion_impl(gbo_checker *c, const double *s1, const double *s2
 gbo_status gbo_check_motion(gbo_checker *c, const double *s1, const double *s2, int64_t n, int64_t ld, int layout,
                             int schedule, uint8_t *ok, int32_t *first_j, int32_t *nd, gbo_stream stream)
 {
+    Trace trace("gbo_check_motion");
     if (!c || n < 0 || (n > 0 && (!s1 || !s2 || !ok)) || !valid_layout(layout, n, ld, c->sp.dim) ||
         schedule < GBO_SCHEDULE_PLAIN || schedule > GBO_SCHEDULE_AUTO)
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad checkMotion arguments");
@@ -1106,6 +1140,7 @@ static void *mapped_host(const void *p)
 
 gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, uint8_t *out)
 {
+    Trace trace("gbo_is_valid_host");
     if (!c || n < 0 || (n > 0 && (!states || !out)))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad isValid arguments");
     if (n == 0)
@@ -1141,6 +1176,7 @@ gbo_status gbo_is_valid_host(gbo_checker *c, const double *states, int64_t n, ui
 gbo_status gbo_check_motion_host(gbo_checker *c, const double *s1, const double *s2, int64_t n, uint8_t *ok,
                                  double *last_t, double *last_state)
 {
+    Trace trace("gbo_check_motion_host");
     if (!c || n < 0 || (n > 0 && (!s1 || !s2 || !ok)))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad checkMotion arguments");
     if (n == 0)
@@ -1236,6 +1272,7 @@ static gbo_status sampler_words(gbo_sampler *s, int64_t n, gbo_stream stream, in
 
 gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream)
 {
+    Trace trace("gbo_sample_uniform");
     if (!s || n < 0 || (n > 0 && !out) || !valid_layout(layout, n, ld, s->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
     StatesView ov = make_view(out, ld, layout);
@@ -1272,6 +1309,7 @@ gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double di
 gbo_status gbo_sample_valid(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out, int64_t ld,
                             int layout, uint8_t *ok, gbo_stream stream)
 {
+    Trace trace("gbo_sample_valid");
     if (!s || !c || n < 0 || (n > 0 && (!out || !ok)) || !valid_layout(layout, n, ld, s->sp.dim) ||
         c->sp.dim != s->sp.dim)
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleValid arguments");
@@ -1500,6 +1538,7 @@ static gbo_status ensure_box_cells(gbo_nn *nn, const LaunchCfg &lc)
 gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
                             const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream)
 {
+    Trace trace("gbo_nn_nearest_k");
     if (!nn || nq < 0 || k < 1 || (nq > 0 && (!q || !idx)) || !valid_layout(layout, nq, ld, nn->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearestK arguments");
     if (k > 64)

@@ -80,6 +80,7 @@ bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const 
 void launch_distance(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, int64_t n, double *out);
 void launch_interpolate(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, const double *t,
                         int64_t n, MutStatesView out);
+void launch_wait_probe(unsigned long long limit_ns, unsigned long long *out);
 void launch_motion_states(const LaunchCfg &lc, const SpaceParams &sp, StatesView v1, StatesView v2, int64_t n,
                           unsigned count, int endpoints, MutStatesView out);
 void launch_gather_rows(const LaunchCfg &lc, StatesView src, const int64_t *idx, int64_t n, int dim,

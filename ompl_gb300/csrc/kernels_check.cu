@@ -846,6 +846,29 @@ void launch_gather_rows(const LaunchCfg &lc, StatesView src, const int64_t *idx,
     note_launch();
 }
 
+// Self-test of the bounded waits: a barrier nothing arrives at, waited on for limit_ns; out[0] = 1 when
+// the wait ran out, out[1] = the nanoseconds it took.
+__global__ void wait_probe_kernel(unsigned long long limit_ns, unsigned long long *out)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0)
+        mbar_init(&bar, 1);
+    __syncthreads();
+    const unsigned long long t0 = global_ns();
+    const bool ok = mbar_wait_bounded(&bar, 0, limit_ns);
+    if (threadIdx.x == 0)
+    {
+        out[0] = ok ? 0ull : 1ull;
+        out[1] = global_ns() - t0;
+    }
+}
+
+void launch_wait_probe(unsigned long long limit_ns, unsigned long long *out)
+{
+    wait_probe_kernel<<<1, 32>>>(limit_ns, out);
+    note_launch();
+}
+
 void launch_interpolate(const LaunchCfg &lc, const SpaceParams &sp, StatesView a, StatesView b, const double *t,
                         int64_t n, MutStatesView out)
 {

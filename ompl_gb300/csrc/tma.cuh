@@ -6,7 +6,14 @@
 namespace gbo
 {
 
-constexpr unsigned kWaitLimit = 1u << 26;  // try_wait polls (each may suspend ~ a microsecond)
+constexpr unsigned long long kWaitNs = 1000000000ull;  // a bounded wait gives up after one second
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
@@ -49,12 +56,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+// Wait for phase `parity` of the barrier for at most limit_ns nanoseconds (global timer): false when
+// the time ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned long long limit_ns = kWaitNs)
 {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+    const unsigned long long t0 = global_ns();
+    while (true)
+    {
         if (mbar_try_wait(bar, parity))
             return true;
-    return false;
+        if (global_ns() - t0 > limit_ns)
+            return false;
+    }
 }
 
 __device__ __forceinline__ unsigned dynamic_smem_bytes()

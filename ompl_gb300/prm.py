@@ -35,6 +35,33 @@ class Roadmap:
     checked_states: int          # states the ordered DiscreteMotionValidator evaluates
     timings_ms: dict
 
+    def adjacency_csr(self):
+        """Undirected adjacency of the milestones (PRM's boost::adjacency_list<undirectedS> lists an edge
+        at both ends, PRM.cpp:590-596): (offsets int64[M + 1], neighbours int64[2E]), neighbours of a
+        vertex ascending."""
+        m = int(self.milestones.shape[1])
+        src = self.edge_src.cpu().numpy().astype(np.int64)
+        dst = self.edge_dst.cpu().numpy().astype(np.int64)
+        a, b = np.concatenate([src, dst]), np.concatenate([dst, src])
+        order = np.lexsort((b, a))
+        a, b = a[order], b[order]
+        offsets = np.zeros(m + 1, dtype=np.int64)
+        np.add.at(offsets, a + 1, 1)
+        return np.cumsum(offsets), b
+
+    def save(self, path):
+        """Snapshot of the roadmap on the host: milestone states (one row each), their indices in the
+        sample stream and the CSR adjacency, as a numpy .npz archive (Roadmap.load reads it back)."""
+        offsets, neighbours = self.adjacency_csr()
+        np.savez(path, states=self.milestones.T.cpu().numpy(), sample_index=self.sample_index.cpu().numpy(),
+                 offsets=offsets, neighbours=neighbours, samples=np.int64(self.samples))
+
+    @staticmethod
+    def load(path):
+        """The arrays Roadmap.save wrote: dict(states, sample_index, offsets, neighbours, samples)."""
+        with np.load(path) as z:
+            return {k: z[k] for k in z.files}
+
 
 def construct_roadmap(space: B.StateSpace, checker: B.StateValidityChecker, sampler_seed: int, n_samples: int,
                       k: int = 10, schedule: int = capi.SCHEDULE_AUTO, stream=None) -> Roadmap:

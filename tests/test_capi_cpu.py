@@ -98,3 +98,12 @@ def test_device_calls_fail_cleanly_without_gpu(lib):
     w = np.zeros((1, 3))
     assert lib.gbo_checker_create(h, 1, w.ctypes.data_as(dp), 1, None, 0, 0, 0.0, C.byref(ck)) == capi.ERR_NO_DEVICE
     lib.gbo_space_destroy(h)
+
+
+def test_bounded_wait_selftest_rejects_bad_limits():
+    import ctypes as C
+    from ompl_gb300 import capi
+    lib = capi.lib()
+    el = C.c_double()
+    assert lib.gbo_selftest_bounded_wait(0, C.byref(el)) == capi.ERR_INVALID_ARGUMENT
+    assert lib.gbo_selftest_bounded_wait(3_000_000_000, C.byref(el)) == capi.ERR_INVALID_ARGUMENT
