@@ -174,6 +174,10 @@ gbo_status gbo_nn_nearest_r_count(gbo_nn *nn, const double *q, int64_t nq, int64
 gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
                                  const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream);
 gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks);
+/* FP32 metric error of the last FP32_GUARDED nearestK call (no OMPL counterpart): the largest
+ * |distance_fp32 - distance_fp64| over the candidates it re-checked in FP64, and the bound the guard band
+ * assumes for it (the re-check band is twice that bound). */
+gbo_status gbo_nn_error_stats(const gbo_nn *nn, float *max_abs_error, float *bound);
 
 /* nearestK exactly as gbo_nn_nearest_k, but the call allocates no device memory (no counterpart in
  * OMPL). For callers that cannot allocate once set up: work captured into CUDA graphs, real-time

@@ -417,7 +417,10 @@ class NearestNeighborsGPU:
     def stats(self):
         q, r, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
         check(lib().gbo_nn_stats(self._h, C.byref(q), C.byref(r), C.byref(f)))
-        return {"queries": q.value, "rechecked": r.value, "fallbacks": f.value}
+        e, b = C.c_float(), C.c_float()
+        check(lib().gbo_nn_error_stats(self._h, C.byref(e), C.byref(b)))
+        return {"queries": q.value, "rechecked": r.value, "fallbacks": f.value, "max_fp32_error": e.value,
+                "fp32_error_bound": b.value}
 
     def nearestK(self, queries, k, prefix=None, soa=False, want_dist=True, stream=None):
         t, n, ld, lay = _batch(queries, self.space.dim, soa)

@@ -85,6 +85,7 @@ SIGNATURES = {
     "gbo_sincos32": (C.c_int, [_P, _I64, _P, _P, _P]),
     "gbo_launch_count": (C.c_uint64, []),
     "gbo_selftest_bounded_wait": (C.c_int, [_I64, C.POINTER(C.c_double)]),
+    "gbo_nn_error_stats": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 }
 
 

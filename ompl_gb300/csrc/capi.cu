@@ -1645,6 +1645,23 @@ gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_
     return GBO_OK;
 }
 
+gbo_status gbo_nn_error_stats(const gbo_nn *nn, float *max_abs_error, float *bound)
+{
+    if (!nn)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "nn is NULL");
+    RunCounters h{};
+    CUDA_TRY(cudaMemcpy(&h, nn->ctr.dev + nn->ctr.last, sizeof(h), cudaMemcpyDeviceToHost));
+    if (max_abs_error)
+    {
+        float e;
+        std::memcpy(&e, &h.max_err_bits, sizeof(e));
+        *max_abs_error = e;
+    }
+    if (bound)
+        *bound = nn->eps32;
+    return GBO_OK;
+}
+
 gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks)
 {
     if (!nn)

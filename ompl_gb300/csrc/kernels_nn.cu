@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
         k64[j] = INT64_MAX;
     }
     int nc = 0;
+    float max_err = 0.f;
     for (int j = 0; j < K_KEEP; ++j)
     {
         if (ik[j] < 0 || !(j < k || dk[j] <= band))
@@ -389,6 +390,9 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
         double x[MAXD];
         load_point<MAXD>(nn.pts64, nn.cap, sp.dim, ik[j], x);
         double cd = distance64<MAXD>(sp, x, q64);
+        // measured FP32 metric error (the lists hold distances for the chain, squares otherwise)
+        const float d32 = KIND == GBO_SPACE_KINEMATIC_CHAIN ? dk[j] : sqrtf(dk[j]);
+        max_err = fmaxf(max_err, fabsf((float)(cd - (double)d32)));
         int64_t ck = ik[j];
 #pragma unroll
         for (int m = 0; m < K_KEEP; ++m)
@@ -404,6 +408,8 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
         ++nc;
     }
     atomicAdd(&ctr->rechecked, (unsigned long long)nc);
+    if (max_err > 0.f)
+        atomicMax(&ctr->max_err_bits, __float_as_uint(max_err));  // non-negative floats order as integers
     for (int j = 0; j < k; ++j)
     {
         const bool have = k64[j] != INT64_MAX;

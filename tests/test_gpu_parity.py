@@ -536,6 +536,8 @@ def test_knn_large_batch_vs_exact_scan(kind):
     def both(k, prefix=None):
         nn.setPrecision("fp32_guarded")
         i32, d32 = nn.nearestK(queries, k, prefix=prefix)
+        st = nn.stats()  # the measured FP32 metric error stays inside the bound the guard band assumes
+        assert 0.0 < st["max_fp32_error"] <= st["fp32_error_bound"], (kind, st)
         nn.setPrecision("fp64")
         i64, d64 = nn.nearestK(queries, k, prefix=prefix)
         assert np.array_equal(i32, i64), (kind, k)
