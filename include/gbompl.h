@@ -146,6 +146,15 @@ gbo_status gbo_sampler_destroy(gbo_sampler *s);
 gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream);
 gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double distance, int64_t n, int64_t ld,
                                    int layout, double *out, gbo_stream stream);
+/* StateSampler::sampleGaussian (src/ompl/base/StateSampler.h:96-100; RealVectorStateSpace.cpp:67-82,
+ * SO2StateSpace.cpp:58-62) for n states: row i of out drawn around row i of mean (same ld and layout)
+ * with standard deviation stddev per coordinate, clamped to the bounds (wrapped for SO2). The values
+ * come from RNG::gaussian (src/ompl/util/RandomNumbers.h:98-101, libstdc++'s polar method) and its
+ * cached second value carries across calls of s, as OMPL's does; log is rounded to nearest, so a pair
+ * whose log glibc rounds the other way differs in the last bits (the stream position never does).
+ * Device arrays; returns when done (the host reads each chunk's accepted-candidate count). */
+gbo_status gbo_sample_gaussian(gbo_sampler *s, const double *mean, double stddev, int64_t n, int64_t ld, int layout,
+                               double *out, gbo_stream stream);
 /* UniformValidStateSampler::sample (src/ompl/base/samplers/src/UniformValidStateSampler.cpp:46-57)
  * called n times: call i draws sampleUniform states from s until c reports one valid or `attempts`
  * were drawn (MAX_VALID_SAMPLE_ATTEMPTS = 100 in OMPL); row i of out = the state it ended on,
@@ -200,6 +209,7 @@ gbo_status gbo_nn_nearest_r_host(gbo_nn *nn, const double *q, double r, int64_t 
 /* Host-memory sampling (AoS rows; synchronous). */
 gbo_status gbo_sample_uniform_host(gbo_sampler *s, int64_t n, double *out);
 gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, double distance, int64_t n, double *out);
+gbo_status gbo_sample_gaussian_host(gbo_sampler *s, const double *mean, double stddev, int64_t n, double *out);
 gbo_status gbo_sample_valid_host(gbo_sampler *s, gbo_checker *c, int64_t n, unsigned attempts, double *out,
                                  uint8_t *ok);
 

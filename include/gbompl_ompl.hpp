@@ -237,9 +237,12 @@ public:
         throwIf(gbo_sample_uniform_near_host(s_, nr.data(), distance, 1, row.data()), "sampleUniformNear");
         ctx_->fromRow(row.data(), state);
     }
-    void sampleGaussian(ompl::base::State *, const ompl::base::State *, double) override
+    void sampleGaussian(ompl::base::State *state, const ompl::base::State *mean, double stdDev) override
     {
-        throw ompl::Exception("gbompl: sampleGaussian is not provided by the GPU sampler");
+        std::vector<double> mr(ctx_->dim()), row(ctx_->dim());
+        ctx_->toRow(mean, mr.data());
+        throwIf(gbo_sample_gaussian_host(s_, mr.data(), stdDev, 1, row.data()), "sampleGaussian");
+        ctx_->fromRow(row.data(), state);
     }
     /* n consecutive sampleUniform draws. */
     void sampleUniformBatch(std::vector<ompl::base::State *> &states)

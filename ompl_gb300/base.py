@@ -353,6 +353,13 @@ class StateSampler:
                                             _stream(stream)))
         return out if isinstance(near, torch.Tensor) else _host(out)
 
+    def sampleGaussian(self, mean, stddev, stream=None):
+        """StateSampler::sampleGaussian for each row of `mean` (RealVectorStateSpace.cpp:67-82,
+        SO2StateSpace.cpp:58-62); the cached second normal value carries across calls."""
+        t, n, ld, lay = _batch(mean, self.space.dim, False)
+        out = torch.empty_like(t)
+        check(lib().gbo_sample_gaussian(self._h, _ptr(t), float(stddev), n, ld, lay, _ptr(out), _stream(stream)))
+        return out if isinstance(mean, torch.Tensor) else _host(out)
 
     def sampleValid(self, checker, n, attempts=100, stream=None, host=True):
         """UniformValidStateSampler::sample called n times on this sampler's stream: (states, ok)."""

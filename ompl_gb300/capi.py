@@ -54,6 +54,7 @@ SIGNATURES = {
     "gbo_sampler_destroy": (C.c_int, [_P]),
     "gbo_sample_uniform": (C.c_int, [_P, _I64, _P, _I64, C.c_int, _P]),
     "gbo_sample_uniform_near": (C.c_int, [_P, _P, C.c_double, _I64, _I64, C.c_int, _P, _P]),
+    "gbo_sample_gaussian": (C.c_int, [_P, _P, C.c_double, _I64, _I64, C.c_int, _P, _P]),
     "gbo_sample_valid": (C.c_int, [_P, _P, _I64, C.c_uint, _P, _I64, C.c_int, _P, _P]),
     "gbo_sample_valid_host": (C.c_int, [_P, _P, _I64, C.c_uint, _P, _P]),
     "gbo_nn_create": (C.c_int, [_P, _I64, C.POINTER(_P)]),
@@ -74,6 +75,7 @@ SIGNATURES = {
     "gbo_nn_nearest_r_host": (C.c_int, [_P, _P, C.c_double, _I64, C.POINTER(_I64), _P, _P]),
     "gbo_sample_uniform_host": (C.c_int, [_P, _I64, _P]),
     "gbo_sample_uniform_near_host": (C.c_int, [_P, _P, C.c_double, _I64, _P]),
+    "gbo_sample_gaussian_host": (C.c_int, [_P, _P, C.c_double, _I64, _P]),
     "gbo_server_create": (C.c_int, [C.c_int, _I64, C.POINTER(_P)]),
     "gbo_server_destroy": (C.c_int, [_P]),
     "gbo_server_submit": (C.c_int, [_P, _P, C.POINTER(C.c_uint64)]),

@@ -235,6 +235,8 @@ struct gbo_sampler
     cudaStream_t host_stream = nullptr;
     Pinned pin;
     DevBuf dev, words;  // words: the word-stream scratch of the device calls
+    DevBuf gwork;       // GaussChunk + per-CTA counts of sampleGaussian
+    bool has_saved = false;  // mirrors SamplerState::has_saved (a cached Gaussian value is pending)
     ~gbo_sampler()
     {
         if (host_stream)
@@ -1300,6 +1302,39 @@ gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double di
     return GBO_OK;
 }
 
+// StateSampler::sampleGaussian (StateSampler.h:96-100) for n states, state i drawn around mean row i
+// (mean and out share ld and layout). Returns after the call's stream work: the number of candidate
+// draws is data dependent and the host reads each chunk's progress.
+gbo_status gbo_sample_gaussian(gbo_sampler *s, const double *mean, double stddev, int64_t n, int64_t ld, int layout,
+                               double *out, gbo_stream stream)
+{
+    Trace trace("gbo_sample_gaussian");
+    if (!s || n < 0 || (n > 0 && (!out || !mean)) || !valid_layout(layout, n, ld, s->sp.dim))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleGaussian arguments");
+    const int64_t M = n * s->sp.dim;
+    if (M == 0)
+        return GBO_OK;
+    // raw words for the expected candidates plus a margin and one whole block (capped; larger calls
+    // run in several chunks)
+    const double mu = (double)((M + 1) / 2) / 0.7853981633974483;
+    const int64_t cap = std::min<int64_t>(((int64_t)1 << 24) + 628,
+                                          4 * (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0) + 628);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (auto e = s->words.reserve((size_t)cap * sizeof(unsigned), st))
+        return e;
+    if (auto e = s->gwork.reserve(sizeof(GaussChunk) + sizeof(long long) * (size_t)(cap / 4096 + 2), st))
+        return e;
+    const StatesView ov = make_view(out, ld, layout);
+    const int64_t chunks = launch_sample_gaussian(
+        lcfg(st), s->st, s->has_saved, s->sp, make_view(mean, ld, layout), stddev, n, MutStatesView{out, ov.si, ov.sd},
+        (unsigned *)s->words.p, cap, (GaussChunk *)s->gwork.p, (long long *)((char *)s->gwork.p + sizeof(GaussChunk)));
+    if (chunks < 0)
+        return fail(GBO_ERR_CUDA, std::string("sampleGaussian: ") + cudaGetErrorString(cudaGetLastError()));
+    CHECK_LAUNCH();
+    s->has_saved = ((M - (s->has_saved ? 1 : 0)) & 1) != 0;
+    return GBO_OK;
+}
+
 // UniformValidStateSampler::sample, n calls. A call draws until a valid state or `attempts` draws;
 // the stream must end where OMPL's would, so no draw is made that no call consumes. Each round draws
 // one state per unresolved call (every such call consumes at least one more), checks them, and walks
@@ -1826,6 +1861,27 @@ gbo_status gbo_sample_uniform_near_host(gbo_sampler *s, const double *near, doub
     std::memcpy(s->pin.p, near, b);
     CUDA_TRY(cudaMemcpyAsync(dn, s->pin.p, b, cudaMemcpyHostToDevice, s->host_stream));
     if (auto st = gbo_sample_uniform_near(s, dn, distance, n, s->sp.dim, GBO_LAYOUT_AOS, dout, s->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(s->pin.p, dout, b, cudaMemcpyDeviceToHost, s->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(s->host_stream));
+    std::memcpy(out, s->pin.p, b);
+    return GBO_OK;
+}
+
+gbo_status gbo_sample_gaussian_host(gbo_sampler *s, const double *mean, double stddev, int64_t n, double *out)
+{
+    if (!s || n < 0 || (n > 0 && (!out || !mean)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleGaussian arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const size_t b = (size_t)n * s->sp.dim * sizeof(double);
+    if (auto st = s->dev.reserve(2 * b + 32, s->host_stream))
+        return st;
+    if (auto st = s->pin.reserve(b + 16))
+        return st;
+    double *dm = (double *)s->dev.p, *dout = (double *)((char *)s->dev.p + pad16(b));
+    std::memcpy(s->pin.p, mean, b);
+    CUDA_TRY(cudaMemcpyAsync(dm, s->pin.p, b, cudaMemcpyHostToDevice, s->host_stream));
+    if (auto st = gbo_sample_gaussian(s, dm, stddev, n, s->sp.dim, GBO_LAYOUT_AOS, dout, s->host_stream))
         return st;
     CUDA_TRY(cudaMemcpyAsync(s->pin.p, dout, b, cudaMemcpyDeviceToHost, s->host_stream));
     CUDA_TRY(cudaStreamSynchronize(s->host_stream));

@@ -59,13 +59,27 @@ void launch_radius(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp,
 struct SamplerState
 {
     unsigned int mt[624];
-    unsigned int pos;     // next word index in mt (624 = twist needed)
-    unsigned int pad[3];
+    unsigned int pos;        // next word index in mt (624 = twist needed)
+    unsigned int has_saved;  // normal_distribution's cached second value of the last polar pair
+    double saved;
+};
+// Progress of one chunk of a Gaussian sampling call (device memory, read back by the host)
+struct GaussChunk
+{
+    long long accepted;  // accepted candidates of the chunk
+    long long consumed;  // stream words used: through the last needed accepted candidate, else all
 };
 // words: scratch of cap_words (even, >= 2) 32-bit words; calls above cap_words / 2 values run in chunks
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
                            StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *words,
                            int64_t cap_words);
+// sampleGaussian values [v_first, M) of a call; st->has_saved says whether value 0 is the cached one.
+// One chunk of at most cap_words / 4 - 156 polar candidates per host round trip; returns the chunks run
+// or -1 on an error. words: scratch of cap_words words; ctl: device GaussChunk; cnt: scratch of
+// (cap_words / 4096 + 2) long longs.
+int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
+                               StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt);
 double measure_fp32_peak(const LaunchCfg &lc);
 double measure_fp64_peak(const LaunchCfg &lc);
 void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s);

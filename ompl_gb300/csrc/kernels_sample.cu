@@ -8,7 +8,9 @@
 // sampler's word stream (mt_words_kernel) and the whole GPU converts word pairs into coordinates
 // (words_to_states_kernel); large calls alternate the two over chunks of the stream.
 #include <algorithm>
+#include <cmath>
 
+#include "crlog.cuh"
 #include "kernels_nn.cuh"
 
 namespace gbo
@@ -43,6 +45,10 @@ __device__ __forceinline__ double canonical53(unsigned w0, unsigned w1)
 // out, then saves the generator. A block's regeneration runs in the three dependency-free chunks
 // [0,227), [227,454), [454,623) and word 623 into a second buffer (4 barriers per block), and each
 // word is tempered and stored as soon as its chunk produces it.
+// kRaw (speculative draws): the words are stored untempered, every new block is stored whole (up to
+// W + 623 words) and the generator is left unchanged, so that any prefix of the stream can later be
+// committed by copying the block that holds its last word (gauss_advance_kernel).
+template <bool kRaw>
 __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t W, unsigned *out)
 {
     __shared__ unsigned buf[2][624];
@@ -54,18 +60,18 @@ __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t
     __syncthreads();
     int64_t w = min((int64_t)(624 - pos), W);  // the rest of the current block
     for (int i = t; i < (int)w; i += blockDim.x)
-        out[i] = temper(cur[pos + i]);
+        out[i] = kRaw ? cur[pos + i] : temper(cur[pos + i]);
     pos += (int)w;
     while (w < W)
     {
-        const int m = (int)min((int64_t)624, W - w);  // words of the new block that are used
+        const int m = kRaw ? 624 : (int)min((int64_t)624, W - w);  // words of the new block that are stored
         unsigned *o = out + w;
         if (t < 227)
         {
             const unsigned v = twist_word(cur[t], cur[t + 1], cur[t + 397]);
             nxt[t] = v;
             if (t < m)
-                o[t] = temper(v);
+                o[t] = kRaw ? v : temper(v);
         }
         __syncthreads();
         if (t < 227)
@@ -73,7 +79,7 @@ __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t
             const unsigned v = twist_word(cur[t + 227], cur[t + 228], nxt[t]);
             nxt[t + 227] = v;
             if (t + 227 < m)
-                o[t + 227] = temper(v);
+                o[t + 227] = kRaw ? v : temper(v);
         }
         __syncthreads();
         if (t < 169)
@@ -81,7 +87,7 @@ __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t
             const unsigned v = twist_word(cur[t + 454], cur[t + 455], nxt[t + 227]);
             nxt[t + 454] = v;
             if (t + 454 < m)
-                o[t + 454] = temper(v);
+                o[t + 454] = kRaw ? v : temper(v);
         }
         __syncthreads();
         if (t == 0)
@@ -89,7 +95,7 @@ __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t
             const unsigned v = twist_word(cur[623], nxt[0], nxt[396]);
             nxt[623] = v;
             if (623 < m)
-                o[623] = temper(v);
+                o[623] = kRaw ? v : temper(v);
         }
         __syncthreads();
         unsigned *tmp = cur;
@@ -98,6 +104,8 @@ __global__ void __launch_bounds__(256) mt_words_kernel(SamplerState *st, int64_t
         w += m;
         pos = m;
     }
+    if (kRaw)
+        return;
     for (int i = t; i < 624; i += blockDim.x)
         st->mt[i] = cur[i];
     if (t == 0)
@@ -160,12 +168,277 @@ void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpacePar
     for (int64_t v0 = 0; v0 < total; v0 += chunk)
     {
         const int64_t nv = std::min(chunk, total - v0);
-        mt_words_kernel<<<1, 256, 0, lc.stream>>>(st, 2 * nv, words);
+        mt_words_kernel<false><<<1, 256, 0, lc.stream>>>(st, 2 * nv, words);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t)lc.sm_count * 8));
         words_to_states_kernel<<<grid, 256, 0, lc.stream>>>(words, v0, nv, sp, nearv, near != nullptr, distance, out);
         note_launch();
         note_launch();
     }
+}
+
+// ---------------------------------------------------------------- sampleGaussian
+// RealVectorStateSampler::sampleGaussian (RealVectorStateSpace.cpp:67-82: per coordinate
+// rng_.gaussian(mean, stdDev) clamped to the bounds) and SO2StateSampler::sampleGaussian
+// (SO2StateSpace.cpp:58-62: wrapped by enforceBounds). RNG::gaussian (RandomNumbers.h:98-101) is
+// libstdc++'s normal_distribution, the polar method of Marsaglia and Bray (1964) with a cached pair:
+// a candidate takes two uniform01 draws (4 stream words), x = 2U - 1, y = 2V - 1, r2 = x^2 + y^2, and is
+// rejected while r2 > 1 or r2 == 0; an accepted one gives mult = sqrt(-2 log(r2) / r2) and the values
+// y * mult (returned) then x * mult (cached for the next draw of the same RNG, across calls).
+// Every operation is the same IEEE double operation except log, which is log_cr (crlog.cuh, rounded
+// to nearest); glibc's log differs from the correctly rounded value in the last bit for a small
+// fraction of arguments, and only the values of those pairs differ (by an ulp or two).
+//
+// Stream consumption is data dependent, so a chunk draws a bounded surplus of candidates
+// speculatively (raw words, generator unchanged), ranks the accepted ones across the GPU, converts
+// the ones the call needs and then commits exactly the words used (gauss_advance_kernel).
+constexpr int kGaussPerCta = 1024;  // candidates per CTA: 256 threads x 4
+
+__device__ __forceinline__ bool polar_candidate(uint4 w, double &x, double &y, double &r2)
+{
+    x = __dsub_rn(__dmul_rn(2.0, canonical53(temper(w.x), temper(w.y))), 1.0);
+    y = __dsub_rn(__dmul_rn(2.0, canonical53(temper(w.z), temper(w.w))), 1.0);
+    r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+    return !(r2 > 1.0 || r2 == 0.0);
+}
+
+// Value v of the call (coordinate v % dim of state v / dim) from a standard normal value g:
+// normal_distribution's g * 1 + 0 (which turns -0 into +0), then * stdDev + mean and the bounds.
+__device__ __forceinline__ void gauss_emit(const SpaceParams &sp, StatesView mean, double stddev, MutStatesView out,
+                                           int64_t v, double g)
+{
+    const int64_t i = v / sp.dim;
+    const int d = (int)(v - i * sp.dim);
+    double z = __dadd_rn(__dmul_rn(__dadd_rn(g, 0.0), stddev), mean(i, d));
+    if (sp.kind == GBO_SPACE_SO2)
+    {
+        // SO2StateSpace::enforceBounds (SO2StateSpace.cpp:79-87)
+        double r = fmod(z, 2.0 * kPi);
+        if (r < -kPi)
+            r = __dadd_rn(r, 2.0 * kPi);
+        else if (r >= kPi)
+            r = __dsub_rn(r, 2.0 * kPi);
+        z = r;
+    }
+    else if (z < sp.low[d])
+        z = sp.low[d];
+    else if (z > sp.high[d])
+        z = sp.high[d];
+    out(i, d) = z;
+}
+
+// Value 0 of a call from the cached value of the previous call.
+__global__ void gauss_saved_kernel(SamplerState *st, SpaceParams sp, StatesView mean, double stddev, MutStatesView out)
+{
+    if (threadIdx.x == 0)
+    {
+        gauss_emit(sp, mean, stddev, out, 0, st->saved);
+        st->has_saved = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) gauss_count_kernel(const uint4 *cand, int64_t G, long long *cnt)
+{
+    const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
+    int c = 0;
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r)
+    {
+        const int64_t k = base + r * 256 + threadIdx.x;
+        bool a = false;
+        if (k < G)
+        {
+            double x, y, r2;
+            a = polar_candidate(cand[k], x, y, r2);
+        }
+        c += __syncthreads_count(a);
+    }
+    if (threadIdx.x == 0)
+        cnt[blockIdx.x] = c;
+}
+
+// Exclusive scan of the per-CTA counts in place (one CTA of 1024 threads); the total goes to ctl.
+__global__ void __launch_bounds__(1024) gauss_scan_kernel(long long *cnt, int nb, GaussChunk *ctl)
+{
+    __shared__ long long part[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long run = 0;
+    for (int b0 = 0; b0 < nb; b0 += 1024)
+    {
+        const int b = b0 + (int)threadIdx.x;
+        const long long v = b < nb ? cnt[b] : 0;
+        long long x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o)
+                x += y;
+        }
+        if (lane == 31)
+            part[warp] = x;
+        __syncthreads();
+        if (warp == 0)
+        {
+            long long p = part[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const long long y = __shfl_up_sync(0xffffffffu, p, o);
+                if (lane >= o)
+                    p += y;
+            }
+            part[lane] = p;
+        }
+        __syncthreads();
+        if (b < nb)
+            cnt[b] = run + (warp ? part[warp - 1] : 0) + x - v;
+        run += part[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        ctl->accepted = run;
+        ctl->consumed = -1;
+    }
+}
+
+struct GaussArgs
+{
+    const uint4 *cand;      // candidate k = raw words 4k .. 4k+3
+    int64_t G;              // candidates of the chunk
+    const long long *off;   // accepted candidates before each CTA
+    int64_t need;           // pairs the call still needs
+    int64_t v0;             // value index of the chunk's first pair
+    int64_t M;              // values of the call
+    double stddev;
+    SpaceParams sp;
+    StatesView mean;
+    MutStatesView out;
+    SamplerState *st;
+    GaussChunk *ctl;
+};
+
+// Accepted candidate j of the chunk (in stream order) becomes pair j: values v0 + 2j and v0 + 2j + 1.
+__global__ void __launch_bounds__(256) gauss_values_kernel(const __grid_constant__ GaussArgs a)
+{
+    __shared__ int wcnt[4][8];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
+    unsigned bal[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+    {
+        const int64_t k = base + r * 256 + t;
+        bool acc = false;
+        if (k < a.G)
+        {
+            double x, y, r2;
+            acc = polar_candidate(a.cand[k], x, y, r2);
+        }
+        bal[r] = __ballot_sync(0xffffffffu, acc);
+        if (lane == 0)
+            wcnt[r][warp] = __popc(bal[r]);
+    }
+    __syncthreads();
+    long long rank = a.off[blockIdx.x];
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r)
+    {
+        int before = 0, all = 0;
+        for (int w = 0; w < 8; ++w)
+        {
+            before += w < warp ? wcnt[r][w] : 0;
+            all += wcnt[r][w];
+        }
+        const bool acc = (bal[r] >> lane) & 1u;
+        const long long j = rank + before + __popc(bal[r] & ((1u << lane) - 1u));
+        rank += all;
+        if (!acc || j >= a.need)
+            continue;
+        const int64_t k = base + r * 256 + t;
+        double x, y, r2;
+        polar_candidate(a.cand[k], x, y, r2);
+        const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log_cr(r2)), r2));
+        const double g1 = __dmul_rn(y, mult), g2 = __dmul_rn(x, mult);
+        const int64_t v = a.v0 + 2 * j;
+        gauss_emit(a.sp, a.mean, a.stddev, a.out, v, g1);
+        if (v + 1 < a.M)
+            gauss_emit(a.sp, a.mean, a.stddev, a.out, v + 1, g2);
+        else
+        {
+            a.st->saved = g2;
+            a.st->has_saved = 1;
+        }
+        if (j == a.need - 1)
+            a.ctl->consumed = 4 * (k + 1);
+    }
+}
+
+// Commits the words the chunk used: K = ctl->consumed (or all W words when the chunk fell short).
+// raw holds the rest of the generator's current block (r = 624 - pos words) and then whole blocks,
+// untempered, so the generator after word K is the block holding word K - 1.
+__global__ void __launch_bounds__(256) gauss_advance_kernel(SamplerState *st, const unsigned *raw, int64_t W,
+                                                            const GaussChunk *ctl)
+{
+    const long long c = ctl->consumed;
+    const int64_t K = c >= 0 ? c : W;
+    const int64_t r = 624 - (int64_t)st->pos;
+    __syncthreads();  // every thread has read pos
+    if (K <= r)
+    {
+        if (threadIdx.x == 0)
+            st->pos = (unsigned)(624 - r + K);
+        return;
+    }
+    const int64_t start = r + 624 * ((K - r - 1) / 624);
+    for (int i = threadIdx.x; i < 624; i += blockDim.x)
+        st->mt[i] = raw[start + i];
+    if (threadIdx.x == 0)
+        st->pos = (unsigned)(K - start);
+}
+
+int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
+                               StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt)
+{
+    const int64_t M = n * sp.dim;
+    if (M == 0)
+        return 0;
+    int64_t v = 0;
+    if (has_saved)
+    {
+        gauss_saved_kernel<<<1, 32, 0, lc.stream>>>(st, sp, meanv, stddev, out);
+        note_launch();
+        v = 1;
+    }
+    int64_t need = (M - v + 1) / 2, chunks = 0;
+    const int64_t gmax = (cap_words - 624) / 4;
+    while (need > 0)
+    {
+        // acceptance pi/4: the expected count plus 8 standard deviations of the candidates needed
+        const double mu = (double)need / 0.7853981633974483;
+        const int64_t G = std::max<int64_t>(1, std::min<int64_t>(gmax, (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0)));
+        const int nb = (int)((G + kGaussPerCta - 1) / kGaussPerCta);
+        mt_words_kernel<true><<<1, 256, 0, lc.stream>>>(st, 4 * G, words);
+        gauss_count_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt);
+        gauss_scan_kernel<<<1, 1024, 0, lc.stream>>>(cnt, nb, ctl);
+        GaussArgs a{(const uint4 *)words, G, cnt, need, v, M, stddev, sp, meanv, out, st, ctl};
+        gauss_values_kernel<<<nb, 256, 0, lc.stream>>>(a);
+        gauss_advance_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
+        for (int i = 0; i < 5; ++i)
+            note_launch();
+        GaussChunk h{};
+        if (cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, lc.stream) != cudaSuccess ||
+            cudaStreamSynchronize(lc.stream) != cudaSuccess)
+            return -1;
+        const int64_t got = std::min<int64_t>(h.accepted, need);
+        if (got <= 0)  // >= 64 candidates without one accepted: the stream is broken, not unlucky
+            return -1;
+        v += 2 * got;
+        need -= got;
+        ++chunks;
+    }
+    return chunks;
 }
 
 // FP32 FMA throughput probe: independent FMA chains, no memory traffic in the loop.

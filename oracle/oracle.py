@@ -183,6 +183,24 @@ class Oracle:
                                          C.c_long(near.shape[0]), _dp(out))
         return out
 
+    def sample_script(self, sp, seed, ops, mean=None, stddev=0.0, log_mode=0):
+        """ops: list of ("uniform" | "gaussian", count); gaussian calls take the next rows of mean."""
+        kinds = np.array([1 if k == "gaussian" else 0 for k, _ in ops], dtype=np.int32)
+        counts = np.array([c for _, c in ops], dtype=np.int64)
+        mean = np.zeros((1, sp.dim)) if mean is None else _rows(mean, sp.dim)
+        out = np.empty((int(counts.sum()), sp.dim))
+        s = sp.c()
+        self.lib.ora_sample_script(C.byref(s), C.c_uint(seed), kinds.ctypes.data_as(C.POINTER(C.c_int)),
+                                   counts.ctypes.data_as(C.POINTER(C.c_long)), C.c_int(len(ops)), _dp(mean),
+                                   C.c_double(stddev), C.c_int(log_mode), _dp(out))
+        return out
+
+    def log_rn(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty_like(x)
+        self.lib.ora_log_rn(_dp(x), C.c_long(x.size), _dp(out))
+        return out
+
     def is_valid(self, sp, ck, states):
         st = _rows(states, sp.dim)
         out = np.empty(st.shape[0], dtype=np.uint8)

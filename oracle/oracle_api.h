@@ -87,6 +87,15 @@ void ora_sample_uniform(const ora_space *s, unsigned seed, long n, double *out);
 /* sampleUniformNear(out_i, near_i, distance) for i = 0..n-1 from one sampler. */
 void ora_sample_uniform_near(const ora_space *s, unsigned seed, const double *near, double distance, long n,
                              double *out);
+/* One sampler (RNG seeded with setLocalSeed(seed)) running a script of calls: call k draws counts[k]
+ * states with sampleUniform (kinds[k] = 0) or with sampleGaussian around the next counts[k] rows of
+ * mean, standard deviation stddev (kinds[k] = 1); out receives every drawn row in order.
+ * log_mode (restatement only; the reference build takes 0): 0 = std::normal_distribution, as OMPL;
+ * 1 = the same polar method with the log rounded to nearest (ora_log_rn). */
+void ora_sample_script(const ora_space *s, unsigned seed, const int *kinds, const long *counts, int nops,
+                       const double *mean, double stddev, int log_mode, double *out);
+/* Natural log rounded to nearest (double-double evaluation) of positive normal doubles. */
+void ora_log_rn(const double *x, long n, double *out);
 /* Raw RNG draws: uniform01 (kind 0) or uniformReal(lo, hi) (kind 1), n values from RNG(seed). */
 void ora_rng_uniform(unsigned seed, int kind, double lo, double hi, long n, double *out);
 

@@ -522,6 +522,171 @@ void ora_sample_uniform_near(const ora_space *d, unsigned seed, const double *ne
     }
 }
 
+// Natural log rounded to nearest, evaluated in double-double: x = 2^e m, m in [sqrt(1/2), sqrt(2)),
+// s = (m - 1)/(m + 1), log m = 2 (s + s^3/3 + s^5/5 + ...) up to s^41/41 (terms from s^21 on in plain
+// FP64), log x = e ln2 + log m; ln 2 and 1/(2k+1) split exactly into two doubles. Two-sum (Knuth) and
+// fma two-product give the double-double operations.
+namespace
+{
+struct DD
+{
+    double hi, lo;
+};
+DD two_sum(double a, double b)
+{
+    const double s = a + b, bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+DD fast_two_sum(double a, double b)
+{
+    const double s = a + b;
+    return {s, b - (s - a)};
+}
+DD dd_add(DD a, DD b)
+{
+    DD s = two_sum(a.hi, b.hi);
+    const DD t = two_sum(a.lo, b.lo);
+    s.lo += t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+DD dd_mul(DD a, DD b)
+{
+    const double p = a.hi * b.hi;
+    double e = std::fma(a.hi, b.hi, -p);
+    e = std::fma(a.hi, b.lo, e);
+    e = std::fma(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+DD dd_div(double a, DD b)
+{
+    const double q1 = a / b.hi;
+    const DD p1 = dd_mul({q1, 0.0}, b);
+    DD r = two_sum(a, -p1.hi);
+    r.lo -= p1.lo;
+    const double q2 = (r.hi + r.lo) / b.hi;
+    const DD p2 = dd_mul({q2, 0.0}, b);
+    const DD r2 = dd_add(r, {-p2.hi, -p2.lo});
+    const double q3 = (r2.hi + r2.lo) / b.hi;
+    return dd_add(fast_two_sum(q1, q2), {q3, 0.0});
+}
+double log_rn(double x)
+{
+    static const double kHi[21] = {0.0, 0x1.5555555555555p-2, 0x1.999999999999ap-3, 0x1.2492492492492p-3,
+                                   0x1.c71c71c71c71cp-4, 0x1.745d1745d1746p-4, 0x1.3b13b13b13b14p-4,
+                                   0x1.1111111111111p-4, 0x1.e1e1e1e1e1e1ep-5, 0x1.af286bca1af28p-5,
+                                   0x1.8618618618618p-5, 0x1.642c8590b2164p-5, 0x1.47ae147ae147bp-5,
+                                   0x1.2f684bda12f68p-5, 0x1.1a7b9611a7b96p-5, 0x1.0842108421084p-5,
+                                   0x1.f07c1f07c1f08p-6, 0x1.d41d41d41d41dp-6, 0x1.bacf914c1bad0p-6,
+                                   0x1.a41a41a41a41ap-6, 0x1.8f9c18f9c18fap-6};
+    static const double kLo[10] = {0.0, 0x1.5555555555555p-56, -0x1.999999999999ap-57, 0x1.2492492492492p-57,
+                                   0x1.c71c71c71c71cp-58, -0x1.745d1745d1746p-59, -0x1.3b13b13b13b14p-58,
+                                   0x1.1111111111111p-60, 0x1.e1e1e1e1e1e1ep-61, 0x1.af286bca1af28p-59};
+    int e = 0;
+    double m = std::frexp(x, &e);
+    if (m < 0x1.6a09e667f3bcdp-1)
+    {
+        m *= 2.0;
+        --e;
+    }
+    const DD s = dd_div(m - 1.0, two_sum(m, 1.0));
+    const DD z = dd_mul(s, s);
+    double q = kHi[20];
+    for (int k = 19; k >= 10; --k)
+        q = std::fma(q, z.hi, kHi[k]);
+    DD P{q, 0.0};
+    for (int k = 9; k >= 1; --k)
+        P = dd_add({kHi[k], kLo[k]}, dd_mul(z, P));
+    DD lm = dd_add(s, dd_mul(dd_mul(s, z), P));
+    lm.hi *= 2.0;
+    lm.lo *= 2.0;
+    return dd_add(dd_mul({(double)e, 0.0}, {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56}), lm).hi;
+}
+
+// RNG:98-101 (gaussian = normalDist_(generator_) * stddev + mean) with log_mode 1: libstdc++'s
+// normal_distribution restated (polar method of Marsaglia and Bray, cached second value), log
+// replaced by log_rn. log_mode 0 uses std::normal_distribution itself, as OMPL.
+struct Gaussian
+{
+    int log_mode = 0;
+    std::normal_distribution<> nd{0, 1};
+    bool saved_available = false;
+    double saved = 0.0;
+    double operator()(std::mt19937 &gen, std::uniform_real_distribution<> &uni)
+    {
+        if (log_mode == 0)
+            return nd(gen);
+        double ret;
+        if (saved_available)
+        {
+            saved_available = false;
+            ret = saved;
+        }
+        else
+        {
+            double x, y, r2;
+            do
+            {
+                x = 2.0 * uni(gen) - 1.0;
+                y = 2.0 * uni(gen) - 1.0;
+                r2 = x * x + y * y;
+            } while (r2 > 1.0 || r2 == 0.0);
+            const double mult = std::sqrt(-2.0 * log_rn(r2) / r2);
+            saved = x * mult;
+            saved_available = true;
+            ret = y * mult;
+        }
+        return ret * 1.0 + 0.0;
+    }
+};
+}  // namespace
+
+void ora_log_rn(const double *x, long n, double *out)
+{
+    for (long i = 0; i < n; ++i)
+        out[i] = log_rn(x[i]);
+}
+
+// RV:67-82 (clamped to the bounds) and SO2:58-62 (wrapped by enforceBounds), interleaved with
+// sampleUniform calls (RV:45-53, SO2:46-49) on one RNG.
+void ora_sample_script(const ora_space *d, unsigned seed, const int *kinds, const long *counts, int nops,
+                       const double *mean, double stddev, int log_mode, double *out)
+{
+    Space s = make_space(d);
+    std::mt19937 gen(seed);
+    std::uniform_real_distribution<> uni{0, 1};
+    Gaussian gauss;
+    gauss.log_mode = log_mode;
+    long rows = 0, mrows = 0;
+    for (int k = 0; k < nops; ++k)
+        for (long i = 0; i < counts[k]; ++i)
+        {
+            double *o = out + (size_t)(rows++) * s.dim;
+            if (kinds[k] != 1)
+            {
+                for (int j = 0; j < s.dim; ++j)
+                    o[j] = (s.high[j] - s.low[j]) * uni(gen) + s.low[j];
+                continue;
+            }
+            const double *m = mean + (size_t)(mrows++) * s.dim;
+            for (int j = 0; j < s.dim; ++j)
+            {
+                double v = gauss(gen, uni) * stddev + m[j];
+                if (s.kind != ORA_SPACE_SO2)
+                {
+                    if (v < s.low[j])
+                        v = s.low[j];
+                    else if (v > s.high[j])
+                        v = s.high[j];
+                }
+                o[j] = v;
+            }
+            if (s.kind == ORA_SPACE_SO2)
+                enforce_bounds(s, o);
+        }
+}
+
 void ora_is_valid(const ora_space *d, const ora_checker *c, const double *states, long n, unsigned char *out)
 {
     Space s = make_space(d);

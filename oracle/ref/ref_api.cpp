@@ -377,6 +377,41 @@ void ora_sample_uniform_near(const ora_space *d, unsigned seed, const double *ne
     }
 }
 
+void ora_sample_script(const ora_space *d, unsigned seed, const int *kinds, const long *counts, int nops,
+                       const double *mean, double stddev, int log_mode, double *out)
+{
+    (void)log_mode;  // OMPL's own RNG::gaussian only
+    auto B = build(d, nullptr);
+    auto smp = seeded_sampler(*B, d->kind, seed);
+    StateRows O(*B, nullptr, 1);
+    long rows = 0, mrows = 0;
+    for (int k = 0; k < nops; ++k)
+    {
+        if (kinds[k] == 1)
+        {
+            StateRows M(*B, mean + (size_t)mrows * B->dim, counts[k]);
+            for (long i = 0; i < counts[k]; ++i)
+            {
+                smp->sampleGaussian(O.v[0], M.v[i], stddev);
+                to_row(*B, O.v[0], out + (size_t)(rows++) * B->dim);
+            }
+            mrows += counts[k];
+        }
+        else
+            for (long i = 0; i < counts[k]; ++i)
+            {
+                smp->sampleUniform(O.v[0]);
+                to_row(*B, O.v[0], out + (size_t)(rows++) * B->dim);
+            }
+    }
+}
+
+void ora_log_rn(const double *x, long n, double *out)
+{
+    for (long i = 0; i < n; ++i)
+        out[i] = std::log(x[i]);  // the reference build has no rounded-to-nearest log; glibc's
+}
+
 void ora_is_valid(const ora_space *d, const ora_checker *c, const double *states, long n, unsigned char *out)
 {
     auto B = build(d, c);

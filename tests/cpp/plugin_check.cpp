@@ -7,7 +7,9 @@
 #include <ompl/base/spaces/RealVectorStateSpace.h>
 #include <ompl/datastructures/NearestNeighborsLinear.h>
 
+#include <cmath>
 #include <cstdio>
+#include <limits>
 #include <random>
 
 #include "gbompl_ompl.hpp"
@@ -129,6 +131,34 @@ int main()
     gvs.sampleBatch(batch, bok);
     for (size_t i = 0; i < batch.size(); ++i)
         mism += rvs.sample(a) != bok[i] || !space->equalStates(a, batch[i]);
+    // sampleGaussian interleaved with sampleUniform: the stream positions agree exactly; a Gaussian
+    // value may differ by a few ulps where glibc's log is not rounded to nearest (rarely)
+    SeededSampler rs(space.get(), 91);
+    gbompl::GpuStateSampler gs(space.get(), ctx, 91);
+    int gauss_differ = 0;
+    for (int i = 0; i < 400; ++i)
+    {
+        if (i % 7 == 3)
+        {
+            rs.sampleUniform(a);
+            gs.sampleUniform(b);
+            mism += !space->equalStates(a, b);
+            continue;
+        }
+        auto *m = la->as<ob::RealVectorStateSpace::StateType>()->values;
+        m[0] = U(g);
+        m[1] = U(g);
+        rs.sampleGaussian(a, la, 0.3);
+        gs.sampleGaussian(b, la, 0.3);
+        auto *va = a->as<ob::RealVectorStateSpace::StateType>()->values;
+        auto *vb = b->as<ob::RealVectorStateSpace::StateType>()->values;
+        for (int k = 0; k < 2; ++k)
+        {
+            gauss_differ += va[k] != vb[k];
+            mism += std::fabs(va[k] - vb[k]) > 4 * std::numeric_limits<double>::epsilon();
+        }
+    }
+    mism += gauss_differ > 8;
     std::printf("%s mismatches=%d valid=%u invalid=%u\n", mism ? "MISMATCH" : "MATCH", mism,
                 gmv.getValidMotionCount(), gmv.getInvalidMotionCount());
     return mism ? 1 : 0;

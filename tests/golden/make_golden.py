@@ -104,6 +104,11 @@ def main(tree):
         "chain10": SpaceDesc(SPACE_KINEMATIC_CHAIN, 10, link_length=0.1, lvs_fraction=0.005),
         "wrap7": SpaceDesc(SPACE_WRAP_L2, 7, lvs_fraction=0.01 / math.sqrt(7 * PI * PI)),
     }
+    # sampleGaussian calls interleaved with sampleUniform on one RNG (RealVectorStateSpace.cpp:67-82,
+    # SO2StateSpace.cpp:58-62, RandomNumbers.h:98-101): odd call sizes carry the cached normal value
+    gauss_ops = [("gaussian", 151), ("uniform", 3), ("gaussian", 100), ("gaussian", 1), ("uniform", 2),
+                 ("gaussian", 147)]
+    grng = np.random.default_rng(777)
     for name, sp in spaces.items():
         lo = np.asarray(sp.low) if sp.kind == SPACE_REAL_VECTOR else np.full(sp.dim, -PI)
         hi = np.asarray(sp.high) if sp.kind == SPACE_REAL_VECTOR else np.full(sp.dim, PI)
@@ -122,6 +127,11 @@ def main(tree):
             sample_seed=7, sample=R.sample_uniform(sp, 7, 700),
             near=near, near_distance=0.3, sample_near=R.sample_uniform_near(sp, 11, near, 0.3),
             oob=out_of_bounds, enforce=R.enforce_bounds(sp, out_of_bounds))
+        gmean = grng.uniform(lo, hi, size=(399, sp.dim))
+        out[f"space_{name}"].update(
+            gauss_kinds=np.array([1 if k == "gaussian" else 0 for k, _ in gauss_ops]),
+            gauss_counts=np.array([c for _, c in gauss_ops]), gauss_seed=5, gauss_mean=gmean, gauss_stddev=0.4,
+            gauss_out=R.sample_script(sp, 5, gauss_ops, gmean, 0.4))
 
     # Workload-0 circles world (seeded), checked with the reference DiscreteMotionValidator.
     w0 = W.config0(seed=0, n_states=3000, n_edges=3000, n_queries=300)

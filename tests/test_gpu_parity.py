@@ -103,6 +103,79 @@ def test_sampler_stream_vs_ompl(golden, name):
     assert same_bits(near, g["sample_near"])
 
 
+def _gpu_script(smp, ops, mean, stddev):
+    rows, m = [], 0
+    for kind, c in ops:
+        if kind == "gaussian":
+            rows.append(smp.sampleGaussian(mean[m:m + c], stddev))
+            m += c
+        else:
+            rows.append(smp.sampleUniform(c))
+    return np.vstack(rows)
+
+
+def _gauss_rows(ops):
+    return np.concatenate([np.full(c, k == "gaussian") for k, c in ops])
+
+
+@pytest.mark.parametrize("name", ["rv2", "rv7", "so2", "chain10", "wrap7"])
+def test_sampler_gaussian_vs_ompl(golden, port, name):
+    """sampleGaussian interleaved with sampleUniform on one sampler, odd call sizes (the cached normal
+    value crosses calls). Bitwise against the polar method with a log rounded to nearest (the oracle's
+    log_mode 1); against OMPL's own output every uniform row is bitwise (same stream position) and a
+    Gaussian value differs only where glibc's log rounds the other way: by at most 4 ulps of the
+    value's magnitude or of the mean's, in under 1% of the values."""
+    g = golden(f"space_{name}")
+    sp = space_of(g)
+    ops = [(("uniform", "gaussian")[int(k)], int(c)) for k, c in zip(g["gauss_kinds"], g["gauss_counts"])]
+    mean, sd = g["gauss_mean"], float(g["gauss_stddev"])
+    got = _gpu_script(B.StateSampler(gpu_space(g), int(g["gauss_seed"])), ops, mean, sd)
+    assert same_bits(got, port.sample_script(sp, int(g["gauss_seed"]), ops, mean, sd, log_mode=1))
+    ref = g["gauss_out"]
+    gr = _gauss_rows(ops)
+    assert same_bits(got[~gr], ref[~gr])
+    a, b = got[gr], ref[gr]
+    scale = np.maximum(np.maximum(np.abs(a), np.abs(b)), 1.0)
+    assert np.all(np.abs(a - b) <= 4 * np.finfo(np.float64).eps * scale)
+    assert np.count_nonzero(a != b) <= 0.01 * a.size
+
+
+def test_sampler_gaussian_across_chunks_vs_oracle(port):
+    """One sampleGaussian call of 7M values (more polar candidates than one chunk of the word scratch
+    holds, so two host rounds), then a uniform call: bitwise against the oracle's polar method with
+    the log rounded to nearest, and the stream position after the call is OMPL's."""
+    d = SpaceDesc(capi.SPACE_REAL_VECTOR, 7, np.full(7, -2.0), np.full(7, 2.0))
+    s = gpu_space(d)
+    n = 1_000_001
+    rng = np.random.default_rng(5)
+    mean = rng.uniform(-1.5, 1.5, size=(n + 3, 7))
+    ops = [("gaussian", 2), ("gaussian", n), ("gaussian", 1), ("uniform", 9)]
+    smp = B.StateSampler(s, 77)
+    got = _gpu_script(smp, ops, mean, 0.5)
+    want = port.sample_script(d, 77, ops, mean, 0.5, log_mode=1)
+    assert same_bits(got[:1000], want[:1000]) and same_bits(got[-20:], want[-20:])
+    assert same_bits(got, want)
+    # the same values on the device through the torch wrapper (device mean rows)
+    smp2 = B.StateSampler(s, 77)
+    dm = torch.from_numpy(mean[:5]).cuda()
+    assert same_bits(smp2.sampleGaussian(dm, 0.5).cpu().numpy(), want[:5])
+
+
+def test_sampler_gaussian_so2_wraps_and_rv_clamps(port):
+    """Large standard deviations: SO2 values wrap into [-pi, pi) and RealVector values clamp to the
+    bounds, as OMPL's samplers do (bitwise against the oracle with the rounded-to-nearest log)."""
+    for d, sd in ((SpaceDesc(capi.SPACE_SO2, 1), 9.0),
+                  (SpaceDesc(capi.SPACE_REAL_VECTOR, 3, np.array([0.0, -1.0, 5.0]), np.array([1.0, 1.0, 5.5])), 3.0)):
+        mean = np.random.default_rng(2).uniform(-3, 3, size=(5001, d.dim))
+        got = B.StateSampler(gpu_space(d), 3).sampleGaussian(mean, sd)
+        want = port.sample_script(d, 3, [("gaussian", 5001)], mean, sd, log_mode=1)
+        assert same_bits(got, want)
+        if d.kind == capi.SPACE_SO2:
+            assert np.all((got >= -math.pi) & (got < math.pi))
+        else:
+            assert np.all((got >= d.low) & (got <= d.high)) and np.any(got == d.low) and np.any(got == d.high)
+
+
 def test_sampler_large_stream_vs_oracle(port):
     d = SpaceDesc(capi.SPACE_REAL_VECTOR, 7, np.full(7, -math.pi), np.full(7, math.pi))
     s = gpu_space(d)

@@ -42,6 +42,40 @@ def test_state_samplers(port, golden, name):
     assert same_bits(port.sample_uniform_near(sp, 11, g["near"], float(g["near_distance"])), g["sample_near"])
 
 
+GAUSS_NAMES = {0: "uniform", 1: "gaussian"}
+
+
+def gauss_script(g):
+    return [(GAUSS_NAMES[int(k)], int(c)) for k, c in zip(g["gauss_kinds"], g["gauss_counts"])]
+
+
+@pytest.mark.parametrize("name", SPACES)
+def test_state_sampler_gaussian(port, golden, name):
+    # sampleGaussian (RealVectorStateSpace.cpp:67-82, SO2StateSpace.cpp:58-62) interleaved with
+    # sampleUniform on one RNG; std::normal_distribution's cached value carries across calls
+    g = golden(f"space_{name}")
+    sp = space_of(g)
+    out = port.sample_script(sp, int(g["gauss_seed"]), gauss_script(g), g["gauss_mean"], float(g["gauss_stddev"]))
+    assert same_bits(out, g["gauss_out"])
+
+
+def test_log_rounded_to_nearest(port):
+    """ora_log_rn against a 200-bit evaluation (mpmath), on the arguments the polar method feeds it
+    (x^2 + y^2 in (0, 1]) and on arguments next to 1 and to powers of two."""
+    mpmath = pytest.importorskip("mpmath")
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1, 1, size=(6000, 2))
+    r2 = (x * x).sum(axis=1)
+    r2 = r2[(r2 > 0) & (r2 <= 1)]
+    near1 = 1.0 - np.ldexp(rng.integers(1, 1 << 52, size=1000).astype(np.float64), -rng.integers(53, 110, size=1000))
+    pow2 = np.ldexp(1.0 + rng.uniform(-0.3, 0.4, size=1000), -rng.integers(0, 200, size=1000))
+    args = np.concatenate([r2, near1, pow2, [1.0, 0.5, 0.25, np.nextafter(1.0, 0.0), 2.0 ** -1000]])
+    got = port.log_rn(args)
+    mpmath.mp.prec = 200
+    want = np.array([float(mpmath.log(mpmath.mpf(float(v)))) for v in args])
+    assert same_bits(got, want)
+
+
 @pytest.mark.parametrize("name", ["circles_seeded", "circles_ompl_tests", "chain_seeded", "chain_horn", "dh_arm"])
 def test_validity_and_discrete_motion(port, golden, name):
     g = golden(name)
