@@ -486,7 +486,8 @@ def arm_bench(args):
 
 def prm_bench(args):
     """Full PRM roadmap construction (2M uniform samples, validity filter, prefix nearestK k=10 in
-    the wrap-L2 joint space, n->m edges at 0.01 rad) for the DH arm among 16,384 spheres."""
+    the wrap-L2 joint space, n->m edges at 0.01 rad) for the DH arm among 16,384 spheres.
+    PRM_STAR=1: PRM* connection counts (KStarStrategy, k(m) = ceil((e + e/7) log(m + 1)))."""
     import torch
 
     from ompl_gb300 import base as B
@@ -494,14 +495,15 @@ def prm_bench(args):
     from ompl_gb300 import workloads as W
     w = W.config4()
     n = int(os.environ.get("PRM_SAMPLES", w.extra["n_samples"]))
+    star = os.environ.get("PRM_STAR", "0") == "1"
     space = B.WrapL2StateSpace(7)
     space.setLongestValidSegmentFraction(w.lvs_fraction)
     checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
     checker.setPrecision("fp32_guarded")
-    prm.construct_roadmap(space, checker, w.extra["sampler_seed"], 20_000)  # warm-up (autotune, allocs)
+    prm.construct_roadmap(space, checker, w.extra["sampler_seed"], 20_000, star=star)  # warm-up (autotune, allocs)
     torch.cuda.synchronize()
     t = time.perf_counter()
-    rm = prm.construct_roadmap(space, checker, w.extra["sampler_seed"], n)
+    rm = prm.construct_roadmap(space, checker, w.extra["sampler_seed"], n, star=star)
     total = time.perf_counter() - t
     nm = rm.milestones.shape[1]
     # the motion phase under each persistent schedule (the autotuner picks one per checker)
@@ -518,7 +520,8 @@ def prm_bench(args):
         torch.cuda.synchronize()
         sched[name] = s1.shape[1] / (time.perf_counter() - t0)
     comps = prm.connected_components(nm, rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy())
-    print(json.dumps({"metric": "PRM roadmap construction (DH arm, 16384 spheres)", "samples": n,
+    print(json.dumps({"metric": "PRM%s roadmap construction (DH arm, 16384 spheres)" % ("*" if star else ""),
+                      "samples": n,
                       "milestones": nm, "candidate_edges": rm.candidate_edges, "edges": int(rm.edge_src.numel()),
                       "components": comps, "total_s": total, "timings_ms": rm.timings_ms,
                       "edges_per_s": rm.candidate_edges / (rm.timings_ms["motion"] * 1e-3),

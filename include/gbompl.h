@@ -173,7 +173,9 @@ gbo_status gbo_nn_remove(gbo_nn *nn, const int64_t *keys, int64_t n, gbo_stream 
 gbo_status gbo_nn_clear(gbo_nn *nn);
 gbo_status gbo_nn_size(const gbo_nn *nn, int64_t *size);
 /* nearestK: idx/dist are nq x k row-major, sorted by (distance, key); -1 / +inf padding when fewer
- * than k elements. prefix (nullable): query i only sees keys < prefix[i] (PRM insertion order).
+ * than k elements; 1 <= k <= 64 (the FP32-guarded form covers k <= 64 on RealVector / wrapped spaces
+ * of dim <= 8 and k <= 20 on the chain space; larger k there runs the FP64 scan).
+ * prefix (nullable): query i only sees keys < prefix[i] (PRM insertion order).
  * dist may be NULL. distance is evaluated as distance(element, query), like NearestNeighborsLinear. */
 gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
                             const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream);

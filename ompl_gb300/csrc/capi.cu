@@ -1585,7 +1585,7 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
     StatesView qv = make_view(q, ld, layout);
     RunCounters *ctr = nn->ctr.take(lc.stream);
     nn->queries += nq;
-    if (nn->precision == GBO_PRECISION_FP32_GUARDED && k <= 20)
+    if (nn->precision == GBO_PRECISION_FP32_GUARDED && k <= knn_fp32_max_k(nn->sp))
     {
         if (auto st = nn->qfeat.reserve(sizeof(float) * nn->F * nq, lc.stream))
             return st;
@@ -1593,7 +1593,7 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
             return st;
         unsigned long long *fb_n = &ctr->queue;
         const int P = knn_chunks(lc, nq, nn->size);
-        const int keep = k <= 12 ? 16 : 24;
+        const int keep = knn_keep(k);
         const size_t pl = (size_t)P * nq * keep;
         if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + 64, lc.stream))
             return st;
@@ -1602,7 +1602,7 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
         // large batches over a large RealVector / wrapped index: cell index (PRM's prefix kNN)
         if ((nn->sp.kind == GBO_SPACE_WRAP_L2 || nn->sp.kind == GBO_SPACE_REAL_VECTOR) && nn->sp.dim <= 8 &&
-            nn->size >= 65536 && nn->size < (1ll << 31) && nq >= 4096)
+            nn->size >= 65536 && nn->size < (1ll << 31) && nq >= 4096 && k <= 20)
         {
             if (auto st = ensure_box_cells(nn, lc))
                 return st;

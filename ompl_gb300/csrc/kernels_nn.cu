@@ -581,6 +581,16 @@ static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpacePara
     note_launch();
 }
 
+int knn_fp32_max_k(const SpaceParams &sp)
+{
+    return (sp.kind == GBO_SPACE_WRAP_L2 || sp.kind == GBO_SPACE_REAL_VECTOR) && sp.dim <= 8 ? 64 : 20;
+}
+
+int knn_keep(int k)
+{
+    return k <= 12 ? 16 : k <= 20 ? 24 : k <= 40 ? 48 : 72;
+}
+
 int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size)
 {
     const int64_t qb = (nq + 127) / 128;
@@ -594,27 +604,38 @@ bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &s
                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
                      const int64_t *qorder)
 {
-    if (k > 20 || nq == 0)
+    if (nq == 0 || k > knn_fp32_max_k(sp))
         return false;
     const int64_t chunk = (nn.size + P - 1) / P;
-#define GBO_FP32(KIND, MAXD, MAXF)                                                                                     \
+#define GBO_FP32(KIND, MAXD, MAXF, KK)                                                                                 \
+    launch_fp32_t<KIND, MAXD, MAXF, KK>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr, part_d,     \
+                                        part_k, P, chunk, qorder)
+#define GBO_FP32_K(KIND, MAXD, MAXF)                                                                                   \
     do                                                                                                                \
     {                                                                                                                 \
         if (k <= 12)                                                                                                  \
-            launch_fp32_t<KIND, MAXD, MAXF, 16>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
-                                                part_d, part_k, P, chunk, qorder);                                            \
+            GBO_FP32(KIND, MAXD, MAXF, 16);                                                                           \
+        else if (k <= 20)                                                                                             \
+            GBO_FP32(KIND, MAXD, MAXF, 24);                                                                           \
+        else if (k <= 40)                                                                                             \
+            GBO_FP32(KIND, MAXD, MAXF, 48);                                                                           \
         else                                                                                                          \
-            launch_fp32_t<KIND, MAXD, MAXF, 24>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
-                                                part_d, part_k, P, chunk, qorder);                                            \
+            GBO_FP32(KIND, MAXD, MAXF, 72);                                                                           \
     } while (0)
     if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN && sp.dim <= 10)
-        GBO_FP32(GBO_SPACE_KINEMATIC_CHAIN, 10, 20);
+    {
+        if (k <= 12)
+            GBO_FP32(GBO_SPACE_KINEMATIC_CHAIN, 10, 20, 16);
+        else
+            GBO_FP32(GBO_SPACE_KINEMATIC_CHAIN, 10, 20, 24);
+    }
     else if (sp.kind == GBO_SPACE_WRAP_L2 && sp.dim <= 8)
-        GBO_FP32(GBO_SPACE_WRAP_L2, 8, 8);
+        GBO_FP32_K(GBO_SPACE_WRAP_L2, 8, 8);
     else if (sp.kind == GBO_SPACE_REAL_VECTOR && sp.dim <= 8)
-        GBO_FP32(GBO_SPACE_REAL_VECTOR, 8, 8);
+        GBO_FP32_K(GBO_SPACE_REAL_VECTOR, 8, 8);
     else
         return false;
+#undef GBO_FP32_K
 #undef GBO_FP32
     return true;
 }
@@ -1114,7 +1135,7 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
                       const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
                       unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
 {
-    if (k > 20 || nq == 0 || sp.dim > 8)
+    if (nq == 0 || sp.dim > 8 || k > 20)  // longer kept lists do not fit the cell kernel's registers
         return false;
 #define GBO_BCELL(KIND)                                                                                                \
     do                                                                                                                \

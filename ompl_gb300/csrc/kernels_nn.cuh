@@ -48,6 +48,10 @@ constexpr int kQueryKeys = 4096;
 void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float *qf, int64_t nq, int *work,
                         int64_t *order);
 int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size);
+// largest k of the FP32-guarded kNN forms (64 for box / wrapped kinds of dim <= 8, else 20; larger k
+// and other kinds use the FP64 scan) and the list length they keep per query and chunk
+int knn_fp32_max_k(const SpaceParams &sp);
+int knn_keep(int k);
 void launch_features(const LaunchCfg &lc, const SpaceParams &sp, StatesView v, int64_t n, float *out, int64_t ld_out);
 void launch_store_points(const LaunchCfg &lc, StatesView v, int64_t n, int dim, double *pts, int64_t cap,
                          int64_t first, unsigned char *alive);

@@ -84,7 +84,7 @@ extern "C" gbo_status gbo_nn_nearest_k_noalloc(gbo_nn *nn, const double *q, int6
     lc.sm_count = sm_count;
     const StatesView qv = make_view(q, ld, layout);
     RunCounters *ctr = (RunCounters *)scratch;
-    const bool fp32 = precision == GBO_PRECISION_FP32_GUARDED && k <= 20 &&
+    const bool fp32 = precision == GBO_PRECISION_FP32_GUARDED && k <= knn_fp32_max_k(sp) &&
                       ((sp.kind == GBO_SPACE_KINEMATIC_CHAIN && sp.dim <= 10) ||
                        ((sp.kind == GBO_SPACE_WRAP_L2 || sp.kind == GBO_SPACE_REAL_VECTOR) && sp.dim <= 8));
     if (!fp32)
@@ -94,7 +94,7 @@ extern "C" gbo_status gbo_nn_nearest_k_noalloc(gbo_nn *nn, const double *q, int6
         return cudaGetLastError() == cudaSuccess ? GBO_OK : internal_fail(GBO_ERR_CUDA, "kernel launch failed");
     }
     // scratch layout: counters | query features [F][nq] | fallback list [nq] | partial lists
-    const int keep = k <= 12 ? 16 : 24;
+    const int keep = knn_keep(k);
     const size_t head = align256(sizeof(RunCounters));
     const size_t feat = align256((size_t)F * nq * sizeof(float));
     const size_t fbl = align256((size_t)nq * sizeof(unsigned long long));

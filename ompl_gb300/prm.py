@@ -12,9 +12,16 @@ filter (always true, PRM.cpp:176), done as whole batches:
 
 The edge set equals the sequential PRM's for the same sampler seed (each connection attempt is
 independent of the others). Connected components are computed from the edge list on the host.
+
+PRM* (PRM(si, starStrategy = true), PRM.cpp:226-227) connects with KStarStrategy
+(ConnectionStrategy.h:120-156): milestone m asks for k(m) = ceil((e + e/d) log n) neighbours, n = m + 1
+the milestone count including m (addMilestone adds the vertex before asking, PRM.cpp:574-583) and d the
+state dimension. The batch runs one prefix nearestK with the largest k(m) and keeps the first k(m) of
+each sorted list.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -22,6 +29,31 @@ import torch
 
 from . import base as B
 from . import capi
+
+
+def kstar_counts(num_milestones: int, dim: int) -> np.ndarray:
+    """KStarStrategy's neighbour count for milestones 0 .. num_milestones - 1: ceil((e + e/d) log(m + 1)),
+    evaluated in double precision with the C library's log, as the C++ code does. k(m) is
+    non-decreasing, so each run of equal counts is located by binary search (a few hundred log calls)."""
+    kc = math.e + math.e / float(dim)
+
+    def kof(m):
+        return int(math.ceil(kc * math.log(float(m + 1))))
+
+    ks = np.empty(num_milestones, dtype=np.int64)
+    m = 0
+    while m < num_milestones:
+        kv = kof(m)
+        lo, hi = m, num_milestones - 1
+        while lo < hi:
+            mid = (lo + hi + 1) // 2
+            if kof(mid) <= kv:
+                lo = mid
+            else:
+                hi = mid - 1
+        ks[m:lo + 1] = kv
+        m = lo + 1
+    return ks
 
 
 @dataclass
@@ -64,7 +96,9 @@ class Roadmap:
 
 
 def construct_roadmap(space: B.StateSpace, checker: B.StateValidityChecker, sampler_seed: int, n_samples: int,
-                      k: int = 10, schedule: int = capi.SCHEDULE_AUTO, stream=None) -> Roadmap:
+                      k: int = 10, schedule: int = capi.SCHEDULE_AUTO, stream=None, star: bool = False) -> Roadmap:
+    """PRM's roadmap over the valid states among n_samples uniform samples: KStrategy with k neighbours,
+    or KStarStrategy (PRM*) when star is set (k is then ignored)."""
     dev = torch.device("cuda")
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     ev[0].record()
@@ -80,7 +114,12 @@ def construct_roadmap(space: B.StateSpace, checker: B.StateValidityChecker, samp
     if nm:
         nn.add(milestones, soa=True, stream=stream)
     prefix = torch.arange(nm, device=dev, dtype=torch.int64)
+    if star:
+        ks = torch.as_tensor(kstar_counts(nm, space.dim), device=dev)
+        k = max(int(ks[-1].item()) if nm else 0, 1)
     nbr, _ = nn.nearestK(milestones, k, prefix=prefix, soa=True, want_dist=False, stream=stream)
+    if star:
+        nbr = torch.where(torch.arange(k, device=dev)[None, :] < ks[:, None], nbr, torch.full_like(nbr, -1))
     ev[3].record()
     dst = torch.arange(nm, device=dev, dtype=torch.int64).repeat_interleave(k)
     src = nbr.reshape(-1)

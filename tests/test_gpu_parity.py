@@ -619,6 +619,9 @@ def test_knn_large_batch_vs_exact_scan(kind):
     for k in (10, 16):
         both(k)
     both(10, prefix=np.minimum(np.arange(len(queries)) * 13, n))
+    if kind != "chain10":  # kept lists of 48 and 72 entries (k up to 64, PRM*'s connection counts)
+        both(33)
+        both(64, prefix=np.minimum(np.arange(len(queries)) * 13, n))
     nn.remove(np.arange(0, n, 7))
     both(16)
     assert nn.stats()["queries"] > 0

@@ -47,3 +47,36 @@ def test_prm_roadmap_matches_sequential_prm(port, precision):
     assert got_edges == ref_edges
     assert prm.connected_components(len(M), rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy()) == \
         prm.connected_components(len(M), src[ok], dst[ok])
+
+
+def test_prm_star_roadmap_matches_sequential_prm(port):
+    """PRM* (KStarStrategy): milestone m connects to its ceil((e + e/7) log(m + 1)) nearest
+    predecessors (22 at the last of ~900 milestones, so the kNN keeps 48-entry lists)."""
+    n_samples = 2500
+    w = W.config4(n_samples=n_samples, n_world=1024)
+    seed = w.extra["sampler_seed"]
+    space = B.WrapL2StateSpace(7)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
+    rm = prm.construct_roadmap(space, checker, seed, n_samples, star=True)
+
+    port.set_threads(16)
+    sd = SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles, dh=w.dh, spheres_per_link=8, sphere_radius=0.05)
+    samples = port.sample_uniform(sd, seed, n_samples)
+    M = samples[port.is_valid(sd, cd, samples).astype(bool)]
+    ks = prm.kstar_counts(len(M), 7)
+    kmax = int(ks[-1])
+    assert kmax > 20
+    nbr, _ = port.knn_prefix(sd, M, M, np.arange(len(M)), kmax)
+    src, dst = [], []
+    for m in range(len(M)):
+        row = nbr[m, :ks[m]]
+        row = row[row >= 0]
+        src.extend(row.tolist())
+        dst.extend([m] * len(row))
+    src, dst = np.array(src, dtype=np.int64), np.array(dst, dtype=np.int64)
+    assert rm.candidate_edges == len(src)
+    ok = port.check_motion(sd, cd, M[src], M[dst], want_state=False, want_bisect=False)["ok"].astype(bool)
+    assert set(zip(rm.edge_src.cpu().tolist(), rm.edge_dst.cpu().tolist())) == \
+        set(zip(src[ok].tolist(), dst[ok].tolist()))

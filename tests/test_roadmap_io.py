@@ -1,11 +1,22 @@
 """Roadmap snapshot (ompl_gb300.prm.Roadmap): undirected CSR adjacency and the .npz round trip, on a
-small hand-made roadmap (no GPU needed)."""
+small hand-made roadmap, and PRM*'s neighbour counts (no GPU needed)."""
+import math
+
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from ompl_gb300.prm import Roadmap, connected_components  # noqa: E402
+from ompl_gb300.prm import Roadmap, connected_components, kstar_counts  # noqa: E402
+
+
+@pytest.mark.parametrize("dim", [1, 2, 7, 10])
+def test_kstar_counts_match_the_per_milestone_formula(dim):
+    # KStarStrategy (ConnectionStrategy.h:143-147): k = ceil((e + e/d) log n), n = milestones so far
+    kc = math.e + math.e / dim
+    want = [int(math.ceil(kc * math.log(m + 1))) for m in range(20000)]
+    assert kstar_counts(20000, dim).tolist() == want
+    assert kstar_counts(0, dim).size == 0 and kstar_counts(1, dim).tolist() == [0]
 
 
 def _roadmap():
