@@ -221,7 +221,10 @@ gbo_status gbo_sample_valid_host(gbo_sampler *s, gbo_checker *c, int64_t n, unsi
  * request when a stream slot is free and its device footprint (inputs, outputs) fits in the server's
  * arena, runs admitted requests concurrently on its streams, and frees slots and memory as requests
  * complete (requests behind a blocked one are admitted when they fit). Inputs and outputs are host
- * arrays (AoS rows; pinned memory copies fastest). Requests on one nearest-neighbour index run one at
+ * arrays (AoS rows). gbo_server_submit copies the inputs into the server's page-locked staging
+ * arena when it has room (up to 2 GiB, at most the device arena's size), and results reach the
+ * caller's arrays when the request completes; without room the request reads and writes the caller's
+ * arrays directly, which is slower. Requests on one nearest-neighbour index run one at
  * a time (they share its scratch). No OMPL counterpart: OMPL's planners call the plugins one state at
  * a time from their own threads (tools/multiplan/ParallelPlan.h, geometric/planners/rrt/pRRT.h,
  * geometric/planners/cforest/CForest.h). */

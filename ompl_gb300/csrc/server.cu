@@ -6,7 +6,15 @@
 // skipping any that does not fit yet (or whose nearest-neighbour index is busy) so that small
 // requests are not held behind a large one, copies inputs host->device, launches the library's
 // kernels on the slot's stream, copies results device->host, and records an event.
+//
+// Host staging: submit() copies a request's inputs into a page-locked staging arena (on the caller's
+// thread) when it has room, so that the dispatcher's copies are asynchronous DMA in both directions
+// and never wait for a stream; results land in staging and are copied to the caller's arrays when the
+// request retires. A request that finds no staging room uses the caller's arrays directly (a copy
+// from or to pageable memory then blocks the dispatcher until it is done).
+#include <algorithm>
 #include <chrono>
+#include <cstring>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -24,14 +32,19 @@ namespace
 {
 using Clock = std::chrono::steady_clock;
 
-// First-fit allocator over one device range (256-byte granules).
+// First-fit allocator over one device range, or one page-locked host range (256-byte granules).
 class Arena
 {
 public:
-    bool init(size_t bytes)
+    bool init(size_t bytes, bool host = false)
     {
-        if (cudaMalloc(&base_, bytes) != cudaSuccess)
+        host_ = host;
+        if ((host ? cudaHostAlloc((void **)&base_, bytes, cudaHostAllocDefault) : cudaMalloc(&base_, bytes)) !=
+            cudaSuccess)
+        {
+            base_ = nullptr;
             return false;
+        }
         size_ = bytes;
         free_[0] = bytes;
         return true;
@@ -39,7 +52,7 @@ public:
     ~Arena()
     {
         if (base_)
-            cudaFree(base_);
+            host_ ? cudaFreeHost(base_) : cudaFree(base_);
     }
     long alloc(size_t bytes)
     {
@@ -83,6 +96,7 @@ public:
 
 private:
     char *base_ = nullptr;
+    bool host_ = false;
     size_t size_ = 0, used_ = 0;
     std::map<size_t, size_t> free_;
 };
@@ -94,6 +108,7 @@ struct Job
     Clock::time_point submitted;
     size_t bytes = 0;
     long off = -1;
+    long hoff = -1;  // host staging range (same layout as the device range), -1: none
     int slot = -1;
     cudaEvent_t done = nullptr;
     gbo_status status = GBO_OK;
@@ -102,19 +117,6 @@ struct Job
     std::string error;
 };
 
-size_t footprint(const gbo_request &r, int dim)
-{
-    const size_t rows = (size_t)r.n * dim * sizeof(double);
-    switch (r.kind)
-    {
-        case GBO_REQ_VALIDITY:
-            return rows + (size_t)r.n + 512;
-        case GBO_REQ_MOTION:
-            return 2 * rows + 9 * (size_t)r.n + 1024;
-        default:
-            return rows + (size_t)r.n * r.k * 16 + 512;
-    }
-}
 }  // namespace
 
 namespace gbo
@@ -127,6 +129,8 @@ using gbo::internal_request_dim;
 struct gbo_server
 {
     Arena arena;
+    Arena staging;  // page-locked host copy of admitted requests' inputs and outputs (may be empty)
+    std::vector<cudaEvent_t> slot_event;
     std::vector<cudaStream_t> streams;
     std::vector<Job *> slot_job;
     std::mutex mu;
@@ -149,54 +153,126 @@ static size_t pad256(size_t b)
     return (b + 255) & ~size_t(255);
 }
 
+// Byte offsets of a request's arrays inside its arena range (the host staging range uses the same
+// layout): inputs first ([0, in_end)), then outputs ([out_begin, out_end)).
+struct ReqLayout
+{
+    size_t in2 = 0, in_end = 0, ok = 0, fj = 0, nd = 0, idx = 0, dist = 0, out_begin = 0, out_end = 0;
+};
+
+static ReqLayout req_layout(const gbo_request &r, int dim)
+{
+    ReqLayout L;
+    const size_t n = (size_t)r.n, rows = n * dim * sizeof(double);
+    if (r.kind == GBO_REQ_VALIDITY)
+    {
+        L.in_end = rows;
+        L.ok = L.out_begin = pad256(rows);
+        L.out_end = L.ok + n;
+    }
+    else if (r.kind == GBO_REQ_MOTION)
+    {
+        L.in2 = pad256(rows);
+        L.in_end = L.in2 + rows;
+        L.fj = L.out_begin = L.in2 + pad256(rows);
+        L.nd = L.fj + pad256(4 * n);
+        L.ok = L.nd + pad256(4 * n);
+        L.out_end = L.ok + n;
+    }
+    else
+    {
+        L.in_end = rows;
+        L.idx = L.out_begin = pad256(rows);
+        L.dist = L.idx + pad256(n * r.k * 8);
+        L.out_end = L.dist + n * r.k * 8;
+    }
+    return L;
+}
+
+// Inputs into the job's staging range (caller's thread, before the job is queued).
+static void stage_inputs(const gbo_request &r, int dim, char *h)
+{
+    const ReqLayout L = req_layout(r, dim);
+    const size_t rows = (size_t)r.n * dim * sizeof(double);
+    if (rows)
+    {
+        std::memcpy(h, r.states, rows);
+        if (r.kind == GBO_REQ_MOTION)
+            std::memcpy(h + L.in2, r.states2, rows);
+    }
+}
+
+// Results from the job's staging range into the caller's arrays (dispatcher, at retirement).
+static void unstage_outputs(const gbo_request &r, int dim, const char *h)
+{
+    const ReqLayout L = req_layout(r, dim);
+    const size_t n = (size_t)r.n;
+    if (r.kind == GBO_REQ_KNN)
+    {
+        std::memcpy(r.idx, h + L.idx, n * r.k * 8);
+        if (r.dist)
+            std::memcpy(r.dist, h + L.dist, n * r.k * 8);
+        return;
+    }
+    std::memcpy(r.ok, h + L.ok, n);
+    if (r.kind == GBO_REQ_MOTION)
+    {
+        if (r.first_j)
+            std::memcpy(r.first_j, h + L.fj, 4 * n);
+        if (r.nd)
+            std::memcpy(r.nd, h + L.nd, 4 * n);
+    }
+}
+
 bool gbo_server::launch(Job *j)
 {
     const gbo_request &r = j->req;
     cudaStream_t st = streams[j->slot];
     int dim = 0;
     internal_request_dim(&r, &dim);
+    const ReqLayout L = req_layout(r, dim);
     char *d = arena.ptr((size_t)j->off);
-    const size_t rows = (size_t)r.n * dim * sizeof(double);
+    char *h = j->hoff >= 0 ? staging.ptr((size_t)j->hoff) : nullptr;  // staged: pinned copies
+    const size_t n = (size_t)r.n, rows = n * dim * sizeof(double);
     gbo_status s = GBO_OK;
+    cudaMemcpyAsync(d, h ? h : (const char *)r.states, rows, cudaMemcpyHostToDevice, st);
     if (r.kind == GBO_REQ_VALIDITY)
     {
-        uint8_t *dok = (uint8_t *)(d + pad256(rows));
-        cudaMemcpyAsync(d, r.states, rows, cudaMemcpyHostToDevice, st);
-        s = gbo_is_valid(r.checker, (const double *)d, r.n, dim, GBO_LAYOUT_AOS, dok, st);
+        s = gbo_is_valid(r.checker, (const double *)d, r.n, dim, GBO_LAYOUT_AOS, (uint8_t *)(d + L.ok), st);
         if (s == GBO_OK)
-            cudaMemcpyAsync(r.ok, dok, (size_t)r.n, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(h ? (void *)(h + L.ok) : (void *)r.ok, d + L.ok, n, cudaMemcpyDeviceToHost, st);
     }
     else if (r.kind == GBO_REQ_MOTION)
     {
-        char *d2 = d + pad256(rows);
-        int32_t *dfj = (int32_t *)(d2 + pad256(rows));
-        int32_t *dnd = (int32_t *)((char *)dfj + pad256(4 * (size_t)r.n));
-        uint8_t *dok = (uint8_t *)((char *)dnd + pad256(4 * (size_t)r.n));
-        cudaMemcpyAsync(d, r.states, rows, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(d2, r.states2, rows, cudaMemcpyHostToDevice, st);
-        s = gbo_check_motion(r.checker, (const double *)d, (const double *)d2, r.n, dim, GBO_LAYOUT_AOS, r.schedule,
-                             dok, dfj, dnd, st);
+        cudaMemcpyAsync(d + L.in2, h ? h + L.in2 : (const char *)r.states2, rows, cudaMemcpyHostToDevice, st);
+        s = gbo_check_motion(r.checker, (const double *)d, (const double *)(d + L.in2), r.n, dim, GBO_LAYOUT_AOS,
+                             r.schedule, (uint8_t *)(d + L.ok), (int32_t *)(d + L.fj), (int32_t *)(d + L.nd), st);
         if (s == GBO_OK)
         {
-            cudaMemcpyAsync(r.ok, dok, (size_t)r.n, cudaMemcpyDeviceToHost, st);
-            if (r.first_j)
-                cudaMemcpyAsync(r.first_j, dfj, 4 * (size_t)r.n, cudaMemcpyDeviceToHost, st);
-            if (r.nd)
-                cudaMemcpyAsync(r.nd, dnd, 4 * (size_t)r.n, cudaMemcpyDeviceToHost, st);
+            if (h)  // one copy of the whole output block
+                cudaMemcpyAsync(h + L.out_begin, d + L.out_begin, L.out_end - L.out_begin, cudaMemcpyDeviceToHost,
+                                st);
+            else
+            {
+                cudaMemcpyAsync(r.ok, d + L.ok, n, cudaMemcpyDeviceToHost, st);
+                if (r.first_j)
+                    cudaMemcpyAsync(r.first_j, d + L.fj, 4 * n, cudaMemcpyDeviceToHost, st);
+                if (r.nd)
+                    cudaMemcpyAsync(r.nd, d + L.nd, 4 * n, cudaMemcpyDeviceToHost, st);
+            }
         }
     }
     else
     {
-        int64_t *didx = (int64_t *)(d + pad256(rows));
-        double *ddist = (double *)((char *)didx + pad256((size_t)r.n * r.k * 8));
-        cudaMemcpyAsync(d, r.states, rows, cudaMemcpyHostToDevice, st);
-        s = gbo_nn_nearest_k(r.nn, (const double *)d, r.n, dim, GBO_LAYOUT_AOS, r.k, nullptr, didx,
-                             r.dist ? ddist : nullptr, st);
+        s = gbo_nn_nearest_k(r.nn, (const double *)d, r.n, dim, GBO_LAYOUT_AOS, r.k, nullptr, (int64_t *)(d + L.idx),
+                             r.dist ? (double *)(d + L.dist) : nullptr, st);
         if (s == GBO_OK)
         {
-            cudaMemcpyAsync(r.idx, didx, (size_t)r.n * r.k * 8, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(h ? (void *)(h + L.idx) : (void *)r.idx, d + L.idx, n * r.k * 8, cudaMemcpyDeviceToHost,
+                            st);
             if (r.dist)
-                cudaMemcpyAsync(r.dist, ddist, (size_t)r.n * r.k * 8, cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(h ? (void *)(h + L.dist) : (void *)r.dist, d + L.dist, n * r.k * 8,
+                                cudaMemcpyDeviceToHost, st);
         }
     }
     if (s != GBO_OK)
@@ -204,7 +280,7 @@ bool gbo_server::launch(Job *j)
         j->status = s;
         j->error = gbo_last_error();
     }
-    cudaEventCreateWithFlags(&j->done, cudaEventDisableTiming);
+    j->done = slot_event[j->slot];
     cudaEventRecord(j->done, st);
     return true;
 }
@@ -229,7 +305,16 @@ void gbo_server::run()
                 j->status = GBO_ERR_CUDA;
                 j->error = cudaGetErrorString(q);
             }
-            cudaEventDestroy(j->done);
+            if (j->hoff >= 0)
+            {
+                if (j->status == GBO_OK)
+                {
+                    int dim = 0;
+                    internal_request_dim(&j->req, &dim);
+                    unstage_outputs(j->req, dim, staging.ptr((size_t)j->hoff));
+                }
+                staging.release((size_t)j->hoff, j->bytes);
+            }
             arena.release((size_t)j->off, j->bytes);
             if (j->req.kind == GBO_REQ_KNN)
                 busy_nn.erase(j->req.nn);
@@ -318,6 +403,14 @@ gbo_status gbo_server_create(int n_streams, int64_t arena_bytes, gbo_server **ou
         s->streams.push_back(st);
     }
     s->slot_job.assign(n_streams, nullptr);
+    for (int i = 0; i < n_streams; ++i)
+    {
+        cudaEvent_t ev;
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        s->slot_event.push_back(ev);
+    }
+    // host staging: as large as the device arena up to 2 GiB; without it requests use the caller's arrays
+    s->staging.init(std::min<size_t>((size_t)arena_bytes, (size_t)2 << 30), true);
     s->worker = std::thread([s] { s->run(); });
     *out = s;
     return GBO_OK;
@@ -337,6 +430,8 @@ gbo_status gbo_server_destroy(gbo_server *s)
         delete kv.second;
     for (auto st : s->streams)
         cudaStreamDestroy(st);
+    for (auto ev : s->slot_event)
+        cudaEventDestroy(ev);
     delete s;
     return GBO_OK;
 }
@@ -355,7 +450,7 @@ gbo_status gbo_server_submit(gbo_server *s, const gbo_request *req, uint64_t *ti
         return GBO_ERR_INVALID_ARGUMENT;
     auto *j = new Job();
     j->req = r;
-    j->bytes = footprint(r, dim);
+    j->bytes = req_layout(r, dim).out_end + 256;
     j->submitted = Clock::now();
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -364,6 +459,13 @@ gbo_status gbo_server_submit(gbo_server *s, const gbo_request *req, uint64_t *ti
             delete j;
             return GBO_ERR_OUT_OF_MEMORY;  // can never be admitted
         }
+        if (s->staging.size())
+            j->hoff = s->staging.alloc(j->bytes);
+    }
+    if (j->hoff >= 0)
+        stage_inputs(r, dim, s->staging.ptr((size_t)j->hoff));  // on the caller's thread, outside the lock
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
         j->ticket = s->next_ticket++;
         *ticket = j->ticket;
         s->jobs[j->ticket] = j;

@@ -93,8 +93,12 @@ def test_admission_by_footprint():
     big = rng.uniform(-math.pi, math.pi, size=(40_000, 7))  # 2.2 MB of states: never fits
     with pytest.raises(capi.GboError):
         srv.submit_validity(ck, big)
-    small = [srv.submit_validity(ck, rng.uniform(-math.pi, math.pi, size=(5000, 7))) for _ in range(10)]
-    for t in small:
+    # the host staging arena (as large as the 1 MiB device arena) holds three of these at a time, so the
+    # later submissions use the caller's arrays directly: both paths must return the direct API's results
+    batches = [rng.uniform(-math.pi, math.pi, size=(5000, 7)) for _ in range(10)]
+    small = [srv.submit_validity(ck, b) for b in batches]
+    for t, b in zip(small, batches):
         res, lat = srv.wait(t)
         assert lat >= 0.0 and res["ok"].shape == (5000,)
+        assert np.array_equal(res["ok"], ck.isValid(b).astype(np.uint8))
     srv.close()
