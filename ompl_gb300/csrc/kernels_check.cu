@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(256) motion_plain_kernel(SpaceParams sp, World
 }
 
 template <int CK, int MAXD, int PREC>
-__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 3 : 1) motion_tile_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
+__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 4 : 1) motion_tile_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
                                                           int64_t n, uint8_t *ok, int32_t *first_j, int32_t *nd_out,
                                                           RunCounters *ctr)
 {
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 3 : 1) motio
 }
 
 template <int CK, int MAXD, int PREC>
-__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 3 : 1) motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
+__global__ void __launch_bounds__(256, CK == GBO_CHECK_DH_SPHERES ? 4 : 1) motion_warp_kernel(SpaceParams sp, WorldArgs wa, StatesView v1, StatesView v2,
                                                           int64_t n, uint8_t *ok, int32_t *first_j, int32_t *nd_out,
                                                           RunCounters *ctr)
 {
