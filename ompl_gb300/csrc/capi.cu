@@ -307,7 +307,7 @@ void note_launch()
 int persistent_grid(const void *kernel, int block, unsigned smem, const LaunchCfg &lc, int64_t max_blocks)
 {
     static std::mutex mu;
-    static std::map<std::pair<const void *, unsigned>, int> occ;
+    static std::map<std::pair<const void *, std::pair<unsigned, int>>, int> occ;
     static std::map<const void *, bool> raised;
     int per_sm = 0;
     {
@@ -322,7 +322,7 @@ int persistent_grid(const void *kernel, int block, unsigned smem, const LaunchCf
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
             raised[kernel] = true;
         }
-        auto key = std::make_pair(kernel, smem);
+        auto key = std::make_pair(kernel, std::make_pair(smem, block));
         auto it = occ.find(key);
         if (it == occ.end())
         {

@@ -51,16 +51,27 @@ __host__ __device__ inline unsigned chain_test_entry(int idx, int n_links, int n
     return (unsigned)(r % m) | ((unsigned)(r / m) << 8);
 }
 
-// Tables in shared memory: `order` (device, optional) is a permutation of the default entries chosen
-// on the host so that likely intersections come first (bit 31 marks a link-link pair).
-__device__ __forceinline__ void build_chain_tables(int n_links, int nw, const unsigned *order, unsigned *tab,
-                                                   ChainTables &t)
+// Per-warp tables in shared memory: `order` (device, optional) is a permutation of the default entries
+// chosen on the host so that likely intersections come first (bit 31 marks a link-link pair). Warp q's
+// table resolves every test to the indices of its two records in the CTA's record array (world
+// segments at [0, nw), warp q's links at [lb_q, lb_q + n_links + 1)): first | (second << 16). The
+// record array lives in shared memory (at most 7,264 records of 32 bytes), so 16 bits hold an index.
+__device__ __forceinline__ void build_chain_tables(int n_links, int nw, const unsigned *order, unsigned *tabs,
+                                                   int n_warps, ChainTables &t)
 {
     int n_self;
     t.n_tests = chain_test_count(n_links, nw, n_self);
     t.n_self = n_self;
-    for (int idx = threadIdx.x; idx < t.n_tests; idx += blockDim.x)
-        tab[idx] = order ? order[idx] : chain_test_entry(idx, n_links, nw);
+    const int total = n_warps * t.n_tests;
+    for (int k = threadIdx.x; k < total; k += blockDim.x)
+    {
+        const int q = k / t.n_tests, idx = k - q * t.n_tests;
+        const unsigned e = order ? order[idx] : chain_test_entry(idx, n_links, nw);
+        const int lb = nw + q * (n_links + 1);
+        const int ia = lb + chain_test_a(e);
+        const int ib = (e & 0x80000000u) ? lb + chain_test_b(e) : chain_test_b(e);
+        tabs[k] = (unsigned)ia | ((unsigned)ib << 16);
+    }
 }
 
 // Link directions of one state: lane k < n holds joint k as float-float (zero elsewhere).
@@ -144,12 +155,16 @@ __device__ __forceinline__ void init_chain_links(ChainSegF32 *links, int count, 
 // FP64 re-evaluation of the tests of one round whose FP32 result is ambiguous (reference operation
 // order): builds the state's FP64 segments from q = joint `lane` in FP64 and reruns the lanes whose
 // r is kAmbiguous. Warp-collective. Out of line so that the FP32 loop carries no FP64 values.
-static __device__ __noinline__ int chain_round64(int lane, int n, double L64, double q, unsigned e, int r,
-                                                 const double *w64)
+// e: the lane's table entry (record indices, see build_chain_tables); nw, lb: world size and the
+// warp's first link record.
+static __device__ __noinline__ int chain_round64(int lane, int n, double L64, double q, unsigned e, int nw, int lb,
+                                                 int r, const double *w64)
 {
     double sx0, sy0, sx1, sy1;
     chain_segments64_warp(q, lane, n, L64, sx0, sy0, sx1, sy1);
-    const int a = chain_test_a(e), b = chain_test_b(e);
+    const int ib = (int)(e >> 16);
+    const bool link = ib >= nw;
+    const int a = (int)(e & 0xffffu) - lb, b = link ? ib - lb : ib;
     const double ax0 = __shfl_sync(0xffffffffu, sx0, a), ay0 = __shfl_sync(0xffffffffu, sy0, a);
     const double ax1 = __shfl_sync(0xffffffffu, sx1, a), ay1 = __shfl_sync(0xffffffffu, sy1, a);
     const double bx0 = __shfl_sync(0xffffffffu, sx0, b & 31), by0 = __shfl_sync(0xffffffffu, sy0, b & 31);
@@ -157,7 +172,7 @@ static __device__ __noinline__ int chain_round64(int lane, int n, double L64, do
     if (r != kAmbiguous)
         return r;
     bool hit;
-    if (e & 0x80000000u)
+    if (link)
         hit = seg_intersect64(ax0, ay0, ax1, ay1, bx0, by0, bx1, by1);
     else
     {
@@ -169,13 +184,13 @@ static __device__ __noinline__ int chain_round64(int lane, int n, double L64, do
 
 // Warp-cooperative state test: kInvalid or kValid (same in all lanes). Lane k <= n holds segment k
 // of the state (vector vx, vy; start px, py). `w` is the CTA's shared record array: the world's
-// segments at [0, nw), this warp's link records at [lb, lb + n + 1). Tests run 32 per round in table
-// order; a round with an ambiguous FP32 result re-evaluates those tests with the FP64 reference code
-// (chain_round64) from q64(lane) = joint `lane` of the state in FP64. `rechecked` counts states that
-// needed FP64.
+// segments at [0, nw), this warp's link records at [lb, lb + n + 1); `tab` is this warp's table of
+// record indices. Tests run 32 per round in table order; a round with an ambiguous FP32 result
+// re-evaluates those tests with the FP64 reference code (chain_round64) from q64(lane) = joint `lane`
+// of the state in FP64. `rechecked` counts states that needed FP64.
 template <class Q64>
 __device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, float vx, float vy, float px,
-                                                  float py, ChainSegF32 *w, int lb, const double *w64,
+                                                  float py, ChainSegF32 *w, int nw, int lb, const double *w64,
                                                   const unsigned *tab, ChainTables t, Q64 q64, unsigned &rechecked)
 {
     __syncwarp();  // the previous state's records are no longer read
@@ -191,9 +206,8 @@ __device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, f
         if (idx < t.n_tests)
         {
             e = tab[idx];
-            const int a = chain_test_a(e), b = chain_test_b(e);
-            const float4 A = *(const float4 *)&w[lb + a];
-            const ChainSegF32 B = w[(e & 0x80000000u) ? lb + b : b];
+            const float4 A = *(const float4 *)&w[e & 0xffffu];
+            const ChainSegF32 B = w[e >> 16];
             r = seg_intersect32(A.z, A.w, B.sx, B.sy, A.x - B.x0, A.y - B.y0, B.lo, B.hi, B.e_den);
         }
         if (__ballot_sync(0xffffffffu, r != kValid))
@@ -205,7 +219,7 @@ __device__ __forceinline__ int chain_state_warp32(int lane, int n, double L64, f
                     have64 = true;
                     ++rechecked;
                 }
-                r = chain_round64(lane, n, L64, q64(lane), e, r, w64);
+                r = chain_round64(lane, n, L64, q64(lane), e, nw, lb, r, w64);
             }
             if (__any_sync(0xffffffffu, r == kInvalid))
                 return kInvalid;

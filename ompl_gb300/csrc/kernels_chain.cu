@@ -20,12 +20,13 @@ namespace gbo
 {
 
 // Dynamic shared memory of the warp kernels: the world's ChainSegF32 records (bytes32 = 32 * nw),
-// then (dim + 1) link records per warp, then the test table (one u32 per test).
+// then (dim + 1) link records per warp, then one test table per warp (one u32 per test).
 struct ChainSmem
 {
     ChainSegF32 *w32;
-    const unsigned *tab;
-    int lb;  // index of this warp's first link record in w32
+    const unsigned *tab;  // this warp's table
+    int nw;               // world segments
+    int lb;               // index of this warp's first link record in w32
     ChainTables t;
 };
 
@@ -37,11 +38,12 @@ __device__ bool chain_setup(const SpaceParams &sp, const WorldArgs &wa, unsigned
     ChainSegF32 *w = (ChainSegF32 *)smem;
     const int per_warp = sp.dim + 1, n_link_recs = (int)(blockDim.x >> 5) * per_warp;
     init_chain_links(w + wa.n, n_link_recs, wa.guard);
-    unsigned *tab = (unsigned *)(w + wa.n + n_link_recs);
-    build_chain_tables(sp.dim, wa.n, wa.test_order, tab, cs.t);
+    unsigned *tabs = (unsigned *)(w + wa.n + n_link_recs);
+    build_chain_tables(sp.dim, wa.n, wa.test_order, tabs, (int)(blockDim.x >> 5), cs.t);
     __syncthreads();
     cs.w32 = w;
-    cs.tab = tab;
+    cs.tab = tabs + (threadIdx.x >> 5) * cs.t.n_tests;
+    cs.nw = wa.n;
     cs.lb = wa.n + (int)(threadIdx.x >> 5) * per_warp;
     return true;
 }
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(256, 4) chain_validity_warp_kernel(const __gri
         float vx, vy, px, py;
         chain_segments32(lane_joint(v, i, lane, dim), lane, dim, L, vx, vy, px, py);
         auto q64 = [&](int ln) { return ln < dim ? v(i, ln) : 0.0; };
-        const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t, q64,
+        const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.nw, cs.lb, w64, cs.tab, cs.t, q64,
                                          rechecks);
         if (lane == 0)
             out[i] = r == kValid ? 1 : 0;
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(const __grid_
             float vx, vy, px, py;
             chain_segments32(q, lane, dim, L, vx, vy, px, py);
             auto q64 = [&](int ln) { return ln < dim ? motion_joint64(v1, v2, e, ln, j, nd, top) : 0.0; };
-            const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.lb, w64, cs.tab, cs.t, q64,
+            const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.nw, cs.lb, w64, cs.tab, cs.t, q64,
                                              rechecks);
             ++evaluated;
             if (r == kInvalid)
@@ -281,7 +283,8 @@ static unsigned chain_smem(const SpaceParams &sp, const WorldArgs &wa, int block
 {
     const int m = sp.dim + 1;
     const int n_tests = (m - 1) * (m - 2) / 2 + m * wa.n;
-    return wa.bytes32 + (unsigned)((block / 32) * m * sizeof(ChainSegF32)) + (unsigned)((4 * n_tests + 15) & ~15);
+    return wa.bytes32 + (unsigned)((block / 32) * m * sizeof(ChainSegF32)) +
+           (unsigned)((4 * (block / 32) * n_tests + 15) & ~15);
 }
 
 // The dynamic shared memory limit of a persistent kernel is raised to the opt-in maximum - 1 KB.
@@ -293,16 +296,30 @@ static bool chain_smem_fits(unsigned bytes)
     return (int64_t)bytes + 1024 <= (int64_t)optin;
 }
 
+// Block size of the warp kernels: 256 threads, or fewer warps per CTA when the per-warp test tables of
+// a large world would not fit in shared memory (down to one warp, which needs what a single shared
+// table did). Returns 0 when even that does not fit.
+static int chain_block(const SpaceParams &sp, const WorldArgs &wa, unsigned &sm)
+{
+    for (int block = 256; block >= 32; block /= 2)
+    {
+        sm = chain_smem(sp, wa, block);
+        if (chain_smem_fits(sm))
+            return block;
+    }
+    return 0;
+}
+
 bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v,
                                 int64_t n, uint8_t *out, RunCounters *ctr)
 {
-    if (sp.dim > 31 || !wa.stage32)
+    unsigned sm = 0;
+    const int block = sp.dim > 31 || !wa.stage32 ? 0 : chain_block(sp, wa, sm);
+    if (!block)
         return false;
-    const unsigned sm = chain_smem(sp, wa, 256);
-    if (!chain_smem_fits(sm))
-        return false;
-    const int grid = persistent_grid((const void *)chain_validity_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
-    chain_validity_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v, n, out, ctr);
+    const int grid =
+        persistent_grid((const void *)chain_validity_warp_kernel, block, sm, lc, (n * 32 + block - 1) / block);
+    chain_validity_warp_kernel<<<grid, block, sm, lc.stream>>>(sp, wa, v, n, out, ctr);
     note_launch();
     return true;
 }
@@ -310,13 +327,13 @@ bool launch_chain_validity_warp(const LaunchCfg &lc, const SpaceParams &sp, cons
 bool launch_chain_motion_warp(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v1,
                               StatesView v2, int64_t n, uint8_t *ok, int32_t *fj, int32_t *nd, RunCounters *ctr)
 {
-    if (sp.dim > 31 || !wa.stage32)
+    unsigned sm = 0;
+    const int block = sp.dim > 31 || !wa.stage32 ? 0 : chain_block(sp, wa, sm);
+    if (!block)
         return false;
-    const unsigned sm = chain_smem(sp, wa, 256);
-    if (!chain_smem_fits(sm))
-        return false;
-    const int grid = persistent_grid((const void *)chain_motion_warp_kernel, 256, sm, lc, (n * 32 + 255) / 256);
-    chain_motion_warp_kernel<<<grid, 256, sm, lc.stream>>>(sp, wa, v1, v2, n, ok, fj, nd, ctr);
+    const int grid =
+        persistent_grid((const void *)chain_motion_warp_kernel, block, sm, lc, (n * 32 + block - 1) / block);
+    chain_motion_warp_kernel<<<grid, block, sm, lc.stream>>>(sp, wa, v1, v2, n, ok, fj, nd, ctr);
     note_launch();
     return true;
 }

@@ -374,6 +374,32 @@ def test_chain_motion_valid_endpoints_vs_oracle(chain_case, port):
             assert np.array_equal(r["nd"], ref["nd"])
 
 
+@pytest.mark.parametrize("n_seg", [600, 1500])
+def test_chain_large_world_vs_oracle(port, n_seg):
+    """Worlds of 600 and 1,500 short segments: the warp kernels' per-warp test tables then need fewer
+    warps per CTA (128 and 64 threads) to fit in shared memory. Validity and motion vs the oracle."""
+    rng = np.random.default_rng(n_seg)
+    c = rng.uniform(-1, 1, size=(n_seg, 2))
+    ang = rng.uniform(-math.pi, math.pi, n_seg)
+    half = 0.004 * np.stack([np.cos(ang), np.sin(ang)], axis=1)
+    world = np.concatenate([c - half, c + half], axis=1)
+    sp = SpaceDesc(capi.SPACE_KINEMATIC_CHAIN, 10, link_length=0.1, lvs_fraction=0.005)
+    ckd = CheckerDesc(capi.CHECK_CHAIN_SEGMENTS, world)
+    states = rng.uniform(-math.pi, math.pi, size=(6000, 10))
+    port.set_threads(16)
+    valid = port.is_valid(sp, ckd, states).astype(bool)
+    vs = states[valid]
+    assert len(vs) > 100
+    i, j = rng.integers(0, len(vs), 400), rng.integers(0, len(vs), 400)
+    ref = port.check_motion(sp, ckd, vs[i], vs[j], want_state=False, want_bisect=False)
+    s = gpu_space(sp)
+    ck = gpu_checker(s, ckd)
+    ck.setPrecision("fp32_guarded")
+    assert np.array_equal(ck.isValid(states), valid)
+    r = B.DiscreteMotionValidator(ck).checkMotions(vs[i], vs[j], schedule=capi.SCHEDULE_WARP)
+    assert np.array_equal(r["ok"], ref["ok"]) and np.array_equal(r["first_j"], ref["first_j"])
+
+
 def _chain_points(q, L=0.1):
     """Joint positions in the reference's operation order (KinematicChain.h:214-228)."""
     th, x, y, pts = 0.0, 0.0, 0.0, [(0.0, 0.0)]
