@@ -74,13 +74,13 @@ __device__ __forceinline__ void build_chain_tables(int n_links, int nw, const un
     }
 }
 
-// Link directions of one state: lane k < n holds joint k as float-float (zero elsewhere).
-// Returns, in lane k <= n, the segment vector V_k and start point P_k (lane n = tip segment).
-__device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L, float &vx, float &vy, float &px,
-                                                 float &py)
+// Segments of one state from its absolute link angles: lane k < n holds theta_k = q_0 + ... + q_k as
+// float-float. Returns, in lane k <= n, the segment vector V_k and start point P_k (lane n = tip segment).
+__device__ __forceinline__ void chain_segments32_theta(ff theta, int lane, int n, float L, float &vx, float &vy,
+                                                       float &px, float &py)
 {
     float c, s;
-    sincos_ff(warp_scan_ff(q, lane), c, s);
+    sincos_ff(theta, c, s);
     // tip segment (lane n) uses the last link's direction with length 0.001
     const float cl = __shfl_sync(0xffffffffu, c, n > 0 ? n - 1 : 0);
     const float sl = __shfl_sync(0xffffffffu, s, n > 0 ? n - 1 : 0);
@@ -96,6 +96,13 @@ __device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L,
         px = 0.f;
         py = 0.f;
     }
+}
+
+// The same from the joints: lane k < n holds joint k as float-float (zero elsewhere).
+__device__ __forceinline__ void chain_segments32(ff q, int lane, int n, float L, float &vx, float &vy, float &px,
+                                                 float &py)
+{
+    chain_segments32_theta(warp_scan_ff(q, lane), lane, n, L, vx, vy, px, py);
 }
 
 // FP64 segments of one state in the reference's operation order (KinematicChain.h:214-228): theta
@@ -259,14 +266,15 @@ __device__ __forceinline__ void chain_state_hits32(int lane, float vx, float vy,
     }
 }
 
-// Workspace distance of two states (lane k < n holds joint k of each) and the FP32 segment count.
-// Returns the segment count, or -1 when ceil(distance / lvs) is not decided by the error bound.
-__device__ __forceinline__ int chain_segment_count_warp(ff qa, ff qb, int lane, int n, float L, float inv_lvs,
+// Workspace distance of two states given their absolute link angles (lane k < n: theta_k of each, as
+// from warp_scan_ff of the joints) and the FP32 segment count. Returns the segment count, or -1 when
+// ceil(distance / lvs) is not decided by the error bound.
+__device__ __forceinline__ int chain_segment_count_warp(ff ta, ff tb, int lane, int n, float L, float inv_lvs,
                                                         float e_dist, unsigned factor)
 {
     float c1, s1, c2, s2;
-    sincos_ff(warp_scan_ff(qa, lane), c1, s1);
-    sincos_ff(warp_scan_ff(qb, lane), c2, s2);
+    sincos_ff(ta, c1, s1);
+    sincos_ff(tb, c2, s2);
     const float dx = warp_scan_f(lane < n ? c1 - c2 : 0.f, lane);
     const float dy = warp_scan_f(lane < n ? s1 - s2 : 0.f, lane);
     const float dist = warp_sum_f(lane < n ? sqrtf(fmaf(dx, dx, dy * dy)) : 0.f) * L;

@@ -6,7 +6,9 @@
 //                               (DiscreteMotionValidator.cpp:48-91), stopping at the first invalid one.
 // Interpolated joints are formed in float-float from exact splits of s1 and s2:
 //   q_i(t) = s1_i + D_i t, D_i the shortest-arc difference of KinematicChain.h:150-176 (the wrap by
-//   2*pi that interpolate applies changes no sine or cosine), t = j / nd in float-float.
+//   2*pi that interpolate applies changes no sine or cosine), t = j / nd in float-float; the link
+//   angles theta_k(t) = sum_{i<=k} q_i(t) = A_k + t S_k come from per-edge prefix sums A_k of s1 and
+//   S_k of D, so a state needs no scan of its joints.
 // Anything the FP32 error bounds leave undecided is settled with the FP64 reference-order code: an
 // ambiguous segment test (chain_round64), an undecided segment count (chain_nd64), and the states of
 // an edge whose joint difference lies within 1e-9 of pi, where the interpolation's own branch is not
@@ -171,7 +173,10 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(const __grid_
             const ff t2 = two_sum(t1.hi, sgn * (519505.0f / 268435456.0f));
             D = fast_two_sum(t2.hi, (t1.lo + t2.lo) + (diff.lo + sgn * 2.4308403e-10f));
         }
-        int nd = chain_segment_count_warp(a, b, lane, dim, L, wa.inv_lvs32, wa.e_dist, sp.factor);
+        // absolute link angles of s1 and s2 and the prefix sums of the joint differences: state t has
+        // theta_k(t) = ta_k + t * DS_k (the sum over joints of a_i + D_i t)
+        const ff ta = warp_scan_ff(a, lane), tb = warp_scan_ff(b, lane), DS = warp_scan_ff(D, lane);
+        int nd = chain_segment_count_warp(ta, tb, lane, dim, L, wa.inv_lvs32, wa.e_dist, sp.factor);
         const bool nd64 = nd < 0;
         if (nd64)
         {
@@ -192,21 +197,22 @@ __global__ void __launch_bounds__(256, 4) chain_motion_warp_kernel(const __grid_
         for (int j = 1; j <= top; ++j)
         {
             jf += 1.0f;
-            ff q;
+            ff th;  // absolute link angle of lane < dim (j == top and exact are the same in every lane)
             if (j == top)
-                q = b;
+                th = tb;
             else if (exact)
-                q = lane < dim ? split_double(motion_joint64(v1, v2, e, lane, j, nd, top)) : ff{0.f, 0.f};
+                th = warp_scan_ff(lane < dim ? split_double(motion_joint64(v1, v2, e, lane, j, nd, top)) : ff{0.f, 0.f},
+                                  lane);
             else
             {
                 const float t_hi = jf * inv_hi;
                 const float t_lo = fmaf(jf, inv_hi, -t_hi) + jf * inv_lo;
-                const float p_hi = D.hi * t_hi;
-                const float p_lo = fmaf(D.hi, t_hi, -p_hi) + fmaf(D.hi, t_lo, D.lo * t_hi);
-                q = lane < dim ? ff_add(a, {p_hi, p_lo}) : ff{0.f, 0.f};
+                const float p_hi = DS.hi * t_hi;
+                const float p_lo = fmaf(DS.hi, t_hi, -p_hi) + fmaf(DS.hi, t_lo, DS.lo * t_hi);
+                th = ff_add(ta, {p_hi, p_lo});
             }
             float vx, vy, px, py;
-            chain_segments32(q, lane, dim, L, vx, vy, px, py);
+            chain_segments32_theta(th, lane, dim, L, vx, vy, px, py);
             auto q64 = [&](int ln) { return ln < dim ? motion_joint64(v1, v2, e, ln, j, nd, top) : 0.0; };
             const int r = chain_state_warp32(lane, dim, L64, vx, vy, px, py, cs.w32, cs.nw, cs.lb, w64, cs.tab, cs.t, q64,
                                              rechecks);
