@@ -335,6 +335,23 @@ def ours(args, rank, world, local_rank):
     knn_qps = KNN_QUERIES / (k0.elapsed_time(k1) * 1e-3)
     knn_stats = nn.stats()
 
+    # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them
+    smp = B.StateSampler(space, 5)
+    smp.sampleUniform(1000, host=False)
+    smp.sampleGaussian(torch.zeros((1000, w.dim), dtype=torch.float64, device=dev), 0.1)
+    torch.cuda.synchronize()
+    s0, s1e, s2e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    s0.record()
+    means = smp.sampleUniform(N_STATES, host=False)
+    s1e.record()
+    smp.sampleGaussian(means, 0.1)
+    s2e.record()
+    torch.cuda.synchronize()
+    sampling = {"states": N_STATES, "dim": w.dim,
+                "uniform_states_per_s": N_STATES / (s0.elapsed_time(s1e) * 1e-3),
+                "gaussian_states_per_s": N_STATES / (s1e.elapsed_time(s2e) * 1e-3)}
+    del means
+
     if rank != 0:
         return
     peak_fp32 = B.measure_fp32_peak()
@@ -384,6 +401,7 @@ def ours(args, rank, world, local_rank):
         "states_per_s": states_per_s,
         "knn_queries_per_s": knn_qps,
         "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},
+        "sampling": sampling,
         "recheck": stats,
         "clocks": clocks,
     }
