@@ -1595,10 +1595,12 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         const int P = knn_chunks(lc, nq, nn->size);
         const int keep = knn_keep(k);
         const size_t pl = (size_t)P * nq * keep;
-        if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + 64, lc.stream))
+        if (auto st = nn->part.reserve(pl * (sizeof(float) + sizeof(int64_t)) + (size_t)nq * sizeof(unsigned) + 64,
+                                       lc.stream))
             return st;
         int64_t *part_k = (int64_t *)nn->part.p;
         float *part_d = (float *)(part_k + pl);
+        unsigned *thr = (unsigned *)(part_d + pl);  // per-query bound shared by the chunks of the FP32 scan
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
         // large batches over a large RealVector / wrapped index: cell index (PRM's prefix kNN)
         if ((nn->sp.kind == GBO_SPACE_WRAP_L2 || nn->sp.kind == GBO_SPACE_REAL_VECTOR) && nn->sp.dim <= 8 &&
@@ -1645,7 +1647,7 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
             order = ord;
         }
         if (launch_knn_fp32(lc, a, nn->sp, qv, (const float *)nn->qfeat.p, nq, k, prefix, idx, dist,
-                            (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P, order))
+                            (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P, order, thr))
         {
             // queries whose FP32 band overflowed: exact FP64 scan (count read on the device)
             launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist, (const unsigned long long *)nn->fb_list.p,

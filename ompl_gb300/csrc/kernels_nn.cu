@@ -209,11 +209,16 @@ __device__ __forceinline__ float chain_dist32(const float *a, const float *b, in
 // prune the same elements); its list is kept at position qs.
 // qkey (nullable): only the queries with qkey < key_limit are this launch's (the others' lists are
 // written by the cell kernel).
+// thr (nullable): per query position, the smallest K_KEEP-th distance any chunk has reached so far
+// (float bits; non-negative floats order like their bits). Every chunk's list is an upper bound on the
+// query's K_KEEP-th smallest distance, so each CTA prunes against the smallest one published, reading
+// and publishing it once per tile. An element dropped that way is beyond the merged list's last entry,
+// which the finish kernel's overflow test already treats as possibly dropped.
 template <int KIND, int MAXF, int K_KEEP>
 __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp, const float *qf, int64_t nq,
                                                        const int64_t *prefix, int64_t chunk, float *part_d,
                                                        int64_t *part_k, const int64_t *qorder, const int *qkey,
-                                                       int key_limit)
+                                                       int key_limit, unsigned *thr)
 {
     constexpr int TILE = 128;
     constexpr int FP = (MAXF + 3) / 4 * 4;
@@ -250,6 +255,7 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
         ik[j] = -1;
     }
     const float lscale = KIND == GBO_SPACE_KINEMATIC_CHAIN ? 0.70710678f * (1.0f - 1e-5f) * (float)sp.link : 1.0f;
+    float g = __int_as_float(0x7f800000);  // the shared bound last read
     for (int64_t base = c0; base < block_end; base += TILE)
     {
         __syncthreads();
@@ -264,6 +270,9 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
         __syncthreads();
         if (!active)
             continue;
+        if (thr)
+            g = __uint_as_float(__ldcg(thr + qs));
+        float cut = fminf(dk[K_KEEP - 1], g);
         const int tn = (int)max((int64_t)0, min((int64_t)TILE, limit - base));
         for (int t = 0; t < tn; ++t)
         {
@@ -285,18 +294,23 @@ __global__ void __launch_bounds__(128) knn_scan_kernel(NNArgs nn, SpaceParams sp
                 // outer links first: their terms are the largest, so most elements stop here
                 const int half = sp.dim >> 1;
                 float lb = chain_l1<MAXF>(pf, qfe, sp.dim, half, sp.dim);
-                if (lb * lscale >= dk[K_KEEP - 1])
+                if (lb * lscale >= cut)
                     continue;
                 lb += chain_l1<MAXF>(pf, qfe, sp.dim, 0, half);
-                if (lb * lscale >= dk[K_KEEP - 1])
+                if (lb * lscale >= cut)
                     continue;
                 d = chain_dist32<MAXF>(pf, qfe, sp.dim) * (float)sp.link;
             }
             else
                 d = box_dist2<KIND, MAXF>(pf, qfe, sp.dim);
-            if (d < dk[K_KEEP - 1])
+            if (d < cut)
+            {
                 topk_insert<K_KEEP>(dk, ik, d, (int)(base + t));
+                cut = fminf(cut, dk[K_KEEP - 1]);
+            }
         }
+        if (thr && dk[K_KEEP - 1] < g)
+            atomicMin(thr + qs, __float_as_uint(dk[K_KEEP - 1]));
     }
     if (!active)
         return;
@@ -570,11 +584,14 @@ template <int KIND, int MAXD, int MAXF, int K_KEEP>
 static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                           int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist,
                           unsigned long long *fb_list, unsigned long long *fb_n, RunCounters *ctr, float *part_d,
-                          int64_t *part_k, int P, int64_t chunk, const int64_t *qorder)
+                          int64_t *part_k, int P, int64_t chunk, const int64_t *qorder, unsigned *thr)
 {
     const int qb = (int)((nq + 127) / 128);
+    if (thr && P > 1)
+        cudaMemsetAsync(thr, 0x7f, (size_t)nq * sizeof(unsigned), lc.stream);  // 3.4e38: no bound yet
     knn_scan_kernel<KIND, MAXF, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix, chunk, part_d,
-                                                                           part_k, qorder, nullptr, 0);
+                                                                           part_k, qorder, nullptr, 0,
+                                                                           P > 1 ? thr : nullptr);
     knn_finish_kernel<KIND, MAXD, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,
                                                                     fb_list, fb_n, ctr, qorder);
     note_launch();
@@ -602,14 +619,14 @@ int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size)
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
-                     const int64_t *qorder)
+                     const int64_t *qorder, unsigned *thr)
 {
     if (nq == 0 || k > knn_fp32_max_k(sp))
         return false;
     const int64_t chunk = (nn.size + P - 1) / P;
 #define GBO_FP32(KIND, MAXD, MAXF, KK)                                                                                 \
     launch_fp32_t<KIND, MAXD, MAXF, KK>(lc, nn, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr, part_d,     \
-                                        part_k, P, chunk, qorder)
+                                        part_k, P, chunk, qorder, thr)
 #define GBO_FP32_K(KIND, MAXD, MAXF)                                                                                   \
     do                                                                                                                \
     {                                                                                                                 \
@@ -1121,7 +1138,7 @@ static void launch_bcell_t(const LaunchCfg &lc, const NNArgs &nn, const BoxCellA
         // band 0 (limits below a quarter of the index) through the prefix scan, same P lists
         knn_scan_kernel<KIND, 8, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(nn, sp, qf, nq, prefix,
                                                                             (nn.size + P - 1) / P, part_d, part_k,
-                                                                            qorder, qcell, ci.C);
+                                                                            qorder, qcell, ci.C, nullptr);
         note_launch();
     }
     knn_finish_kernel<KIND, 8, K_KEEP><<<qb, 128, 0, lc.stream>>>(nn, sp, qv, nq, k, P, part_d, part_k, idx, dist,

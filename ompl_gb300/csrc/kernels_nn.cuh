@@ -21,7 +21,7 @@ void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &
 bool launch_knn_fp32(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                      int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P,
-                     const int64_t *qorder);
+                     const int64_t *qorder, unsigned *thr);
 // Cell index of a RealVector / wrapped nearest-neighbour index (large batches, PRM prefix kNN).
 struct BoxCellArgs
 {

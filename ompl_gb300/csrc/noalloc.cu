@@ -119,7 +119,8 @@ extern "C" gbo_status gbo_nn_nearest_k_noalloc(gbo_nn *nn, const double *q, int6
         return internal_fail(GBO_ERR_CUDA, "clearing the no-alloc counters failed");
     unsigned long long *fb_n = &ctr->queue;
     launch_features(lc, sp, qv, nq, qf, nq);
-    launch_knn_fp32(lc, a, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr, part_d, part_k, P, nullptr);
+    launch_knn_fp32(lc, a, sp, qv, qf, nq, k, prefix, idx, dist, fb_list, fb_n, ctr, part_d, part_k, P, nullptr,
+                    nullptr);
     launch_knn_exact(lc, a, sp, qv, nq, k, prefix, idx, dist, fb_list, fb_n, nq < 4096 ? nq : 4096);
     return cudaGetLastError() == cudaSuccess ? GBO_OK : internal_fail(GBO_ERR_CUDA, "kernel launch failed");
 }
