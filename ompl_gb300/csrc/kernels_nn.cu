@@ -791,11 +791,11 @@ void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float 
 // Large batches over a large RealVector / wrapped index (PRM's prefix kNN): the alive elements are
 // bucketed by a uniform grid of L levels per coordinate (counting sort); each cell keeps its elements'
 // FP32 coordinates (two float4 per element, sorted by cell) and their bounding box. Queries are
-// processed in (band of their prefix limit, cell) order, one warp per 32 of them: each lane seeds its
-// threshold T with the k-th FP32 distance among the eligible elements of its own cell (an upper bound on
-// its k-th overall), and the warp skips a cell when, for every lane, the distance from the query to the
-// cell's box is at least min(T, the lane's current K_KEEP-th). Elements beyond T are left out of the
-// lists; the FP64 band of the finish kernel lies below T, so its decisions are unchanged.
+// processed in (band of their prefix limit, cell) order: each query seeds its threshold T with the k-th
+// FP32 distance among the eligible elements of its own cell (an upper bound on its k-th overall), and
+// skips a cell when the distance from the query to the cell's box is at least min(T, its current
+// K_KEEP-th). Elements beyond T are left out of the lists; the FP64 band of the finish kernel lies
+// below T, so its decisions are unchanged.
 
 __device__ __forceinline__ void bcell_range(const SpaceParams &sp, int d, float &lo, float &hi)
 {
@@ -988,88 +988,111 @@ __device__ __forceinline__ float bcell_lb(const float4 *b, const float *q, int d
     return s * (1.0f - 1e-5f);
 }
 
-template <int KIND, int MAXF, int K_KEEP>
-__global__ void __launch_bounds__(128) knn_bcell_kernel(BoxCellArgs ci, SpaceParams sp, float eps, const float *qf,
-                                                        int64_t nq, const int64_t *qorder, const int *qcell,
-                                                        const int64_t *prefix, int k, int cells_per_chunk,
-                                                        float *part_d, int64_t *part_k)
+// Cell search, one warp per query: the 32 lanes test 32 cells' boxes at a time and evaluate a needed
+// cell's elements 32 at a time, so a warp visits only the cells its own query needs (a lane-per-query
+// form, where a warp's 32 queries visit the union of their cells, kept about 10 of 32 lanes busy). The kept list (K_KEEP <= 32 entries,
+// ascending) is spread over the lanes: lane j holds entry j. Seed and thresholds as above: the own
+// cell first, T from its k-th distance, then every other cell whose box is nearer than min(T, the
+// list's last entry). One list per query (P = 1).
+template <int K_KEEP>
+__device__ __forceinline__ void warp_list_insert(float &ld, int &lk, float d, int key, int lane)
 {
-    const int64_t qs = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t qi = qs < nq ? qorder[qs] : 0;
-    // with prefix limits, band 0 (key < C) belongs to the prefix scan
-    const bool active = qs < nq && (!prefix || qcell[qi] >= ci.C);
+    // position = number of entries that stay before (d, key): smaller distance, or equal and kept
+    // earlier (entries are appended in visiting order)
+    const unsigned before = __ballot_sync(0xffffffffu, lane < K_KEEP && ld <= d);
+    const int pos = __popc(before);
+    const float up_d = __shfl_up_sync(0xffffffffu, ld, 1);
+    const int up_k = __shfl_up_sync(0xffffffffu, lk, 1);
+    if (pos < K_KEEP && lane >= pos && lane < K_KEEP)
+    {
+        ld = lane == pos ? d : up_d;
+        lk = lane == pos ? key : up_k;
+    }
+}
+
+template <int KIND, int K_KEEP>
+__global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, SpaceParams sp, float eps,
+                                                             const float *qf, int64_t nq, const int64_t *qorder,
+                                                             const int *qcell, const int64_t *prefix, int k,
+                                                             float *part_d, int64_t *part_k)
+{
+    static_assert(K_KEEP <= 32, "the kept list lives in the lanes of one warp");
+    const int lane = threadIdx.x & 31;
+    const int64_t qs = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (qs >= nq)
+        return;
+    const int64_t qi = qorder[qs];
+    if (prefix && qcell[qi] < ci.C)
+        return;  // band 0 belongs to the prefix scan
     float qfe[8];
 #pragma unroll
     for (int f = 0; f < 8; ++f)
-        qfe[f] = (active && f < sp.dim) ? qf[(int64_t)f * nq + qi] : 0.f;
-    const int64_t limit = active ? (prefix ? prefix[qi] : INT64_MAX) : 0;
-    float dk[K_KEEP];
-    int ik[K_KEEP];
-#pragma unroll
-    for (int j = 0; j < K_KEEP; ++j)
-    {
-        dk[j] = __int_as_float(0x7f800000);
-        ik[j] = -1;
-    }
-    auto dist = [&](int64_t p) {
-        const float4 a = ci.pts8[2 * p], b = ci.pts8[2 * p + 1];
-        const float pf[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        return box_dist2<KIND, MAXF>(pf, qfe, sp.dim);
-    };
-    // seed: the k-th distance among the eligible elements of the query's own cell
-    float T = __int_as_float(0x7f800000);
-    if (active)
-    {
-        const int oc = qcell[qi] % ci.C;  // the query key is band * C + cell
-        for (int p = ci.start[oc]; p < ci.start[oc + 1]; ++p)
-        {
-            if (ci.skey[p] >= limit)
-                continue;  // not yet in the roadmap (PRM prefix)
-            const float d = dist(p);
-            if (d < dk[k - 1])
-                topk_insert<K_KEEP>(dk, ik, d, p);
-        }
-        if (dk[k - 1] < __int_as_float(0x7f800000))
-        {
-            const float r = sqrtf(dk[k - 1]) + 2.f * eps;
-            T = r * r * (1.0f + 1e-5f);
-        }
-#pragma unroll
-        for (int j = 0; j < K_KEEP; ++j)
-        {
-            dk[j] = __int_as_float(0x7f800000);
-            ik[j] = -1;
-        }
-    }
-    const int c0 = blockIdx.y * cells_per_chunk, c1 = min(c0 + cells_per_chunk, ci.C);
-    for (int c = c0; c < c1; ++c)
-    {
+        qfe[f] = f < sp.dim ? qf[(int64_t)f * nq + qi] : 0.f;
+    const int64_t limit = prefix ? prefix[qi] : INT64_MAX;
+    float ld = __int_as_float(0x7f800000);
+    int lk = -1;
+    // one cell's eligible elements, 32 at a time; candidates below `cut` enter the list in lane order
+    auto scan_cell = [&](int c, float T) {
         const int s0 = ci.start[c], s1 = ci.start[c + 1];
-        if (s0 == s1)
-            continue;
-        const bool need = active && bcell_lb<KIND, MAXF>(ci.box + 4 * (int64_t)c, qfe, sp.dim) < fminf(T, dk[K_KEEP - 1]);
-        if (!__any_sync(0xffffffffu, need))
-            continue;
-        if (!need)
-            continue;
-        for (int p = s0; p < s1; ++p)
+        for (int p0 = s0; p0 < s1; p0 += 32)
         {
-            const int64_t key = ci.skey[p];
-            if (key >= limit)
-                continue;
-            const float d = dist(p);
-            if (d < dk[K_KEEP - 1] && d <= T)
-                topk_insert<K_KEEP>(dk, ik, d, (int)key);
+            const int p = p0 + lane;
+            float d = __int_as_float(0x7f800000);
+            int key = -1;
+            if (p < s1)
+            {
+                const int64_t kk = ci.skey[p];
+                if (kk < limit)
+                {
+                    const float4 a = ci.pts8[2 * (int64_t)p], b = ci.pts8[2 * (int64_t)p + 1];
+                    const float pf[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+                    d = box_dist2<KIND, 8>(pf, qfe, sp.dim);
+                    key = (int)kk;
+                }
+            }
+            const float last = __shfl_sync(0xffffffffu, ld, K_KEEP - 1);
+            unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
+            while (m)
+            {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const float dc = __shfl_sync(0xffffffffu, d, src);
+                const int kc = __shfl_sync(0xffffffffu, key, src);
+                if (dc < __shfl_sync(0xffffffffu, ld, K_KEEP - 1))
+                    warp_list_insert<K_KEEP>(ld, lk, dc, kc, lane);
+            }
+        }
+    };
+    // seed: the query's own cell, then T from its k-th distance
+    const int oc = qcell[qi] % ci.C;  // the query key is band * C + cell
+    scan_cell(oc, __int_as_float(0x7f800000));
+    float T = __int_as_float(0x7f800000);
+    const float dkk = __shfl_sync(0xffffffffu, ld, k - 1);
+    if (dkk < __int_as_float(0x7f800000))
+    {
+        const float r = sqrtf(dkk) + 2.f * eps;
+        T = r * r * (1.0f + 1e-5f);
+    }
+    for (int cb = 0; cb < ci.C; cb += 32)
+    {
+        const int c = cb + lane;
+        float lb = __int_as_float(0x7f800000);
+        if (c < ci.C && c != oc && ci.start[c] != ci.start[c + 1])
+            lb = bcell_lb<KIND, 8>(ci.box + 4 * (int64_t)c, qfe, sp.dim);
+        unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, __shfl_sync(0xffffffffu, ld, K_KEEP - 1)));
+        while (m)
+        {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            // the list may have tightened since the cells were tested
+            if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, __shfl_sync(0xffffffffu, ld, K_KEEP - 1)))
+                scan_cell(cb + src, T);
         }
     }
-    if (!active)
-        return;
-    const int64_t o = ((int64_t)blockIdx.y * nq + qs) * K_KEEP;
-#pragma unroll
-    for (int j = 0; j < K_KEEP; ++j)
+    if (lane < K_KEEP)
     {
-        part_d[o + j] = dk[j];
-        part_k[o + j] = ik[j];
+        part_d[qs * K_KEEP + lane] = ld;
+        part_k[qs * K_KEEP + lane] = lk;
     }
 }
 
@@ -1130,9 +1153,9 @@ static void launch_bcell_t(const LaunchCfg &lc, const NNArgs &nn, const BoxCellA
                            unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
 {
     const int qb = (int)((nq + 127) / 128);
-    const int per = (ci.C + P - 1) / P;
-    knn_bcell_kernel<KIND, 8, K_KEEP><<<dim3(qb, P), 128, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qcell,
-                                                                         prefix, k, per, part_d, part_k);
+    P = 1;  // one list per query: the warp kernel visits every cell a query needs
+    knn_bcell_warp_kernel<KIND, K_KEEP><<<(int)((nq * 32 + 255) / 256), 256, 0, lc.stream>>>(
+        ci, sp, nn.eps32, qf, nq, qorder, qcell, prefix, k, part_d, part_k);
     if (prefix)
     {
         // band 0 (limits below a quarter of the index) through the prefix scan, same P lists
