@@ -990,25 +990,78 @@ __device__ __forceinline__ float bcell_lb(const float4 *b, const float *q, int d
 
 // Cell search, one warp per query: the 32 lanes test 32 cells' boxes at a time and evaluate a needed
 // cell's elements 32 at a time, so a warp visits only the cells its own query needs (a lane-per-query
-// form, where a warp's 32 queries visit the union of their cells, kept about 10 of 32 lanes busy). The kept list (K_KEEP <= 32 entries,
-// ascending) is spread over the lanes: lane j holds entry j. Seed and thresholds as above: the own
-// cell first, T from its k-th distance, then every other cell whose box is nearer than min(T, the
-// list's last entry). One list per query (P = 1).
+// form, where a warp's 32 queries visit the union of their cells, kept about 10 of 32 lanes busy). The
+// kept list is spread over the lanes (WarpList). Seed and thresholds as above: the own cell first, T
+// from its k-th distance, then every other cell whose box is nearer than min(T, the list's last entry).
+// One list per query (P = 1).
+// The kept list spread over a warp: entry j = 32 s + lane in slot s of the lane (S = K_KEEP / 32
+// rounded up slots), ascending, unused entries +inf / -1.
 template <int K_KEEP>
-__device__ __forceinline__ void warp_list_insert(float &ld, int &lk, float d, int key, int lane)
+struct WarpList
 {
-    // position = number of entries that stay before (d, key): smaller distance, or equal and kept
-    // earlier (entries are appended in visiting order)
-    const unsigned before = __ballot_sync(0xffffffffu, lane < K_KEEP && ld <= d);
-    const int pos = __popc(before);
-    const float up_d = __shfl_up_sync(0xffffffffu, ld, 1);
-    const int up_k = __shfl_up_sync(0xffffffffu, lk, 1);
-    if (pos < K_KEEP && lane >= pos && lane < K_KEEP)
+    static constexpr int S = (K_KEEP + 31) / 32;
+    float d[S];
+    int k[S];
+    __device__ __forceinline__ void init()
     {
-        ld = lane == pos ? d : up_d;
-        lk = lane == pos ? key : up_k;
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            d[s] = __int_as_float(0x7f800000);
+            k[s] = -1;
+        }
     }
-}
+    // entry j of the list, in every lane
+    __device__ __forceinline__ float at(int j) const
+    {
+        float v = d[0];
+#pragma unroll
+        for (int s = 1; s < S; ++s)
+            if (j >> 5 == s)
+                v = d[s];
+        return __shfl_sync(0xffffffffu, v, j & 31);
+    }
+    __device__ __forceinline__ float last() const { return at(K_KEEP - 1); }
+    // inserts (dd, kk) after the entries with a distance <= dd (those kept earlier stay first)
+    __device__ __forceinline__ void insert(float dd, int kk, int lane)
+    {
+        int pos = 0;
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+            pos += __popc(__ballot_sync(0xffffffffu, 32 * s + lane < K_KEEP && d[s] <= dd));
+        if (pos >= K_KEEP)
+            return;
+        float up_d[S];
+        int up_k[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            up_d[s] = __shfl_up_sync(0xffffffffu, d[s], 1);
+            up_k[s] = __shfl_up_sync(0xffffffffu, k[s], 1);
+            if (s > 0)
+            {
+                // lane 0 of slot s takes entry 32 s - 1: lane 31 of slot s - 1
+                const float cd = __shfl_sync(0xffffffffu, d[s - 1], 31);
+                const int ck = __shfl_sync(0xffffffffu, k[s - 1], 31);
+                if (lane == 0)
+                {
+                    up_d[s] = cd;
+                    up_k[s] = ck;
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+        {
+            const int j = 32 * s + lane;
+            if (j >= pos && j < K_KEEP)
+            {
+                d[s] = j == pos ? dd : up_d[s];
+                k[s] = j == pos ? kk : up_k[s];
+            }
+        }
+    }
+};
 
 template <int KIND, int K_KEEP>
 __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, SpaceParams sp, float eps,
@@ -1016,7 +1069,6 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
                                                              const int *qcell, const int64_t *prefix, int k,
                                                              float *part_d, int64_t *part_k)
 {
-    static_assert(K_KEEP <= 32, "the kept list lives in the lanes of one warp");
     const int lane = threadIdx.x & 31;
     const int64_t qs = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (qs >= nq)
@@ -1029,8 +1081,8 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
     for (int f = 0; f < 8; ++f)
         qfe[f] = f < sp.dim ? qf[(int64_t)f * nq + qi] : 0.f;
     const int64_t limit = prefix ? prefix[qi] : INT64_MAX;
-    float ld = __int_as_float(0x7f800000);
-    int lk = -1;
+    WarpList<K_KEEP> L;
+    L.init();
     // one cell's eligible elements, 32 at a time; candidates below `cut` enter the list in lane order
     auto scan_cell = [&](int c, float T) {
         const int s0 = ci.start[c], s1 = ci.start[c + 1];
@@ -1050,7 +1102,7 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
                     key = (int)kk;
                 }
             }
-            const float last = __shfl_sync(0xffffffffu, ld, K_KEEP - 1);
+            const float last = L.last();
             unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
             while (m)
             {
@@ -1058,8 +1110,8 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
                 m &= m - 1;
                 const float dc = __shfl_sync(0xffffffffu, d, src);
                 const int kc = __shfl_sync(0xffffffffu, key, src);
-                if (dc < __shfl_sync(0xffffffffu, ld, K_KEEP - 1))
-                    warp_list_insert<K_KEEP>(ld, lk, dc, kc, lane);
+                if (dc < L.last())
+                    L.insert(dc, kc, lane);
             }
         }
     };
@@ -1067,7 +1119,7 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
     const int oc = qcell[qi] % ci.C;  // the query key is band * C + cell
     scan_cell(oc, __int_as_float(0x7f800000));
     float T = __int_as_float(0x7f800000);
-    const float dkk = __shfl_sync(0xffffffffu, ld, k - 1);
+    const float dkk = L.at(k - 1);
     if (dkk < __int_as_float(0x7f800000))
     {
         const float r = sqrtf(dkk) + 2.f * eps;
@@ -1079,21 +1131,23 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
         float lb = __int_as_float(0x7f800000);
         if (c < ci.C && c != oc && ci.start[c] != ci.start[c + 1])
             lb = bcell_lb<KIND, 8>(ci.box + 4 * (int64_t)c, qfe, sp.dim);
-        unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, __shfl_sync(0xffffffffu, ld, K_KEEP - 1)));
+        unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
         {
             const int src = __ffs(m) - 1;
             m &= m - 1;
             // the list may have tightened since the cells were tested
-            if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, __shfl_sync(0xffffffffu, ld, K_KEEP - 1)))
+            if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
                 scan_cell(cb + src, T);
         }
     }
-    if (lane < K_KEEP)
-    {
-        part_d[qs * K_KEEP + lane] = ld;
-        part_k[qs * K_KEEP + lane] = lk;
-    }
+#pragma unroll
+    for (int s = 0; s < WarpList<K_KEEP>::S; ++s)
+        if (32 * s + lane < K_KEEP)
+        {
+            part_d[qs * K_KEEP + 32 * s + lane] = L.d[s];
+            part_k[qs * K_KEEP + 32 * s + lane] = L.k[s];
+        }
 }
 
 int bcell_levels(int dim, int64_t n)
@@ -1175,17 +1229,22 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
                       const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
                       unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
 {
-    if (nq == 0 || sp.dim > 8 || k > 20)  // longer kept lists do not fit the cell kernel's registers
+    if (nq == 0 || sp.dim > 8 || k > knn_fp32_max_k(sp))
         return false;
+#define GBO_BCELL_T(KIND, KK)                                                                                         \
+    launch_bcell_t<KIND, KK>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
+                             part_d, part_k, P)
 #define GBO_BCELL(KIND)                                                                                                \
     do                                                                                                                \
     {                                                                                                                 \
         if (k <= 12)                                                                                                  \
-            launch_bcell_t<KIND, 16>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, \
-                                     ctr, part_d, part_k, P);                                                         \
+            GBO_BCELL_T(KIND, 16);                                                                                    \
+        else if (k <= 20)                                                                                             \
+            GBO_BCELL_T(KIND, 24);                                                                                    \
+        else if (k <= 40)                                                                                             \
+            GBO_BCELL_T(KIND, 48);                                                                                    \
         else                                                                                                          \
-            launch_bcell_t<KIND, 24>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, \
-                                     ctr, part_d, part_k, P);                                                         \
+            GBO_BCELL_T(KIND, 72);                                                                                    \
     } while (0)
     if (sp.kind == GBO_SPACE_WRAP_L2)
         GBO_BCELL(GBO_SPACE_WRAP_L2);
@@ -1193,6 +1252,7 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
         GBO_BCELL(GBO_SPACE_REAL_VECTOR);
     else
         return false;
+#undef GBO_BCELL_T
 #undef GBO_BCELL
     return true;
 }
