@@ -940,20 +940,24 @@ __global__ void bcell_box_kernel(const float4 *pts8, const int *start, int C, fl
 
 // query key: band then cell. Without prefix limits one band. With them, band 0 holds the queries whose
 // limit is below a quarter of the index (left to the prefix scan: few eligible elements, no useful
-// threshold), bands 1 .. bands - 1 split the rest evenly.
+// threshold; keyed by limit), bands 1 .. bands - 1 split the rest evenly.
 __global__ void bcell_query_key_kernel(SpaceParams sp, int L, int C, const float *qf, int64_t nq,
                                        const int64_t *prefix, int64_t index_n, int bands, int *key, int *count)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
     {
-        int band = 0;
+        int band = 0, c;
         if (prefix && bands > 1)
         {
             const int64_t lim = prefix[i] < 0 ? 0 : (prefix[i] > index_n ? index_n : prefix[i]);
             const int64_t q4 = index_n / 4, rest = index_n - q4;
             band = lim < q4 ? 0 : 1 + (int)min((int64_t)bands - 2, (lim - q4) * (bands - 1) / (rest > 0 ? rest : 1));
+            // band 0 goes to the prefix scan, whose CTAs scan up to their largest limit: its queries are
+            // ordered by limit (C buckets), so that a CTA's limits are close
+            c = band == 0 ? (int)min((int64_t)C - 1, lim * C / (q4 > 0 ? q4 : 1)) : band * C + bcell_of(sp, L, qf, nq, i);
         }
-        const int c = band * C + bcell_of(sp, L, qf, nq, i);
+        else
+            c = bcell_of(sp, L, qf, nq, i);
         key[i] = c;
         atomicAdd(&count[c], 1);
     }
