@@ -940,7 +940,7 @@ __global__ void bcell_box_kernel(const float4 *pts8, const int *start, int C, fl
 
 // query key: band then cell. Without prefix limits one band. With them, band 0 holds the queries whose
 // limit is below a quarter of the index (left to the prefix scan: few eligible elements, no useful
-// threshold; keyed by limit), bands 1 .. bands - 1 split the rest evenly.
+// threshold; keyed by decreasing limit), bands 1 .. bands - 1 split the rest evenly.
 __global__ void bcell_query_key_kernel(SpaceParams sp, int L, int C, const float *qf, int64_t nq,
                                        const int64_t *prefix, int64_t index_n, int bands, int *key, int *count)
 {
@@ -953,8 +953,10 @@ __global__ void bcell_query_key_kernel(SpaceParams sp, int L, int C, const float
             const int64_t q4 = index_n / 4, rest = index_n - q4;
             band = lim < q4 ? 0 : 1 + (int)min((int64_t)bands - 2, (lim - q4) * (bands - 1) / (rest > 0 ? rest : 1));
             // band 0 goes to the prefix scan, whose CTAs scan up to their largest limit: its queries are
-            // ordered by limit (C buckets), so that a CTA's limits are close
-            c = band == 0 ? (int)min((int64_t)C - 1, lim * C / (q4 > 0 ? q4 : 1)) : band * C + bcell_of(sp, L, qf, nq, i);
+            // ordered by decreasing limit (C buckets), so that a CTA's limits are close and the longest
+            // CTAs start first
+            c = band == 0 ? (C - 1) - (int)min((int64_t)C - 1, lim * C / (q4 > 0 ? q4 : 1))
+                          : band * C + bcell_of(sp, L, qf, nq, i);
         }
         else
             c = bcell_of(sp, L, qf, nq, i);
