@@ -256,6 +256,13 @@ struct NNBoxCells
     DevBuf qcell, qcount, qstart, qfill, qorder;
 };
 
+// Cell index of a kinematic-chain gbo_nn (kernels_nn.cu), built like NNBoxCells.
+struct NNChainCells
+{
+    bool valid = false;
+    DevBuf key, count, start, fill, skey, sfeat, box;
+};
+
 struct gbo_nn
 {
     SpaceParams sp{};
@@ -267,6 +274,7 @@ struct gbo_nn
     unsigned char *alive = nullptr;
     float eps32 = 0.f;
     NNBoxCells cells;
+    NNChainCells ccells;
     DevBuf qfeat, fb_list, part, qorder;
     CounterRing ctr;
     unsigned long long queries = 0;
@@ -1487,6 +1495,7 @@ gbo_status gbo_nn_add(gbo_nn *nn, const double *states, int64_t n, int64_t ld, i
     nn->size += n;
     nn->alive_count += n;
     nn->cells.valid = false;
+    nn->ccells.valid = false;
     return GBO_OK;
 }
 
@@ -1498,6 +1507,7 @@ gbo_status gbo_nn_remove(gbo_nn *nn, const int64_t *keys, int64_t n, gbo_stream 
     CHECK_LAUNCH();
     nn->alive_count = -1;  // recounted on demand
     nn->cells.valid = false;
+    nn->ccells.valid = false;
     return GBO_OK;
 }
 
@@ -1510,6 +1520,7 @@ gbo_status gbo_nn_clear(gbo_nn *nn)
     nn->size = 0;
     nn->alive_count = 0;
     nn->cells.valid = false;
+    nn->ccells.valid = false;
     return GBO_OK;
 }
 
@@ -1565,6 +1576,26 @@ static gbo_status ensure_box_cells(gbo_nn *nn, const LaunchCfg &lc)
             return r;
     launch_bcell_build(lc, nn_args(nn), nn->sp, c.L, c.C, (int *)c.cell.p, (int *)c.count.p, (int *)c.start.p,
                        (int *)c.fill.p, (int64_t *)c.skey.p, (float4 *)c.pts8.p, (float4 *)c.box.p);
+    CHECK_LAUNCH();
+    c.valid = true;
+    return GBO_OK;
+}
+
+static gbo_status ensure_chain_cells(gbo_nn *nn, const LaunchCfg &lc)
+{
+    NNChainCells &c = nn->ccells;
+    if (c.valid)
+        return GBO_OK;
+    const int64_t n = std::max<int64_t>(nn->size, 1);
+    const cudaStream_t s = lc.stream;
+    for (auto r : {c.key.reserve((size_t)n * sizeof(int), s), c.count.reserve(kQueryKeys * sizeof(int), s),
+                   c.start.reserve(kQueryKeys * sizeof(int), s), c.fill.reserve(kQueryKeys * sizeof(int), s),
+                   c.skey.reserve((size_t)n * sizeof(int64_t), s), c.sfeat.reserve((size_t)n * 5 * sizeof(float4), s),
+                   c.box.reserve((size_t)kQueryKeys * 10 * sizeof(float4), s)})
+        if (r)
+            return r;
+    launch_ccell_build(lc, nn_args(nn), nn->sp, (int *)c.key.p, (int *)c.count.p, (int *)c.start.p, (int *)c.fill.p,
+                       (int64_t *)c.skey.p, (float4 *)c.sfeat.p, (float4 *)c.box.p);
     CHECK_LAUNCH();
     c.valid = true;
     return GBO_OK;
@@ -1645,6 +1676,26 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
             int64_t *ord = (int64_t *)((char *)nn->qorder.p + pad16(wb));
             launch_query_order(lc, nn->sp, (const float *)nn->qfeat.p, nq, work, ord);
             order = ord;
+            // a large chain index: the cell search, one warp per query (the query order's keys are the
+            // cells)
+            if (nn->sp.kind == GBO_SPACE_KINEMATIC_CHAIN && nn->sp.dim <= 10 && k <= 20 && nn->size >= 65536 &&
+                nn->size < (1ll << 31))
+            {
+                if (auto st = ensure_chain_cells(nn, lc))
+                    return st;
+                NNChainCells &c = nn->ccells;
+                const ChainCellArgs ci{(const int *)c.start.p, (const int *)c.count.p, (const int64_t *)c.skey.p,
+                                       (const float4 *)c.sfeat.p, (const float4 *)c.box.p};
+                if (launch_knn_ccell(lc, a, ci, nn->sp, qv, (const float *)nn->qfeat.p, nq, ord,
+                                     work + 3 * kQueryKeys, k, idx, dist, (unsigned long long *)nn->fb_list.p, fb_n,
+                                     ctr, part_d, part_k))
+                {
+                    launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist,
+                                     (const unsigned long long *)nn->fb_list.p, fb_n, std::min<int64_t>(nq, 4096));
+                    CHECK_LAUNCH();
+                    return GBO_OK;
+                }
+            }
         }
         if (launch_knn_fp32(lc, a, nn->sp, qv, (const float *)nn->qfeat.p, nq, k, prefix, idx, dist,
                             (unsigned long long *)nn->fb_list.p, fb_n, ctr, part_d, part_k, P, order, thr))

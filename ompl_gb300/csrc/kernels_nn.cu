@@ -708,35 +708,49 @@ __device__ __forceinline__ int query_level(float v, float lo, float hi)
     return l < 0 ? 0 : (l > 7 ? 7 : l);
 }
 
-__global__ void query_key_kernel(SpaceParams sp, const float *qf, int64_t nq, int *key, int *count)
+// Key of row i of SoA features f (row stride ld).
+__device__ __forceinline__ int order_key(const SpaceParams &sp, const float *f, int64_t ld, int64_t i)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
+    int c = 0;
+    if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN)
     {
-        int c = 0;
-        if (sp.kind == GBO_SPACE_KINEMATIC_CHAIN)
+        const int links[2] = {sp.dim - 1, sp.dim / 2 - 1 > 0 ? sp.dim / 2 - 1 : 0};
+        for (int t = 0; t < 2; ++t)
         {
-            const int links[2] = {sp.dim - 1, sp.dim / 2 - 1 > 0 ? sp.dim / 2 - 1 : 0};
-            for (int t = 0; t < 2; ++t)
-            {
-                const float r = 2.5f * sqrtf(0.5f * (float)(links[t] + 1));
-                c = c * 64 + query_level(qf[(int64_t)(2 * links[t]) * nq + i], -r, r) * 8 +
-                    query_level(qf[(int64_t)(2 * links[t] + 1) * nq + i], -r, r);
-            }
+            const float r = 2.5f * sqrtf(0.5f * (float)(links[t] + 1));
+            c = c * 64 + query_level(f[(int64_t)(2 * links[t]) * ld + i], -r, r) * 8 +
+                query_level(f[(int64_t)(2 * links[t] + 1) * ld + i], -r, r);
         }
-        else
+    }
+    else
+    {
+        for (int d = 0; d < 4; ++d)
         {
-            for (int d = 0; d < 4; ++d)
+            int l = 0;
+            if (d < sp.dim)
             {
-                int l = 0;
-                if (d < sp.dim)
-                {
-                    const float lo = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.low[d] : -3.14159265f;
-                    const float hi = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.high[d] : 3.14159265f;
-                    l = hi > lo ? query_level(qf[(int64_t)d * nq + i], lo, hi) : 0;
-                }
-                c = c * 8 + l;
+                const float lo = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.low[d] : -3.14159265f;
+                const float hi = sp.kind == GBO_SPACE_REAL_VECTOR ? (float)sp.high[d] : 3.14159265f;
+                l = hi > lo ? query_level(f[(int64_t)d * ld + i], lo, hi) : 0;
             }
+            c = c * 8 + l;
         }
+    }
+    return c;
+}
+
+// keys of rows [0, n) of features with row stride ld; alive (nullable): rows whose flag is 0 get -1
+__global__ void query_key_kernel(SpaceParams sp, const float *qf, int64_t ld, int64_t n, const unsigned char *alive,
+                                 int *key, int *count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        if (alive && !alive[i])
+        {
+            key[i] = -1;
+            continue;
+        }
+        const int c = order_key(sp, qf, ld, i);
         key[i] = c;
         atomicAdd(&count[c], 1);
     }
@@ -770,7 +784,8 @@ __global__ void query_scatter_kernel(const int *key, int64_t nq, const int *star
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x)
     {
         const int c = key[i];
-        order[start[c] + atomicAdd(&fill[c], 1)] = i;
+        if (c >= 0)
+            order[start[c] + atomicAdd(&fill[c], 1)] = i;
     }
 }
 
@@ -780,7 +795,7 @@ void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float 
     int *count = work, *start = work + kQueryKeys, *fill = work + 2 * kQueryKeys, *key = work + 3 * kQueryKeys;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nq + 255) / 256, (int64_t)lc.sm_count * 8));
     cudaMemsetAsync(count, 0, kQueryKeys * sizeof(int), lc.stream);
-    query_key_kernel<<<grid, 256, 0, lc.stream>>>(sp, qf, nq, key, count);
+    query_key_kernel<<<grid, 256, 0, lc.stream>>>(sp, qf, nq, nq, nullptr, key, count);
     query_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, start, fill);
     query_scatter_kernel<<<grid, 256, 0, lc.stream>>>(key, nq, start, fill, order);
     for (int i = 0; i < 3; ++i)
@@ -1260,6 +1275,233 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
         return false;
 #undef GBO_BCELL_T
 #undef GBO_BCELL
+    return true;
+}
+
+
+// ---------------------------------------------------------------- cell index for the chain metric
+// Elements bucketed by the same key as the query order (the tip and middle-joint points, 8 levels per
+// coordinate: kQueryKeys cells); per cell the elements' features (20 floats, AoS, sorted by cell) and
+// their box (per feature the minimum and maximum). The box bounds the chain distance from below:
+// L * sum_i |(X_i, Y_i)(q) - box_i| <= L * sum_i |(X_i, Y_i)(q) - (X_i, Y_i)(e)| for every element e
+// of the cell (scaled by 1 - 1e-5 against the rounding of both sides, which see the same features).
+// The search is the warp-per-query one of the box kinds: own cell first (threshold seed), then the
+// cells whose bound is below min(T, the list's last entry).
+__global__ void ccell_gather_kernel(const int64_t *skey, const int *start, const int *count, const float *feat,
+                                    int64_t cap, int F, int64_t n, float4 *sfeat)
+{
+    const int64_t total = (int64_t)start[kQueryKeys - 1] + count[kQueryKeys - 1];
+    const int64_t m = min(n, total);
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t key = skey[p];
+        float v[20];
+#pragma unroll
+        for (int f = 0; f < 20; ++f)
+            v[f] = f < F ? feat[(int64_t)f * cap + key] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 5; ++j)
+            sfeat[5 * p + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    }
+}
+
+// box of cell c: 5 float4 of minima, then 5 of maxima (warp per cell)
+__global__ void ccell_box_kernel(const float4 *sfeat, const int *start, const int *count, float4 *box)
+{
+    const int lane = threadIdx.x & 31;
+    for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < kQueryKeys;
+         c += (int)((gridDim.x * blockDim.x) >> 5))
+    {
+        float mn[20], mx[20];
+#pragma unroll
+        for (int f = 0; f < 20; ++f)
+        {
+            mn[f] = __int_as_float(0x7f800000);
+            mx[f] = -__int_as_float(0x7f800000);
+        }
+        for (int p = start[c] + lane; p < start[c] + count[c]; p += 32)
+        {
+#pragma unroll
+            for (int j = 0; j < 5; ++j)
+            {
+                const float4 a = sfeat[5 * (int64_t)p + j];
+                const float v[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                {
+                    mn[4 * j + t] = fminf(mn[4 * j + t], v[t]);
+                    mx[4 * j + t] = fmaxf(mx[4 * j + t], v[t]);
+                }
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < 20; ++f)
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                mn[f] = fminf(mn[f], __shfl_xor_sync(0xffffffffu, mn[f], o));
+                mx[f] = fmaxf(mx[f], __shfl_xor_sync(0xffffffffu, mx[f], o));
+            }
+        if (lane < 5)
+        {
+            const float *m0 = mn + 0, *m1 = mx + 0;
+            float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+#pragma unroll
+            for (int j = 0; j < 5; ++j)
+                if (j == lane)
+                {
+                    lo = make_float4(m0[4 * j], m0[4 * j + 1], m0[4 * j + 2], m0[4 * j + 3]);
+                    hi = make_float4(m1[4 * j], m1[4 * j + 1], m1[4 * j + 2], m1[4 * j + 3]);
+                }
+            box[10 * (int64_t)c + lane] = lo;
+            box[10 * (int64_t)c + 5 + lane] = hi;
+        }
+    }
+}
+
+void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int *key, int *count,
+                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box)
+{
+    const int grid = grid_for(lc, nn.size);
+    cudaMemsetAsync(count, 0, kQueryKeys * sizeof(int), lc.stream);
+    query_key_kernel<<<grid, 256, 0, lc.stream>>>(sp, nn.feat32, nn.cap, nn.size, nn.alive, key, count);
+    query_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, start, fill);
+    query_scatter_kernel<<<grid, 256, 0, lc.stream>>>(key, nn.size, start, fill, skey);
+    ccell_gather_kernel<<<grid, 256, 0, lc.stream>>>(skey, start, count, nn.feat32, nn.cap, 2 * sp.dim, nn.size,
+                                                     sfeat);
+    ccell_box_kernel<<<(kQueryKeys * 32 + 255) / 256, 256, 0, lc.stream>>>(sfeat, start, count, box);
+    for (int i = 0; i < 5; ++i)
+        note_launch();
+}
+
+// chain distance from query features q to the box of a cell (before the scale by the link length)
+__device__ __forceinline__ float ccell_lb(const float4 *b, const float *q, int dim)
+{
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+    {
+        const float4 lo = b[j], hi = b[5 + j];
+        const float l[4] = {lo.x, lo.y, lo.z, lo.w}, h[4] = {hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int t = 0; t < 4; t += 2)
+        {
+            const int i = (4 * j + t) / 2;  // link
+            if (i < dim)
+            {
+                const float dx = fmaxf(fmaxf(l[t] - q[4 * j + t], q[4 * j + t] - h[t]), 0.f);
+                const float dy = fmaxf(fmaxf(l[t + 1] - q[4 * j + t + 1], q[4 * j + t + 1] - h[t + 1]), 0.f);
+                s += sqrt_approx(fmaf(dx, dx, dy * dy));
+            }
+        }
+    }
+    return s;
+}
+
+template <int K_KEEP>
+__global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, SpaceParams sp, float eps,
+                                                             const float *qf, int64_t nq, const int64_t *qorder,
+                                                             const int *qkey, int k, float *part_d, int64_t *part_k)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t qs = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (qs >= nq)
+        return;
+    const int64_t qi = qorder[qs];
+    const int F = 2 * sp.dim;
+    float qfe[20];
+#pragma unroll
+    for (int f = 0; f < 20; ++f)
+        qfe[f] = f < F ? qf[(int64_t)f * nq + qi] : 0.f;
+    const float link = (float)sp.link;
+    WarpList<K_KEEP> L;
+    L.init();
+    auto scan_cell = [&](int c, float T) {
+        const int s0 = ci.start[c], s1 = s0 + ci.count[c];
+        for (int p0 = s0; p0 < s1; p0 += 32)
+        {
+            const int p = p0 + lane;
+            float d = __int_as_float(0x7f800000);
+            int key = -1;
+            if (p < s1)
+            {
+                float pf[20];
+#pragma unroll
+                for (int j = 0; j < 5; ++j)
+                {
+                    const float4 a = ci.sfeat[5 * (int64_t)p + j];
+                    pf[4 * j] = a.x;
+                    pf[4 * j + 1] = a.y;
+                    pf[4 * j + 2] = a.z;
+                    pf[4 * j + 3] = a.w;
+                }
+                d = chain_dist32<20>(pf, qfe, sp.dim) * link;
+                key = (int)ci.skey[p];
+            }
+            const float last = L.last();
+            unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
+            while (m)
+            {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const float dc = __shfl_sync(0xffffffffu, d, src);
+                const int kc = __shfl_sync(0xffffffffu, key, src);
+                if (dc < L.last())
+                    L.insert(dc, kc, lane);
+            }
+        }
+    };
+    const int own = qkey[qi];
+    scan_cell(own, __int_as_float(0x7f800000));
+    float T = __int_as_float(0x7f800000);
+    const float dkk = L.at(k - 1);
+    if (dkk < __int_as_float(0x7f800000))
+        T = (dkk + 2.f * eps) * (1.0f + 1e-5f);
+    for (int cb = 0; cb < kQueryKeys; cb += 32)
+    {
+        const int c = cb + lane;
+        float lb = __int_as_float(0x7f800000);
+        if (c != own && ci.count[c] > 0)
+            lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
+        while (m)
+        {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+                scan_cell(cb + src, T);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < WarpList<K_KEEP>::S; ++s)
+        if (32 * s + lane < K_KEEP)
+        {
+            part_d[qs * K_KEEP + 32 * s + lane] = L.d[s];
+            part_k[qs * K_KEEP + 32 * s + lane] = L.k[s];
+        }
+}
+
+bool launch_knn_ccell(const LaunchCfg &lc, const NNArgs &nn, const ChainCellArgs &ci, const SpaceParams &sp,
+                      StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qkey, int k,
+                      int64_t *idx, double *dist, unsigned long long *fb_list, unsigned long long *fb_n,
+                      RunCounters *ctr, float *part_d, int64_t *part_k)
+{
+    if (nq == 0 || sp.kind != GBO_SPACE_KINEMATIC_CHAIN || sp.dim > 10 || k > 20)
+        return false;
+    const int qb = (int)((nq + 127) / 128), wg = (int)((nq * 32 + 255) / 256);
+    if (k <= 12)
+    {
+        knn_ccell_warp_kernel<16><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k);
+        knn_finish_kernel<GBO_SPACE_KINEMATIC_CHAIN, 10, 16><<<qb, 128, 0, lc.stream>>>(
+            nn, sp, qv, nq, k, 1, part_d, part_k, idx, dist, fb_list, fb_n, ctr, qorder);
+    }
+    else
+    {
+        knn_ccell_warp_kernel<24><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k);
+        knn_finish_kernel<GBO_SPACE_KINEMATIC_CHAIN, 10, 24><<<qb, 128, 0, lc.stream>>>(
+            nn, sp, qv, nq, k, 1, part_d, part_k, idx, dist, fb_list, fb_n, ctr, qorder);
+    }
+    note_launch();
+    note_launch();
     return true;
 }
 

@@ -47,6 +47,26 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
 constexpr int kQueryKeys = 4096;
 void launch_query_order(const LaunchCfg &lc, const SpaceParams &sp, const float *qf, int64_t nq, int *work,
                         int64_t *order);
+// Cell index of a kinematic-chain nearest-neighbour index (large batches without prefix limits):
+// kQueryKeys cells keyed like the query order.
+struct ChainCellArgs
+{
+    const int *start;      // [kQueryKeys] first sorted position of each cell
+    const int *count;      // [kQueryKeys] elements per cell
+    const int64_t *skey;   // element key at each sorted position
+    const float4 *sfeat;   // five float4 (20 features) per sorted position
+    const float4 *box;     // ten float4 per cell: 20 minima, then 20 maxima
+};
+// key: [size] ints; count / start / fill: [kQueryKeys] ints; skey: [size]; sfeat: [5 * size]; box: [10 * kQueryKeys]
+void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int *key, int *count,
+                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box);
+// qorder / qkey: the query order and each query's key (launch_query_order's order and key arrays).
+// Returns true when launched (lists for every query, P = 1, and the finish kernel).
+bool launch_knn_ccell(const LaunchCfg &lc, const NNArgs &nn, const ChainCellArgs &ci, const SpaceParams &sp,
+                      StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qkey, int k,
+                      int64_t *idx, double *dist, unsigned long long *fb_list, unsigned long long *fb_n,
+                      RunCounters *ctr, float *part_d, int64_t *part_k);
+
 int knn_chunks(const LaunchCfg &lc, int64_t nq, int64_t size);
 // largest k of the FP32-guarded kNN forms (64 for box / wrapped kinds of dim <= 8, else 20; larger k
 // and other kinds use the FP64 scan) and the list length they keep per query and chunk
