@@ -1456,11 +1456,52 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
     const float dkk = L.at(k - 1);
     if (dkk < __int_as_float(0x7f800000))
         T = (dkk + 2.f * eps) * (1.0f + 1e-5f);
+    // key digits (3 bits each): tip x, tip y, middle x, middle y; the 80 cells next to the own cell in
+    // that grid come next, so that the list holds near neighbours before the pass over all cells
+    auto near_own = [&](int c) {
+        bool nb = true;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+        {
+            const int dl = ((c >> (3 * t)) & 7) - ((own >> (3 * t)) & 7);
+            nb &= dl >= -1 && dl <= 1;
+        }
+        return nb;
+    };
+    auto visit = [&](int c, bool ok) {
+        float lb = __int_as_float(0x7f800000);
+        if (ok && ci.count[c] > 0)
+            lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
+        while (m)
+        {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+                scan_cell(__shfl_sync(0xffffffffu, c, src), T);
+        }
+    };
+    for (int j0 = 0; j0 < 81; j0 += 32)
+    {
+        // offset j in base 3: digit t in {0, 1, 2} moves digit t of the key by -1, 0, +1
+        const int j = j0 + lane;
+        int c = 0, rem = j;
+        bool ok = j < 81 && j != 40;  // 40: no move (the own cell)
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+        {
+            const int l = ((own >> (3 * t)) & 7) + (rem % 3) - 1;
+            rem /= 3;
+            ok &= l >= 0 && l < 8;
+            c |= (l & 7) << (3 * t);
+        }
+        visit(ok ? c : 0, ok);
+    }
     for (int cb = 0; cb < kQueryKeys; cb += 32)
     {
         const int c = cb + lane;
         float lb = __int_as_float(0x7f800000);
-        if (c != own && ci.count[c] > 0)
+        if (!near_own(c) && ci.count[c] > 0)
             lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
         unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
