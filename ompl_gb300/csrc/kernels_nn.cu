@@ -1422,11 +1422,15 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
             const int p = p0 + lane;
             float d = __int_as_float(0x7f800000);
             int key = -1;
+            const float last = L.last();
             if (p < s1)
             {
+                // links 4.. first (features 8-19): their terms are the largest; the rest (features 0-7)
+                // is read only when the element can still enter the list. Terms are non-negative and
+                // FP32 addition is monotone, so the full sum is at least the partial one.
                 float pf[20];
 #pragma unroll
-                for (int j = 0; j < 5; ++j)
+                for (int j = 2; j < 5; ++j)
                 {
                     const float4 a = ci.sfeat[5 * (int64_t)p + j];
                     pf[4 * j] = a.x;
@@ -1434,10 +1438,37 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
                     pf[4 * j + 2] = a.z;
                     pf[4 * j + 3] = a.w;
                 }
-                d = chain_dist32<20>(pf, qfe, sp.dim) * link;
-                key = (int)ci.skey[p];
+                float outer = 0.f;
+#pragma unroll
+                for (int i = 4; i < 10; ++i)
+                    if (i < sp.dim)
+                    {
+                        const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
+                        outer += sqrt_approx(fmaf(dx, dx, dy * dy));
+                    }
+                if (outer * link < last && outer * link <= T)
+                {
+#pragma unroll
+                    for (int j = 0; j < 2; ++j)
+                    {
+                        const float4 a = ci.sfeat[5 * (int64_t)p + j];
+                        pf[4 * j] = a.x;
+                        pf[4 * j + 1] = a.y;
+                        pf[4 * j + 2] = a.z;
+                        pf[4 * j + 3] = a.w;
+                    }
+                    float inner = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (i < sp.dim)
+                        {
+                            const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
+                            inner += sqrt_approx(fmaf(dx, dx, dy * dy));
+                        }
+                    d = (inner + outer) * link;
+                    key = (int)ci.skey[p];
+                }
             }
-            const float last = L.last();
             unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
             while (m)
             {
