@@ -1635,7 +1635,7 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
         launch_features(lc, nn->sp, qv, nq, (float *)nn->qfeat.p, nq);
         // large batches over a large RealVector / wrapped index: cell index (PRM's prefix kNN)
         if ((nn->sp.kind == GBO_SPACE_WRAP_L2 || nn->sp.kind == GBO_SPACE_REAL_VECTOR) && nn->sp.dim <= 8 &&
-            nn->size >= 65536 && nn->size < (1ll << 31) && nq >= 4096)
+            nn->size >= 65536 && nn->size < (1ll << 31) && nq >= 256)
         {
             if (auto st = ensure_box_cells(nn, lc))
                 return st;
