@@ -1653,10 +1653,9 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
                                      (int64_t *)c.qorder.p);
             BoxCellArgs ci{(const int *)c.start.p, (const int64_t *)c.skey.p, (const float4 *)c.pts8.p,
                            (const float4 *)c.box.p, c.C};
-            const int Pc = std::max(1, std::min(P, c.C));
             if (launch_knn_bcell(lc, a, ci, nn->sp, qv, (const float *)nn->qfeat.p, nq, (const int64_t *)c.qorder.p,
                                  (const int *)c.qcell.p, k, prefix, idx, dist, (unsigned long long *)nn->fb_list.p,
-                                 fb_n, ctr, part_d, part_k, Pc))
+                                 fb_n, ctr, part_d, part_k))
             {
                 launch_knn_exact(lc, a, nn->sp, qv, nq, k, prefix, idx, dist,
                                  (const unsigned long long *)nn->fb_list.p, fb_n, std::min<int64_t>(nq, 4096));

@@ -1225,10 +1225,11 @@ template <int KIND, int K_KEEP>
 static void launch_bcell_t(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
                            StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
                            const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                           unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
+                           unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k)
 {
-    const int qb = (int)((nq + 127) / 128);
-    P = 1;  // one list per query: the warp kernel visits every cell a query needs
+    // one list per query (P = 1): the warp kernel visits every cell a query needs, and the prefix scan
+    // of band 0 covers each of its queries' limits in one CTA
+    const int qb = (int)((nq + 127) / 128), P = 1;
     knn_bcell_warp_kernel<KIND, K_KEEP><<<(int)((nq * 32 + 255) / 256), 256, 0, lc.stream>>>(
         ci, sp, nn.eps32, qf, nq, qorder, qcell, prefix, k, part_d, part_k);
     if (prefix)
@@ -1248,13 +1249,13 @@ static void launch_bcell_t(const LaunchCfg &lc, const NNArgs &nn, const BoxCellA
 bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
                       StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
                       const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P)
+                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k)
 {
     if (nq == 0 || sp.dim > 8 || k > knn_fp32_max_k(sp))
         return false;
 #define GBO_BCELL_T(KIND, KK)                                                                                         \
     launch_bcell_t<KIND, KK>(lc, nn, ci, sp, qv, qf, nq, qorder, qcell, k, prefix, idx, dist, fb_list, fb_n, ctr,     \
-                             part_d, part_k, P)
+                             part_d, part_k)
 #define GBO_BCELL(KIND)                                                                                                \
     do                                                                                                                \
     {                                                                                                                 \

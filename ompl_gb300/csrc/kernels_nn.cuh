@@ -40,7 +40,7 @@ void launch_bcell_query_order(const LaunchCfg &lc, const SpaceParams &sp, int L,
 bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &ci, const SpaceParams &sp,
                       StatesView qv, const float *qf, int64_t nq, const int64_t *qorder, const int *qcell, int k,
                       const int64_t *prefix, int64_t *idx, double *dist, unsigned long long *fb_list,
-                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k, int P);
+                      unsigned long long *fb_n, RunCounters *ctr, float *part_d, int64_t *part_k);
 
 // Spatial processing order of a query batch (counting sort by a cell key of its FP32 features):
 // work holds 3 * kQueryKeys + nq ints, order nq entries.
