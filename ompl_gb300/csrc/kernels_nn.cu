@@ -1159,7 +1159,16 @@ __global__ void __launch_bounds__(256) knn_bcell_warp_kernel(BoxCellArgs ci, Spa
             m &= m - 1;
             // the list may have tightened since the cells were tested
             if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+            {
                 scan_cell(cb + src, T);
+                // T follows the list's k-th distance (the final band only lies lower)
+                const float dk = L.at(k - 1);
+                if (dk < __int_as_float(0x7f800000))
+                {
+                    const float r = sqrtf(dk) + 2.f * eps;
+                    T = fminf(T, r * r * (1.0f + 1e-5f));
+                }
+            }
         }
     }
 #pragma unroll
@@ -1485,9 +1494,13 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
     const int own = qkey[qi];
     scan_cell(own, __int_as_float(0x7f800000));
     float T = __int_as_float(0x7f800000);
-    const float dkk = L.at(k - 1);
-    if (dkk < __int_as_float(0x7f800000))
-        T = (dkk + 2.f * eps) * (1.0f + 1e-5f);
+    // T follows the list's k-th distance (the final band only lies lower)
+    auto tighten = [&]() {
+        const float dk = L.at(k - 1);
+        if (dk < __int_as_float(0x7f800000))
+            T = fminf(T, (dk + 2.f * eps) * (1.0f + 1e-5f));
+    };
+    tighten();
     // key digits (3 bits each): tip x, tip y, middle x, middle y; the 80 cells next to the own cell in
     // that grid come next, so that the list holds near neighbours before the pass over all cells
     auto near_own = [&](int c) {
@@ -1510,7 +1523,10 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
             const int src = __ffs(m) - 1;
             m &= m - 1;
             if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+            {
                 scan_cell(__shfl_sync(0xffffffffu, c, src), T);
+                tighten();
+            }
         }
     };
     for (int j0 = 0; j0 < 81; j0 += 32)
@@ -1541,7 +1557,10 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
             const int src = __ffs(m) - 1;
             m &= m - 1;
             if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+            {
                 scan_cell(cb + src, T);
+                tighten();
+            }
         }
     }
 #pragma unroll
