@@ -10,6 +10,10 @@
 //                     query blocks x chunks, so that few queries still fill the GPU), element features
 //                     staged in shared-memory tiles and read as float4; keeps the best K_KEEP by FP32
 //                     distance (kinematic chain: an L1 lower bound skips the square roots of far elements).
+//   knn_bcell_warp_kernel, knn_ccell_warp_kernel
+//                     FP32 bulk over a cell index of the elements (box / wrapped spaces; the chain
+//                     metric), one warp per query: the lanes test 32 cell boxes at a time and scan a
+//                     needed cell's elements 32 at a time; the kept list lives in the lanes.
 //   knn_finish_kernel merges the chunk lists; every kept element within 2*eps of the k-th FP32
 //                     distance is re-evaluated in FP64 and the final order is decided in FP64. If the
 //                     band may hold more than K_KEEP elements the query is queued for knn_exact_kernel.
