@@ -1,19 +1,25 @@
 """Benchmark: validated edges/s of DiscreteMotionValidator::checkMotion on the planar 10-link
 kinematic-chain workload (32 world segments, segment fraction 0.005 of the extent, edges between
-valid states of a seeded 1M-state set), on one GB300.
+valid states of a seeded 1M-state set), on one GB300, plus the other workloads of the path.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--only-headline]
 
 One step = one batch of 100,000 edges checked by the batched form (persistent work-queue kernel,
 FP32 bulk with FP64 re-check, autotuned schedule). Twelve distinct batches (192 MB of endpoints,
 more than the 129 MB L2) rotate across steps, so no step re-reads L2-resident inputs. `e2e` is the
 same metric through the host-memory C-ABI call (gbo_check_motion_host: H2D of both endpoint
-arrays, kernel, D2H of results and lastValid fractions inside the timed region). Also reported:
-the plain one-launch-per-batch FP64 form on the same batches, state validity of the 1M states,
-and nearestK (k=16) over the 1M states.
+arrays, kernel, D2H of results and lastValid fractions inside the timed region). `parity` compares
+the timed results with the oracle (20,000 edges of a timed batch; 500 of the kNN queries).
+
+The same JSON line carries one object per further workload ("workloads"): circles in RealVector(2)
+at full size, the 7-DoF DH arm among 4,096 spheres (256k edges of 2..2000 steps), the serving loop
+(512 clients, Poisson arrivals, p50/p99) and the PRM roadmap (2M samples, 16,384 spheres); each with
+the plain one-launch-per-call GPU form, the batched/served form, its roofline, parity against the
+oracle and the oracle's CPU time on one thread and on all host threads.
 
 Under torchrun each rank runs an independent replica on its own GPU ("replicas only": the path
-has no exchange step); value = all ranks' edges / max-over-ranks time.
+has no exchange step); value = all ranks' edges / max-over-ranks time; only rank 0 runs the
+further workloads.
 """
 from __future__ import annotations
 
@@ -54,7 +60,47 @@ def parse():
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
     p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm"],
                    help="launch one kernel kind twice on the chain workload (for ncu) and exit")
+    p.add_argument("--only-headline", action="store_true",
+                   help="the chain workload alone (no circles / arm / serving / PRM objects)")
     return p.parse_args()
+
+
+def cpu_info():
+    """Host CPU model and thread count (lscpu's model name; /proc/cpuinfo as a fallback)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return {"cpu_model": model, "threads": os.cpu_count() or 1}
+
+
+def timed(fn):
+    t = time.perf_counter()
+    r = fn()
+    return r, time.perf_counter() - t
+
+
+def cpu_rates(n_all, n_one, run):
+    """Oracle CPU rate on all host threads (n_all units) and on one thread (n_one units): run(n, threads)
+    performs n units. Returns dict(all_core, single_thread, cores)."""
+    threads = os.cpu_count() or 1
+    _, t_all = timed(lambda: run(n_all, threads))
+    _, t_one = timed(lambda: run(n_one, 1))
+    return {"all_core": n_all / t_all, "single_thread": n_one / t_one, "cores": threads,
+            "sample_all_core": n_all, "sample_single_thread": n_one}
 
 
 def workload(seed=1):
@@ -124,13 +170,6 @@ class Clocks:
                 "reasons": reasons, "samples": len(win)}
 
 
-def cpu_edges_per_s(port, sd, cd, s1, s2, threads):
-    port.set_threads(threads)
-    t = time.perf_counter()
-    port.check_motion(sd, cd, s1, s2, want_state=False, want_bisect=False)
-    return len(s1) / (time.perf_counter() - t)
-
-
 def bench_config():
     """The workload both arms report (the reference arm times a bounded sample of each step)."""
     return {"workload": "kinematic_chain10: 10 links x 0.1, 32 segments, 1M states, 100k edges/step between "
@@ -151,23 +190,23 @@ def reference_arm(args, rank, world):
     cd = CheckerDesc(w.checker_kind, w.obstacles)
     valid = port.is_valid(sd, cd, w.states).astype(bool)
     batches = make_batches(w.states[valid], N_BATCHES)
-    sample = 20_000
     for i in range(args.warmup):
         s1, s2 = batches[i % N_BATCHES]
-        port.check_motion(sd, cd, s1[:sample], s2[:sample], want_state=False, want_bisect=False)
+        port.check_motion(sd, cd, s1, s2, want_state=False, want_bisect=False)
     t = time.perf_counter()
     for i in range(args.steps):
         s1, s2 = batches[i % N_BATCHES]
-        port.check_motion(sd, cd, s1[:sample], s2[:sample], want_state=True, want_bisect=False)
+        port.check_motion(sd, cd, s1, s2, want_state=True, want_bisect=False)
     dt = time.perf_counter() - t
-    v = sample * args.steps / dt
+    v = N_EDGES * args.steps / dt
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "edges/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {**bench_config(), "reference_sample_edges_per_step": sample},
-        "cpu_baseline": {"value": v, "unit": "edges/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} edges per step of each 100k-edge batch, all host threads"},
+        "config": bench_config(),
+        "cpu_baseline": {"value": v, "unit": "edges/s", "cores": threads, "kind": "port", **cpu_info(),
+                         "sample": "every step: the whole 100k-edge batch (ordered DiscreteMotionValidator with "
+                                   "lastValid), all host threads"},
         "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -249,7 +288,7 @@ def ours(args, rank, world, local_rank):
     clk.stop()
     launches = B.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    stats = checker.stats()  # states evaluated / re-checked in FP64 by the last timed step
+    stats = checker.stats()  # states evaluated / re-checked in FP64 / one-ulp hazards of the last timed step
     value, dev_s, wall = replica_totals(N_EDGES, args.steps, sum(step_ms) * 1e-3, wall, world, dev)
     mean_ms = statistics.mean(step_ms)
     mean_checked = statistics.mean(checked[i % N_BATCHES] for i in range(args.steps))
@@ -320,6 +359,9 @@ def ours(args, rank, world, local_rank):
     e2e_s = time.perf_counter() - t
     e2e = N_EDGES * args.steps / e2e_s
 
+    # precision statistics of the FP32 form over the 1M states (flip rate before re-check, FP32 error)
+    precision = checker.precisionStats(states_soa, soa=True)
+
     # nearestK k=16 over the 1M states
     nn = B.NearestNeighborsGPU(space, capacity=N_STATES)
     nn.add(states_soa, soa=True)
@@ -329,11 +371,18 @@ def ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record()
-    nn.nearestK(q, 16, soa=True, want_dist=False)
+    knn_idx, _ = nn.nearestK(q, 16, soa=True, want_dist=False)
     k1.record()
     torch.cuda.synchronize()
     knn_qps = KNN_QUERIES / (k0.elapsed_time(k1) * 1e-3)
     knn_stats = nn.stats()
+    knn_idx = knn_idx.cpu().numpy()
+    pq = np.random.default_rng(12).choice(KNN_QUERIES, 500, replace=False)
+    _, knn_dist500 = nn.nearestK(q[:, pq].contiguous(), 16, soa=True)
+    knn_dist500 = knn_dist500.cpu().numpy()
+    # results of the timed batches, for the parity check against the oracle
+    r0 = run(0, capi.SCHEDULE_AUTO)
+    timed0 = {k: r0[k].cpu().numpy() for k in ("ok", "first_j", "nd")}
 
     # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them
     smp = B.StateSampler(space, 5)
@@ -354,7 +403,7 @@ def ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    peak_fp32 = B.measure_fp32_peak()
+    peak_fp32 = _fp32_peak()
     achieved = mean_checked * FLOP_PER_STATE / (mean_ms * 1e-3)
     # DRAM read + write bytes of one launch of the timed kernel, from the committed ncu summary
     # (same 100k-edge batch as one step)
@@ -366,14 +415,31 @@ def ours(args, rank, world, local_rank):
                 traffic = int(line.split(":")[1])
             elif line.startswith("issue_active_frac:"):
                 issue = float(line.split(":")[1])
-    # CPU baseline: the oracle port on all host threads, bounded sample of batch 0
+    # CPU baseline: the oracle port on all host threads and on one thread, bounded samples of batch 0;
+    # the all-core answers double as the parity check of the timed batch
     from oracle.oracle import CheckerDesc, Oracle, SpaceDesc
     port = Oracle.port()
     sd = SpaceDesc(w.space_kind, w.dim, link_length=w.link_length, lvs_fraction=w.lvs_fraction)
     cd = CheckerDesc(w.checker_kind, w.obstacles)
     threads = os.cpu_count() or 1
     sample = 20_000
-    cpu_v = cpu_edges_per_s(port, sd, cd, host_batches[0][0][:sample], host_batches[0][1][:sample], threads)
+    a0, b0 = host_batches[0][0][:sample], host_batches[0][1][:sample]
+    port.set_threads(threads)
+    ref0, dt_all = timed(lambda: port.check_motion(sd, cd, a0, b0, want_state=False, want_bisect=False))
+    port.set_threads(1)
+    _, dt_one = timed(lambda: port.check_motion(sd, cd, a0[:2000], b0[:2000], want_state=False, want_bisect=False))
+    port.set_threads(threads)
+    cpu_v = sample / dt_all
+    agree = (ref0["ok"] == timed0["ok"][:sample]) & (ref0["first_j"] == timed0["first_j"][:sample]) & \
+        (ref0["nd"] == timed0["nd"][:sample])
+    ref_idx, ref_dist = port.knn(sd, w.states, w.states[qi[pq]], 16)
+    knn_agree = (ref_idx == knn_idx[pq]).all(axis=1) & \
+        np.all(np.abs(ref_dist - knn_dist500) <= 1e-12 * np.maximum(np.abs(ref_dist), np.abs(knn_dist500)), axis=1)
+    parity = {"edges_checked": sample, "edges_agree": int(agree.sum()), "knn_checked": len(pq),
+              "knn_agree": int(knn_agree.sum()),
+              "compared": "ok, first invalid index and segment count of 20,000 edges of timed batch 0; "
+                          "index lists (exact) and distances (relative 1e-12, FP64 sin/cos) of 500 of the "
+                          "20,000 kNN queries, against the oracle"}
     clocks = clk.summary(t0, t1)
     out = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
@@ -391,13 +457,23 @@ def ours(args, rank, world, local_rank):
                              "issue_active_frac is ncu's smsp__issue_active of the same launch",
                      "peak_source": "FP32 FMA throughput measured in this run (gbo_measure_fp32_peak)",
                      "work": f"{FLOP_PER_STATE} flop x checked states ({mean_checked:.0f} per step)"},
-        "cpu_baseline": {"value": cpu_v, "unit": "edges/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} edges of batch 0, oracle restatement, all host threads"},
+        "cpu_baseline": {"value": cpu_v, "unit": "edges/s", "cores": threads, "kind": "port", **cpu_info(),
+                         "single_thread": 2000 / dt_one,
+                         "sample": f"{sample} edges of batch 0 on all host threads, 2,000 on one thread "
+                                   "(oracle restatement, FP64)"},
+        "parity": parity,
         "plain_fp64_edges_per_s": plain_eps,
         "batched_vs_plain": value / world / plain_eps,
         "schedule_edges_per_s": sched_eps,
         "graph_replay_edges_per_s": graph_eps,
         "recheck_rate": stats["rechecked"] / max(stats["evaluated"], 1),
+        "flip_rate": precision["flip_rate"],
+        "precision": {**precision, "over": "the 1M states of the workload, all 397 segment tests each",
+                      "hazards_last_step": stats["hazards"],
+                      "note": "flip = FP32 verdict taken at face value differs from the FP64 verdict; the "
+                              "guarded form re-checks every ambiguous state in FP64, so its answers equal "
+                              "the FP64 ones; hazards = FP64 decisions a one-ulp change of a C-library "
+                              "sin/cos could reverse"},
         "states_per_s": states_per_s,
         "knn_queries_per_s": knn_qps,
         "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},
@@ -405,6 +481,10 @@ def ours(args, rank, world, local_rank):
         "recheck": stats,
         "clocks": clocks,
     }
+    if not args.only_headline and world == 1:
+        del dev_batches, pin_in, states_soa, nn
+        torch.cuda.empty_cache()
+        out["workloads"] = other_workloads(port)
     print(json.dumps(out))
 
 
@@ -463,13 +543,107 @@ def profile(kind):
     print(json.dumps({"profile": kind, "ok": True}))
 
 
-def arm_bench(args):
-    """7-DoF DH arm among 4,096 spheres: 256k edges with 2..2000 interpolation steps, one launch."""
+ARM_FLOP_PER_STATE = 504 + 1008 + 672  # FK (7 x (sincos + 36 FMA)), 56 sphere transforms, 56 cell lookups
+NARROW_FLOP_PER_PAIR = 10
+
+
+def _events(n=2):
+    import torch
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def _checked_states(r):
+    """States the reference's ordered DiscreteMotionValidator evaluates: first_j of an invalid motion,
+    max(nd, 1) of a valid one."""
+    import torch
+    fj, nd = r["first_j"].long(), r["nd"].long()
+    return int(torch.where(fj >= 0, fj, torch.clamp(nd, min=1)).sum().item())
+
+
+def _fp32_peak():
+    from ompl_gb300 import base as B
+    if not hasattr(_fp32_peak, "v"):
+        _fp32_peak.v = B.measure_fp32_peak()
+    return _fp32_peak.v
+
+
+def circles_workload(port):
+    """Point robot in RealVector(2) among 100 circles at full size: 10,000 states, 10,000 edges at
+    segment fraction 0.01, nearestK k = 10 for 1,000 queries; FP64 throughout (the circles checker has no
+    FP32 form). Every output compared with the oracle."""
     import torch
 
     from ompl_gb300 import base as B
     from ompl_gb300 import capi
     from ompl_gb300 import workloads as W
+    from oracle.oracle import CheckerDesc, SpaceDesc
+    w = W.config0()
+    space = B.RealVectorStateSpace(2, w.low, w.high)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    ck = B.CirclesValidityChecker(space, w.obstacles)
+    mv = B.DiscreteMotionValidator(ck)
+    st = torch.as_tensor(w.states.T.copy(), device="cuda")
+    a = torch.as_tensor(w.s1.T.copy(), device="cuda")
+    b = torch.as_tensor(w.s2.T.copy(), device="cuda")
+    q = torch.as_tensor(w.queries.T.copy(), device="cuda")
+    nn = B.NearestNeighborsGPU(space, capacity=len(w.states))
+    nn.add(st, soa=True)
+
+    def rate(fn, units, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return units * reps / (e0.elapsed_time(e1) * 1e-3), out
+
+    v_rate, valid = rate(lambda: ck.isValid(st, soa=True), len(w.states))
+    plain, rp = rate(lambda: mv.checkMotions(a, b, schedule=capi.SCHEDULE_PLAIN, soa=True), len(w.s1))
+    batched, rb = rate(lambda: mv.checkMotions(a, b, schedule=capi.SCHEDULE_AUTO, soa=True), len(w.s1))
+    k_rate, (idx, dist) = rate(lambda: nn.nearestK(q, 10, soa=True), len(w.queries))
+    sd = SpaceDesc(w.space_kind, 2, w.low, w.high, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles)
+    port.set_threads(os.cpu_count() or 1)
+    v_ref = port.is_valid(sd, cd, w.states).astype(bool)
+    m_ref = port.check_motion(sd, cd, w.s1, w.s2, want_state=False, want_bisect=False)
+    i_ref, d_ref = port.knn(sd, w.states, w.queries, 10)
+    rb = {k: v.cpu().numpy() for k, v in rb.items()}
+    idx, dist = idx.cpu().numpy(), dist.cpu().numpy()
+    parity = {"states_checked": len(w.states), "states_agree": int((valid.cpu().numpy().astype(bool) == v_ref).sum()),
+              "edges_checked": len(w.s1),
+              "edges_agree": int(((rb["ok"] == m_ref["ok"]) & (rb["first_j"] == m_ref["first_j"]) &
+                                  (rb["nd"] == m_ref["nd"])).sum()),
+              "knn_checked": len(w.queries),
+              "knn_agree": int(((idx == i_ref).all(1) & (dist.view(np.uint64) == d_ref.view(np.uint64)).all(1)).sum())}
+    checked = _checked_states({k: torch.as_tensor(v) for k, v in rb.items()})
+
+    def cpu_motion(n, threads):
+        port.set_threads(threads)
+        port.check_motion(sd, cd, w.s1[:n], w.s2[:n], want_state=False, want_bisect=False)
+
+    cpu = cpu_rates(len(w.s1), 2000, cpu_motion)
+    port.set_threads(os.cpu_count() or 1)
+    return {"workload": "circles2d: point robot in RealVector(2) on [0,1]^2, 100 circles, 10,000 states, 10,000 "
+                        "random edges at segment fraction 0.01, nearestK k=10 for 1,000 queries, FP64",
+            "states_per_s": v_rate, "plain_edges_per_s": plain, "batched_edges_per_s": batched,
+            "knn_queries_per_s": k_rate, "checked_states_per_edge": checked / len(w.s1),
+            "roofline": {"bound": "fp64 latency (tiny batch)", "note": "10,000 edges of ~1.6 checked states "
+                         "finish in tens of microseconds: launch latency, not a roofline, bounds this size"},
+            "cpu_baseline": {"unit": "edges/s", "kind": "port", **cpu},
+            "parity": parity, "flip_rate": None}
+
+
+def arm_workload(port, n_plain=16_384):
+    """7-DoF DH arm among 4,096 spheres: 256k edges with 2..2000 interpolation steps, one launch each."""
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import capi
+    from ompl_gb300 import workloads as W
+    from oracle.oracle import CheckerDesc, SpaceDesc
     w = W.config2()
     space = B.RealVectorStateSpace(7, w.low, w.high)
     space.setLongestValidSegmentFraction(w.lvs_fraction)
@@ -478,81 +652,168 @@ def arm_bench(args):
     s1 = torch.as_tensor(w.s1.T.copy(), device="cuda")
     s2 = torch.as_tensor(w.s2.T.copy(), device="cuda")
     n = s1.shape[1]
-    res = {}
+    res, res_ms, outs = {}, {}, {}
     for prec, sch, name in (("fp32_guarded", capi.SCHEDULE_TILE, "tile"), ("fp32_guarded", capi.SCHEDULE_WARP, "warp"),
-                            ("fp64", capi.SCHEDULE_PLAIN, "plain_fp64")):
+                            ("fp32_guarded", capi.SCHEDULE_AUTO, "batched"), ("fp64", capi.SCHEDULE_PLAIN, "plain_fp64")):
         checker.setPrecision(prec)
-        m = n if name != "plain_fp64" else 16_384
+        m = n if name != "plain_fp64" else n_plain
         a, b = s1[:, :m].contiguous(), s2[:, :m].contiguous()
-        r = mv.checkMotions(a, b, schedule=sch, soa=True)
+        mv.checkMotions(a, b, schedule=sch, soa=True)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
         reps = 3 if name != "plain_fp64" else 1
+        e0, e1 = _events()
+        e0.record()
         for _ in range(reps):
             r = mv.checkMotions(a, b, schedule=sch, soa=True)
         e1.record()
         torch.cuda.synchronize()
         res[name] = reps * m / (e0.elapsed_time(e1) * 1e-3)
-        if name == "tile":
-            fj, nd = r["first_j"].long(), r["nd"].long()
-            checked = int(torch.where(fj >= 0, fj, torch.clamp(nd, min=1)).sum().item())
-            valid = float(r["ok"].float().mean().item())
-            st = checker.stats()
-    print(json.dumps({"metric": "validated edges/s (DH arm, 4096 spheres)", "edges": n,
-                      "edges_per_s": res, "checked_states_per_edge": checked / n, "valid_fraction": valid,
-                      "recheck": st}))
+        res_ms[name] = e0.elapsed_time(e1) / reps
+        outs[name] = (r, checker.stats())  # counters of the last call
+    r, st = outs["batched"]
+    checked = _checked_states(r)
+    pairs = st.get("pairs")
+    flop = checked * ARM_FLOP_PER_STATE + (pairs or 0) * NARROW_FLOP_PER_PAIR
+    peak = _fp32_peak()
+    achieved = flop / (res_ms["batched"] * 1e-3)
+    sd = SpaceDesc(w.space_kind, 7, w.low, w.high, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(w.checker_kind, w.obstacles, w.dh, 8, 0.05)
+    port.set_threads(os.cpu_count() or 1)
+    npar = 2000
+    ref = port.check_motion(sd, cd, w.s1[:npar], w.s2[:npar], want_state=False, want_bisect=False)
+    got = {k: r[k][:npar].cpu().numpy() for k in ("ok", "first_j", "nd")}
+    agree = (got["ok"] == ref["ok"]) & (got["first_j"] == ref["first_j"]) & (got["nd"] == ref["nd"])
+
+    def cpu_motion(k, threads):
+        port.set_threads(threads)
+        port.check_motion(sd, cd, w.s1[:k], w.s2[:k], want_state=False, want_bisect=False)
+
+    cpu = cpu_rates(npar, 200, cpu_motion)
+    port.set_threads(os.cpu_count() or 1)
+    # precision statistics over every state the ordered validator would build for the first 1,000 edges
+    # (RealVector interpolation from + (to - from) * t with t = j / nd, as RealVectorStateSpace.cpp:257-265)
+    nd0 = ref["nd"][:1000].astype(np.int64)
+    rows = np.repeat(np.arange(1000), np.maximum(nd0, 1))
+    jj = np.concatenate([np.arange(1, max(k, 1) + 1) for k in nd0]).astype(np.float64)
+    tt = jj / np.maximum(nd0[rows], 1)
+    pstates = w.s1[rows] + (w.s2[rows] - w.s1[rows]) * tt[:, None]
+    checker.setPrecision("fp32_guarded")
+    precision = checker.precisionStats(pstates)
+    checker.setPrecision("fp64")
+    mv.checkMotions(s1[:, :n_plain].contiguous(), s2[:, :n_plain].contiguous(), schedule=capi.SCHEDULE_PLAIN, soa=True)
+    hz_plain = checker.stats()["hazards"]
+    checker.setPrecision("fp32_guarded")
+    return {"workload": "dh_arm7: 7-DoF DH arm (8 spheres r 0.05 per link), 4,096 world spheres in a 64^3 grid, "
+                        "256k edges of 2..2000 interpolation steps, one launch",
+            "edges": n, "edges_per_s": res, "plain_edges_per_s": res["plain_fp64"],
+            "batched_edges_per_s": res["batched"], "batched_vs_plain": res["batched"] / res["plain_fp64"],
+            "plain_sample_edges": n_plain, "checked_states_per_edge": checked / n,
+            "valid_fraction": float(r["ok"].float().mean().item()),
+            "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / peak,
+                         "work": f"{ARM_FLOP_PER_STATE} flop x checked states ({checked}) + {NARROW_FLOP_PER_PAIR} "
+                                 f"flop x narrow-phase pairs examined ({pairs})",
+                         "peak_source": "FP32 FMA throughput measured in this run (gbo_measure_fp32_peak)"},
+            "recheck": st, "cpu_baseline": {"unit": "edges/s", "kind": "port", **cpu},
+            "parity": {"edges_checked": npar, "edges_agree": int(agree.sum())},
+            "flip_rate": precision["flip_rate"],
+            "precision": {**precision, "over": f"the {len(pstates)} states of the first 1,000 edges",
+                          "hazards_batched": st.get("hazards"), "hazards_plain_fp64": hz_plain},
+            "l2": "inputs (29 MB) fit in L2; each launch is compute-bound (3 ms)"}
 
 
-def prm_bench(args):
+def prm_workload(port, n=None, star=False):
     """Full PRM roadmap construction (2M uniform samples, validity filter, prefix nearestK k=10 in
-    the wrap-L2 joint space, n->m edges at 0.01 rad) for the DH arm among 16,384 spheres.
-    PRM_STAR=1: PRM* connection counts (KStarStrategy, k(m) = ceil((e + e/7) log(m + 1)))."""
+    the wrap-L2 joint space, n->m edges at 0.01 rad) for the DH arm among 16,384 spheres; PRM* with
+    KStarStrategy when star is set."""
+    import hashlib
+
     import torch
 
     from ompl_gb300 import base as B
+    from ompl_gb300 import capi
     from ompl_gb300 import prm
     from ompl_gb300 import workloads as W
+    from oracle.oracle import CheckerDesc, SpaceDesc
     w = W.config4()
-    n = int(os.environ.get("PRM_SAMPLES", w.extra["n_samples"]))
-    star = os.environ.get("PRM_STAR", "0") == "1"
+    n = int(n or w.extra["n_samples"])
     space = B.WrapL2StateSpace(7)
     space.setLongestValidSegmentFraction(w.lvs_fraction)
     checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
     checker.setPrecision("fp32_guarded")
-    prm.construct_roadmap(space, checker, w.extra["sampler_seed"], 20_000, star=star)  # warm-up (autotune, allocs)
+    seed = w.extra["sampler_seed"]
+    small = 20_000
+    prm.construct_roadmap(space, checker, seed, small, star=star)  # warm-up (autotune, allocations)
     torch.cuda.synchronize()
-    t = time.perf_counter()
-    rm = prm.construct_roadmap(space, checker, w.extra["sampler_seed"], n, star=star)
-    total = time.perf_counter() - t
+    _, gpu_small_s = timed(lambda: (prm.construct_roadmap(space, checker, seed, small, star=star),
+                                    torch.cuda.synchronize()))
+    torch.cuda.synchronize()
+    rm, total = timed(lambda: prm.construct_roadmap(space, checker, seed, n, star=star))
     nm = rm.milestones.shape[1]
-    # the motion phase under each persistent schedule (the autotuner picks one per checker)
-    from ompl_gb300 import capi
+    src, dst = rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy()
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    comps = connected_components(coo_matrix((np.ones(len(src)), (src, dst)), shape=(nm, nm)), directed=False)[0]
+    # the motion phase: batched (persistent, FP32 + FP64 re-check) vs plain (one FP64 launch) on a sample
     mv = B.DiscreteMotionValidator(checker)
-    s1 = rm.milestones[:, rm.edge_src[:200_000]].contiguous()
-    s2 = rm.milestones[:, rm.edge_dst[:200_000]].contiguous()
-    sched = {}
-    for name, sch in (("tile", capi.SCHEDULE_TILE), ("warp", capi.SCHEDULE_WARP)):
-        mv.checkMotions(s1, s2, schedule=sch, soa=True)
+    m = min(200_000, int(rm.edge_src.numel()))
+    a = rm.milestones[:, rm.edge_src[:m]].contiguous()
+    b = rm.milestones[:, rm.edge_dst[:m]].contiguous()
+    forms = {}
+    for name, prec, sch in (("batched", "fp32_guarded", capi.SCHEDULE_AUTO), ("plain_fp64", "fp64", capi.SCHEDULE_PLAIN)):
+        checker.setPrecision(prec)
+        mv.checkMotions(a[:, :1000].contiguous(), b[:, :1000].contiguous(), schedule=sch, soa=True)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        mv.checkMotions(s1, s2, schedule=sch, soa=True)
+        e0, e1 = _events()
+        e0.record()
+        mv.checkMotions(a, b, schedule=sch, soa=True)
+        e1.record()
         torch.cuda.synchronize()
-        sched[name] = s1.shape[1] / (time.perf_counter() - t0)
-    comps = prm.connected_components(nm, rm.edge_src.cpu().numpy(), rm.edge_dst.cpu().numpy())
-    print(json.dumps({"metric": "PRM%s roadmap construction (DH arm, 16384 spheres)" % ("*" if star else ""),
-                      "samples": n,
-                      "milestones": nm, "candidate_edges": rm.candidate_edges, "edges": int(rm.edge_src.numel()),
-                      "components": comps, "total_s": total, "timings_ms": rm.timings_ms,
-                      "edges_per_s": rm.candidate_edges / (rm.timings_ms["motion"] * 1e-3),
-                      "knn_queries_per_s": nm / (rm.timings_ms["nn add+prefix kNN"] * 1e-3),
-                      "checked_states": rm.checked_states, "valid_edge_schedules_edges_per_s": sched}))
+        forms[name] = m / (e0.elapsed_time(e1) * 1e-3)
+    checker.setPrecision("fp32_guarded")
+    samples = B.StateSampler(space, seed).sampleUniform(min(n, 2_000_000), soa=True, host=False)
+    precision = checker.precisionStats(samples, soa=True)
+    del samples
+    out = {"workload": "prm%s_dh_arm7: PRM roadmap from %d uniform samples, 7-DoF DH arm among 16,384 spheres, "
+                       "wrap-L2 joint space, nearestK k=10 (prefix), edges at 0.01 rad" % ("_star" if star else "", n),
+           "samples": n, "milestones": nm, "candidate_edges": rm.candidate_edges, "edges": int(len(src)),
+           "components": int(comps), "total_s": total, "timings_ms": rm.timings_ms,
+           "edges_per_s": rm.candidate_edges / (rm.timings_ms["motion"] * 1e-3),
+           "knn_queries_per_s": nm / (rm.timings_ms["nn add+prefix kNN"] * 1e-3),
+           "checked_states": rm.checked_states,
+           "motion_sample_edges": m, "plain_edges_per_s": forms["plain_fp64"],
+           "batched_edges_per_s": forms["batched"], "batched_vs_plain": forms["batched"] / forms["plain_fp64"],
+           "flip_rate": precision["flip_rate"], "precision": {**precision, "over": "the uniform samples"}}
+    if not star:
+        dg = os.path.join(ROOT, "tests", "golden", "prm_dh_arm7_digest.json")
+        ref = json.load(open(dg))["sizes"].get(str(n)) if os.path.exists(dg) else None
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from golden.make_prm_digest import roadmap_digest
+        got = roadmap_digest(rm.sample_index.cpu().numpy(), src, dst, rm.candidate_edges)
+        out["parity"] = {"digest_match": (got == ref) if ref else None, "edges": got["edges"],
+                         "reference": "tests/golden/prm_dh_arm7_digest.json (oracle on the CPU)"}
+        sd = SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction)
+        cd = CheckerDesc(w.checker_kind, w.obstacles, w.dh, 8, 0.05)
+
+        def cpu_prm(k, threads):
+            port.set_threads(threads)
+            port.prm_roadmap(sd, cd, seed, k, 10)
+
+        cpu = cpu_rates(small, 4000, cpu_prm)
+        port.set_threads(os.cpu_count() or 1)
+        out["cpu_baseline"] = {"unit": "samples/s", "kind": "port", **cpu,
+                               "gpu_same_sample_samples_per_s": small / gpu_small_s,
+                               "note": "whole roadmap construction of the first 20,000 (all threads) / 4,000 (one "
+                                       "thread) samples"}
+    return out
 
 
-def serve_bench(args):
-    """Serving: 512 clients, each with its own world (1,024..8,192 spheres, the 7-DoF DH arm) and roadmap
-    (10k..200k joint states, nearestK k=10); Poisson arrivals of motion requests (16..65,536 edges) and
-    nearestK requests (1..4,096 queries). Reports saturation throughput and, at 70% of it, p50/p99."""
+def serve_workload(port, n_clients=512, n_req=2000):
+    """Serving: n_clients clients, each with its own world (1,024..8,192 spheres, the 7-DoF DH arm) and
+    roadmap (10k..200k joint states, nearestK k=10); Poisson arrivals of motion requests (16..65,536
+    edges) and nearestK requests (1..4,096 queries). Reports saturation throughput and, at 70% of it,
+    p50/p99; the plain form runs the same requests one at a time (FP64 plain motion schedule, FP64 exact
+    nearestK). Parity: 24 served requests against the oracle."""
     import threading as th
 
     import torch
@@ -561,25 +822,29 @@ def serve_bench(args):
     from ompl_gb300 import capi
     from ompl_gb300 import serve
     from ompl_gb300 import workloads as W
-    n_clients = int(os.environ.get("SERVE_CLIENTS", 512))
-    n_req = int(os.environ.get("SERVE_REQUESTS", 3000))
+    from oracle.oracle import CheckerDesc, SpaceDesc
     rng = np.random.default_rng(3)
     dh = W.dh_arm(np.random.default_rng(2))
     lvs_fraction = 1.0 / 2500.0
     clients = []
     t_setup = time.perf_counter()
-    for c in range(n_clients):
+
+    def client_data(c):
         crng = np.random.default_rng(3 + 1000 * (c + 1))
         world = W.sphere_world(crng, int(crng.integers(1024, 8193)))
+        nroad = int(np.exp(crng.uniform(np.log(10_000), np.log(200_000))))
+        return world, crng.uniform(-math.pi, math.pi, size=(7, nroad))
+
+    for c in range(n_clients):
+        world, road = client_data(c)
         space = B.RealVectorStateSpace(7, -math.pi, math.pi)
         space.setLongestValidSegmentFraction(lvs_fraction)
         ck = B.DHSphereArmValidityChecker(space, dh, world, 8, 0.05)
         ck.setPrecision("fp32_guarded")
-        nroad = int(np.exp(crng.uniform(np.log(10_000), np.log(200_000))))
         wspace = B.WrapL2StateSpace(7)
-        nn = B.NearestNeighborsGPU(wspace, capacity=nroad)
-        nn.add(torch.as_tensor(crng.uniform(-math.pi, math.pi, size=(7, nroad)), device="cuda"), soa=True)
-        clients.append((ck, nn, nroad))
+        nn = B.NearestNeighborsGPU(wspace, capacity=road.shape[1])
+        nn.add(torch.as_tensor(road, device="cuda"), soa=True)
+        clients.append((ck, nn, road.shape[1]))
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     lo, hi = np.full(7, -math.pi), np.full(7, math.pi)
@@ -610,6 +875,7 @@ def serve_bench(args):
 
     def run(rate):
         lat = [None] * len(reqs)
+        results = [None] * len(reqs)
         tickets = [None] * len(reqs)
         done = th.Event()
 
@@ -617,11 +883,11 @@ def serve_bench(args):
             for i in range(len(reqs)):
                 while tickets[i] is None:
                     time.sleep(0.0002)
-                lat[i] = srv.wait(tickets[i])[1]
+                results[i], lat[i] = srv.wait(tickets[i])
             done.set()
 
-        w = th.Thread(target=waiter)
-        w.start()
+        wt = th.Thread(target=waiter)
+        wt.start()
         t0 = time.perf_counter()
         gaps = np.random.default_rng(9).exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
         t_next = t0
@@ -633,14 +899,14 @@ def serve_bench(args):
             tickets[i] = submit(r)
         done.wait()
         wall = time.perf_counter() - t0
-        w.join()
-        return wall, lat
+        wt.join()
+        return wall, lat, results
 
-    wall_sat, _ = run(None)
+    wall_sat, _, results = run(None)
     edges = sum(len(r[2]) for r in reqs if r[0] == "motion")
     queries = sum(len(r[2]) for r in reqs if r[0] == "knn")
     rate = 0.7 * len(reqs) / wall_sat
-    wall, lat = run(rate)
+    wall, lat, _ = run(rate)
 
     def pct(kind, q):
         xs = [l for r, l in zip(reqs, lat) if kind in (None, r[0])]
@@ -665,9 +931,29 @@ def serve_bench(args):
     plain_s = time.perf_counter() - t
     st = srv.stats()
     srv.close()
-    print(json.dumps({
-        "metric": "serving: validated edges/s and kNN queries/s, p50/p99 latency", "clients": n_clients,
-        "requests": n_req, "setup_s": setup_s,
+    # parity and the CPU baseline: 24 served requests replayed on the oracle (all threads, then one)
+    port.set_threads(os.cpu_count() or 1)
+    sd = SpaceDesc(0, 7, lo, hi, lvs_fraction=lvs_fraction)
+    sdw = SpaceDesc(3, 7, lvs_fraction=lvs_fraction)
+    pick = np.random.default_rng(4).choice(len(reqs), 24, replace=False)
+    agree, cpu_t, cpu_units = 0, 0.0, 0
+    for i in pick:
+        kind, c, a, b = reqs[i]
+        world, road = client_data(c)
+        t = time.perf_counter()
+        if kind == "motion":
+            ref = port.check_motion(sd, CheckerDesc(3, world, dh, 8, 0.05), a, b, want_state=False, want_bisect=False)
+            same = np.array_equal(ref["ok"], results[i]["ok"]) and np.array_equal(ref["first_j"], results[i]["first_j"])
+        else:
+            ri, _ = port.knn(sdw, road.T.copy(), a, 10)
+            same = np.array_equal(ri, results[i]["idx"])
+        cpu_t += time.perf_counter() - t
+        cpu_units += len(a)
+        agree += int(same)
+    return {
+        "workload": f"serving: {n_clients} clients, own worlds of 1,024..8,192 spheres and roadmaps of 10k..200k "
+                    f"joint states, {n_req} Poisson requests (motion 16..65,536 edges / nearestK 1..4,096 queries)",
+        "clients": n_clients, "requests": n_req, "setup_s": setup_s,
         "saturation": {"wall_s": wall_sat, "edges_per_s": edges / wall_sat, "queries_per_s": queries / wall_sat,
                        "requests_per_s": n_req / wall_sat},
         "offered_load_requests_per_s": rate,
@@ -679,19 +965,37 @@ def serve_bench(args):
                                     "edges_per_s": pe / plain_s if plain_s else None,
                                     "work_units_per_s": (pe + pq) / plain_s},
         "served_vs_plain_edges": (edges / wall_sat) / (pe / plain_s) if pe else None,
-        "server": st}))
+        "plain_edges_per_s": pe / plain_s if pe else None, "batched_edges_per_s": edges / wall_sat,
+        "parity": {"requests_checked": len(pick), "requests_agree": agree},
+        "cpu_baseline": {"unit": "work units/s (edges + queries)", "kind": "port", "all_core": cpu_units / cpu_t,
+                         "cores": os.cpu_count() or 1, "sample": "the 24 parity requests replayed on all threads"},
+        "server": st}
+
+
+def other_workloads(port):
+    import torch
+    out = {}
+    for name, fn in (("circles2d", circles_workload), ("dh_arm7_4096", arm_workload),
+                     ("prm_dh_arm7_2M", prm_workload), ("serve_512_clients", serve_workload)):
+        t = time.perf_counter()
+        out[name] = fn(port)
+        out[name]["bench_wall_s"] = time.perf_counter() - t
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
     args = parse()
-    if args.workload == "serve" and not args.profile and args.impl == "ours":
-        serve_bench(args)
-        return
-    if args.workload == "arm" and not args.profile and args.impl == "ours":
-        arm_bench(args)
-        return
-    if args.workload == "prm" and not args.profile and args.impl == "ours":
-        prm_bench(args)
+    if args.workload != "chain" and not args.profile and args.impl == "ours":
+        from oracle.oracle import Oracle
+        port = Oracle.port()
+        if args.workload == "serve":
+            r = serve_workload(port, int(os.environ.get("SERVE_CLIENTS", 512)), int(os.environ.get("SERVE_REQUESTS", 2000)))
+        elif args.workload == "arm":
+            r = arm_workload(port)
+        else:
+            r = prm_workload(port, os.environ.get("PRM_SAMPLES"), os.environ.get("PRM_STAR", "0") == "1")
+        print(json.dumps(r))
         return
     if args.profile:
         profile(args.profile)

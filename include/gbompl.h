@@ -114,6 +114,29 @@ gbo_status gbo_checker_destroy(gbo_checker *c);
 gbo_status gbo_checker_set_precision(gbo_checker *c, int precision);
 /* Re-check statistics of the last FP32_GUARDED call: states evaluated, states re-checked in FP64. */
 gbo_status gbo_checker_stats(const gbo_checker *c, uint64_t *evaluated, uint64_t *rechecked);
+/* The same counters of the last call plus its one-ulp hazards: FP64 decisions (segment-test or sphere
+ * comparisons) so close to their thresholds that a one-ulp change of a sine or cosine of the forward
+ * kinematics could reverse them. The FP64 forms use correctly rounded sin/cos; the reference calls the
+ * C library's, which differs by one ulp on a small fraction of arguments, so a call with no hazard
+ * decided every FP64 comparison as the reference does. No reference counterpart (diagnostic). */
+gbo_status gbo_checker_counters(const gbo_checker *c, uint64_t *evaluated, uint64_t *rechecked, uint64_t *hazards);
+
+/* Precision statistics of the FP32 form on a batch of states (measurement call; synchronous; allocates
+ * a small device buffer): states, flips = states whose FP32 verdict taken at face value (the reference's
+ * comparisons on the FP32 values, no guard band) differs from the FP64 verdict, ambiguous = states the
+ * guarded FP32 form hands to the FP64 re-check, max_abs_err = largest |FP32 - FP64| of the compared
+ * quantities (chain: segment-test denominators and numerators; DH arm: d^2 - (rs + ro)^2 of the listed
+ * sphere pairs). GBO_ERR_UNSUPPORTED for checkers without an FP32 form (circles, all-valid).
+ * No reference counterpart (diagnostic). */
+typedef struct
+{
+    uint64_t states;
+    uint64_t flips;
+    uint64_t ambiguous;
+    double max_abs_err;
+} gbo_precision_stats;
+gbo_status gbo_checker_precision_stats(gbo_checker *c, const double *states, int64_t n, int64_t ld, int layout,
+                                       gbo_precision_stats *out, gbo_stream stream);
 
 /* StateValidityChecker::isValid over a batch: out[i] = 1 valid, 0 invalid. */
 gbo_status gbo_is_valid(gbo_checker *c, const double *states, int64_t n, int64_t ld, int layout, uint8_t *out,
@@ -262,6 +285,9 @@ gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream);
 gbo_status gbo_sincos32(const double *theta, int64_t n, float *cos_out, float *sin_out, gbo_stream stream);
 /* FP64 FMA throughput of this GPU (FLOP/s). */
 gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
+/* Correctly rounded FP64 sin and cos (the device routine of the FP64 forms) of n device values, for
+ * tests. No reference counterpart (diagnostic). */
+gbo_status gbo_sincos_cr(const double *x, int64_t n, double *sin_out, double *cos_out, gbo_stream stream);
 /* Number of kernels this library launched since load (for launch accounting). */
 uint64_t gbo_launch_count(void);
 /* Self-test of the bounded device waits (no OMPL counterpart): a kernel waits limit_ns nanoseconds

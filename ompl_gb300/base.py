@@ -198,9 +198,21 @@ class StateValidityChecker:
         self.precision = p
 
     def stats(self):
-        e, r = C.c_uint64(), C.c_uint64()
-        check(lib().gbo_checker_stats(self._h, C.byref(e), C.byref(r)))
-        return {"evaluated": e.value, "rechecked": r.value}
+        """Counters of the last call: states evaluated, states re-checked in FP64, one-ulp hazards of
+        the FP64 decisions (gbo_checker_counters)."""
+        e, r, h = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(lib().gbo_checker_counters(self._h, C.byref(e), C.byref(r), C.byref(h)))
+        return {"evaluated": e.value, "rechecked": r.value, "hazards": h.value}
+
+    def precisionStats(self, states, soa=False, stream=None):
+        """Flip rate of the FP32 form (face-value FP32 verdict vs FP64 verdict), the guarded form's
+        ambiguous states and the largest |FP32 - FP64| of the compared quantities, on a batch of states."""
+        t, n, ld, lay = _batch(states, self.space.dim, soa)
+        out = capi.PrecisionStats()
+        check(lib().gbo_checker_precision_stats(self._h, _ptr(t), n, ld, lay, C.byref(out), _stream(stream)))
+        return {"states": out.states, "flips": out.flips, "flip_rate": out.flips / max(out.states, 1),
+                "ambiguous": out.ambiguous, "ambiguous_rate": out.ambiguous / max(out.states, 1),
+                "max_abs_err": out.max_abs_err}
 
     def isValid(self, states, soa=False, stream=None):
         t, n, ld, lay = _batch(states, self.space.dim, soa)

@@ -88,7 +88,16 @@ SIGNATURES = {
     "gbo_launch_count": (C.c_uint64, []),
     "gbo_selftest_bounded_wait": (C.c_int, [_I64, C.POINTER(C.c_double)]),
     "gbo_nn_error_stats": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "gbo_checker_counters": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "gbo_checker_precision_stats": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P]),
+    "gbo_sincos_cr": (C.c_int, [_P, _I64, _P, _P, _P]),
 }
+
+
+class PrecisionStats(C.Structure):
+    """gbo_precision_stats (include/gbompl.h)."""
+    _fields_ = [("states", C.c_uint64), ("flips", C.c_uint64), ("ambiguous", C.c_uint64),
+                ("max_abs_err", C.c_double)]
 
 
 class GboError(RuntimeError):

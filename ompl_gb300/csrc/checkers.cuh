@@ -65,6 +65,92 @@ __device__ __forceinline__ bool seg_intersect64(double ax0, double ay0, double a
     return true;
 }
 
+// ---------------------------------------------------------------- one-ulp hazards of the FP64 forms
+// The FP64 forms evaluate the reference's arithmetic on the same doubles, except that the sines and
+// cosines of the forward kinematics are correctly rounded (crtrig.cuh) where the reference calls the C
+// library, whose results differ from the correctly rounded ones by one ulp on a small fraction of
+// arguments. A decision is a hazard when a comparison lies so close to its threshold that inputs moved
+// by that much could change it: the kernels count those in RunCounters::hazards, so a run with no
+// hazard took every FP64 decision as the reference does, whatever its C library returned.
+//
+// Bound on |x'y' - xy| + roundings for inputs moved by at most dx, dy: zero when nothing moved
+// (identical inputs give identical results).
+__device__ __forceinline__ double prod_move(double x, double y, double dx, double dy)
+{
+    if (dx == 0.0 && dy == 0.0)
+        return 0.0;
+    return dx * fabs(y) + fabs(x) * dy + dx * dy + 0x1p-52 * fabs(x * y);
+}
+
+// Hazard test of the segment test of demos/KinematicChain.h:251-276 for segment a (endpoints moved by at
+// most pa per coordinate) and segment b (pb): `stage` is how far the reference's branch sequence got
+// (0: |denom| test, 1: + s_numer test, 2: + t_numer test, 3: + first final clause, 4: + second); a
+// hazard is counted on *hz. Comparisons farther than 1e-9 from their thresholds are never hazards here
+// (the bounds are below 1e-12 for coordinates of magnitude <= 4), so callers form the bounds only for
+// close comparisons.
+static __device__ __noinline__ void seg_hazard64(double ax0, double ay0, double ax1, double ay1, double bx0,
+                                                double by0, double bx1, double by1, int stage, double pa, double pb,
+                                                unsigned long long *hz)
+{
+    const double s10x = dsub(ax1, ax0), s10y = dsub(ay1, ay0);
+    const double s32x = dsub(bx1, bx0), s32y = dsub(by1, by0);
+    const double denom = dsub(dmul(s10x, s32y), dmul(s32x, s10y));
+    const double s02x = dsub(ax0, bx0), s02y = dsub(ay0, by0);
+    const double sn = dsub(dmul(s10x, s02y), dmul(s10y, s02x));
+    const double tn = dsub(dmul(s32x, s02y), dmul(s32y, s02x));
+    const double u2 = 0x1p-52;
+    const double d10x = pa > 0.0 ? 2.0 * pa + u2 * fabs(s10x) : 0.0, d10y = pa > 0.0 ? 2.0 * pa + u2 * fabs(s10y) : 0.0;
+    const double d32x = pb > 0.0 ? 2.0 * pb + u2 * fabs(s32x) : 0.0, d32y = pb > 0.0 ? 2.0 * pb + u2 * fabs(s32y) : 0.0;
+    const double pp = pa + pb;
+    const double d02x = pp > 0.0 ? pp + u2 * fabs(s02x) : 0.0, d02y = pp > 0.0 ? pp + u2 * fabs(s02y) : 0.0;
+    auto moved = [&](double m, double v) { return m == 0.0 ? 0.0 : 2.0 * (m + u2 * fabs(v)); };
+    const double e_den = moved(prod_move(s10x, s32y, d10x, d32y) + prod_move(s32x, s10y, d32x, d10y), denom);
+    const double e_s = moved(prod_move(s10x, s02y, d10x, d02y) + prod_move(s10y, s02x, d10y, d02x), sn);
+    const double e_t = moved(prod_move(s32x, s02y, d32x, d02y) + prod_move(s32y, s02x, d32y, d02x), tn);
+    bool h = fabs(fabs(denom) - kDblEps) <= e_den || fabs(denom) <= e_den;
+    h |= stage >= 1 && fabs(sn - kFltEps) <= e_s;
+    h |= stage >= 2 && fabs(tn - kFltEps) <= e_t;
+    h |= stage >= 3 && fabs(dsub(sn, denom) + kFltEps) <= moved(e_s + e_den, sn - denom);
+    h |= stage >= 4 && fabs(dsub(tn, denom) - kFltEps) <= moved(e_t + e_den, tn - denom);
+    if (h)
+        atomicAdd(hz, 1ull);
+}
+
+// seg_intersect64 that also counts a hazard (atomicAdd on *hz) when one of the comparisons it evaluated
+// lies within 1e-9 of its threshold and within the moved-input bound (seg_hazard64, out of line).
+__device__ __forceinline__ bool seg_intersect64_hz(double ax0, double ay0, double ax1, double ay1, double bx0,
+                                                   double by0, double bx1, double by1, double pa, double pb,
+                                                   unsigned long long *hz)
+{
+    const double s10_x = dsub(ax1, ax0), s10_y = dsub(ay1, ay0);
+    const double s32_x = dsub(bx1, bx0), s32_y = dsub(by1, by0);
+    const double denom = dsub(dmul(s10_x, s32_y), dmul(s32_x, s10_y));
+    const double s02_x = dsub(ax0, bx0), s02_y = dsub(ay0, by0);
+    const double s_numer = dsub(dmul(s10_x, s02_y), dmul(s10_y, s02_x));
+    const double t_numer = dsub(dmul(s32_x, s02_y), dmul(s32_y, s02_x));
+    bool result = true;
+    int stage = 0;
+    const bool denomPositive = denom > 0;
+    if (fabs(denom) < kDblEps)
+        result = false;
+    else if (stage = 1, (s_numer < kFltEps) == denomPositive)
+        result = false;
+    else if (stage = 2, (t_numer < kFltEps) == denomPositive)
+        result = false;
+    else if (stage = 3, (dsub(s_numer, denom) > -kFltEps) == denomPositive)
+        result = false;
+    else if (stage = 4, (dsub(t_numer, denom) > kFltEps) == denomPositive)
+        result = false;
+    const double near = 1e-9;
+    const bool close = fabs(fabs(denom) - kDblEps) <= near || fabs(denom) <= near ||
+                       (stage >= 1 && fabs(s_numer - kFltEps) <= near) || (stage >= 2 && fabs(t_numer - kFltEps) <= near) ||
+                       (stage >= 3 && fabs(s_numer - denom + kFltEps) <= near) ||
+                       (stage >= 4 && fabs(t_numer - denom - kFltEps) <= near);
+    if (hz && close)
+        seg_hazard64(ax0, ay0, ax1, ay1, bx0, by0, bx1, by1, stage, pa, pb, hz);
+    return result;
+}
+
 // Adjacent chain segments (i, i+1) share an endpoint, so in FP64 s02 == -s10 exactly, s_numer == +0 and
 // t_numer == denom bitwise; every branch of the test above then reports "no collision". Both forms
 // therefore skip adjacent pairs without changing any result.
@@ -81,7 +167,7 @@ __device__ __forceinline__ void chain_points64(const SpaceParams &s, const doubl
         if (i < s.dim)
         {
             theta = dadd(theta, q[i]);
-            sincos(theta, &sn, &c);
+            sincos_cr(theta, &sn, &c);
             x = dadd(x, dmul(c, s.link));
             y = dadd(y, dmul(sn, s.link));
             X[i + 1] = x;
@@ -96,9 +182,11 @@ __device__ __forceinline__ void chain_points64(const SpaceParams &s, const doubl
         }
 }
 
-// world: n rows of (x0, y0, x1, y1) doubles.
+// world: n rows of (x0, y0, x1, y1) doubles. hz_pos bounds how far a joint position can move when
+// every sine and cosine moves by one ulp; hazards are counted on *hz (nullable).
 template <int MAXD>
-__device__ bool chain_valid64(const SpaceParams &s, const double *q, const double *w, int nw)
+__device__ bool chain_valid64(const SpaceParams &s, const double *q, const double *w, int nw, double hz_pos = 0.0,
+                              unsigned long long *hz = nullptr)
 {
     double X[MAXD + 2], Y[MAXD + 2];
     chain_points64<MAXD>(s, q, X, Y);
@@ -108,14 +196,15 @@ __device__ bool chain_valid64(const SpaceParams &s, const double *q, const doubl
 #pragma unroll
         for (int j = i + 2; j < MAXD + 1; ++j)
             if (j < m)
-                if (seg_intersect64(X[i], Y[i], X[i + 1], Y[i + 1], X[j], Y[j], X[j + 1], Y[j + 1]))
+                if (seg_intersect64_hz(X[i], Y[i], X[i + 1], Y[i + 1], X[j], Y[j], X[j + 1], Y[j + 1], hz_pos, hz_pos,
+                                       hz))
                     return false;
 #pragma unroll
     for (int i = 0; i < MAXD + 1; ++i)
         if (i < m)
             for (int j = 0; j < nw; ++j)
-                if (seg_intersect64(X[i], Y[i], X[i + 1], Y[i + 1], w[4 * j], w[4 * j + 1], w[4 * j + 2],
-                                    w[4 * j + 3]))
+                if (seg_intersect64_hz(X[i], Y[i], X[i + 1], Y[i + 1], w[4 * j], w[4 * j + 1], w[4 * j + 2],
+                                       w[4 * j + 3], hz_pos, 0.0, hz))
                     return false;
     return true;
 }
@@ -127,15 +216,22 @@ __device__ bool chain_valid64(const SpaceParams &s, const double *q, const doubl
 //   lo, hi         : FLT_EPSILON - e and FLT_EPSILON + e rounded outward, e a bound on |fp32 - fp64| of
 //                    s_numer, t_numer, s_numer - denom and t_numer - denom for a link vs this segment
 //   e_den          : bound on |fp32 - fp64| of denom
+//   e              : max(hi - FLT_EPSILON, FLT_EPSILON - lo) rounded up (the warp kernels' margin form)
 struct __align__(16) ChainSegF32
 {
-    float x0, y0, sx, sy, lo, hi, e_den, pad;
+    float x0, y0, sx, sy, lo, hi, e_den, e;
 };
+
+// Null segment of the warp kernels' packed tests (chain_round.cuh): far away with a zero vector, a tiny
+// margin and e_den -1, so that every test against it is definitely clear.
+constexpr float kNullCoord = 1.0e4f;
+constexpr float kNullE = 1.0e-30f;
 
 struct ChainGuard
 {
     float eps_dir;                      // bound on |cos/sin fp32 - fp64| of one link direction
     float self_lo, self_hi, self_den;   // lo, hi, e_den of link-vs-link tests
+    float self_e;                       // max(self_hi - FLT_EPSILON, FLT_EPSILON - self_lo), rounded up
 };
 
 // Guarded segment test: returns kInvalid (definite collision), kValid (definite none) or kAmbiguous.

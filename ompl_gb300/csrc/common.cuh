@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gbompl.h"
+#include "crtrig.cuh"
 
 #define GBO_MAXD 16
 #define GBO_PI 3.141592653589793238462643383279502884
@@ -95,8 +96,8 @@ __device__ double distance64(const SpaceParams &s, const double *a, const double
                 t1 = dadd(t1, a[i]);
                 t2 = dadd(t2, b[i]);
                 double s1, c1, s2, c2;
-                sincos(t1, &s1, &c1);
-                sincos(t2, &s2, &c2);
+                sincos_cr(t1, &s1, &c1);
+                sincos_cr(t2, &s2, &c2);
                 dx = dadd(dx, dsub(c1, c2));
                 dy = dadd(dy, dsub(s1, s2));
                 dist = dadd(dist, dsqrt(dadd(dmul(dx, dx), dmul(dy, dy))));

@@ -13,6 +13,7 @@ struct RunCounters
     unsigned long long evaluated;  // states evaluated
     unsigned long long rechecked;  // states (or segment counts / kNN queries) re-evaluated in FP64
     unsigned long long fallbacks;  // kNN queries answered by the exact FP64 scan
+    unsigned long long hazards;    // FP64 decisions a one-ulp change of a sine or cosine could reverse
     unsigned int max_err_bits;     // kNN: largest |FP32 - FP64| distance of a re-checked candidate (float bits)
     unsigned int timeout;          // a bounded wait ran out
     unsigned int error;
@@ -51,7 +52,16 @@ struct WorldArgs
     double glo64[3], ginv64[3];
     float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere test near contact
     float dh_qmax;  // largest |joint angle| the FP32 guard covers (larger: FP64)
-    const unsigned *test_order;  // kinematic chain: segment-test order (likely intersections first)
+    // one-ulp hazard bounds of the FP64 forms (checkers.cuh): how far a chain joint position / a DH sphere
+    // centre (Euclidean) can move when every sine and cosine of the forward kinematics moves by one ulp
+    double hz_pos;
+    double hz_dh;
+    // kinematic chain, warp kernels (chain_round.cuh): world segment pairs (+ a null pair), 48 bytes
+    // each, and the round order
+    const void *wpair;
+    int n_pairs;
+    const unsigned short *units;
+    int n_units, n_self_units;
 };
 
 struct LaunchCfg
@@ -86,13 +96,29 @@ void launch_motion_states(const LaunchCfg &lc, const SpaceParams &sp, StatesView
                           unsigned count, int endpoints, MutStatesView out);
 void launch_gather_rows(const LaunchCfg &lc, StatesView src, const int64_t *idx, int64_t n, int dim,
                         MutStatesView out);
+bool launch_precision_stats(const LaunchCfg &lc, const SpaceParams &sp, const WorldArgs &wa, StatesView v, int64_t n,
+                            void *tally);
+void launch_sincos_cr(const LaunchCfg &lc, const double *x, int64_t n, double *s, double *c);
 
 // ---------------------------------------------------------------- DH sphere arm
 // FP64 form: the arm definition (this operation order for the sphere centres is the definition the
 // test oracle restates), candidates from the uniform grid (a superset of every colliding sphere),
 // exact test.
+// Hazard test of one FP64 sphere pair (see checkers.cuh): t = |d|^2 with d moved by at most P.
+__device__ __forceinline__ void dh_hazard64(double dx, double dy, double dz, double t, double rr2, double P,
+                                            unsigned long long *hz)
+{
+    if (hz && fabs(t - rr2) <= 1e-9)
+    {
+        const double e = 2.0 * (2.0 * (fabs(dx) + fabs(dy) + fabs(dz)) * P + 3.0 * P * P + 0x1p-51 * (t + rr2));
+        if (fabs(t - rr2) <= e)
+            atomicAdd(hz, 1ull);
+    }
+}
+
 template <int MAXD>
-__device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, const WorldArgs &wa)
+__device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, const WorldArgs &wa,
+                           unsigned long long *hz = nullptr)
 {
     double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     double p[3] = {0, 0, 0};
@@ -101,7 +127,7 @@ __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, c
     for (int i = 0; i < arm.joints; ++i)
     {
         double cq, sq;
-        sincos(q[i], &sq, &cq);
+        sincos_cr(q[i], &sq, &cq);
         const double ca = (double)arm.ca[i], sa = (double)arm.sa[i];
         const double A[3][3] = {{cq, dmul(-sq, ca), dmul(sq, sa)}, {sq, dmul(cq, ca), dmul(-cq, sa)}, {0.0, sa, ca}};
         const double pA[3] = {dmul(arm.a[i], cq), dmul(arm.a[i], sq), arm.d[i]};
@@ -142,7 +168,9 @@ __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, c
                 double dy = dsub(c[1], o[1]);
                 double dz = dsub(c[2], o[2]);
                 double rr = dadd(arm.rs, o[3]);
-                if (dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < dmul(rr, rr))
+                const double t = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), rr2 = dmul(rr, rr);
+                dh_hazard64(dx, dy, dz, t, rr2, wa.hz_dh, hz);
+                if (t < rr2)
                     return false;
             }
         }
@@ -164,7 +192,8 @@ __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, c
 // lanes, each centre and each pair test in the operation order of dh_valid64. Same boolean as
 // dh_valid64 on the same state. Out of line: the callers' FP32 loops keep their registers.
 static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const double *q, const double *w,
-                                                    const WorldArgs &wa, double (*pos)[3], int lane)
+                                                    const WorldArgs &wa, double (*pos)[3], int lane,
+                                                    unsigned long long *hz)
 {
     double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     double p[3] = {0, 0, 0};
@@ -175,7 +204,7 @@ static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const doub
     for (int i = 0; i < arm.joints; ++i)
     {
         double cq, sq;
-        sincos(q[i], &sq, &cq);
+        sincos_cr(q[i], &sq, &cq);
         const double ca = (double)arm.ca[i], sa = (double)arm.sa[i];
         const double A[3][3] = {{cq, dmul(-sq, ca), dmul(sq, sa)}, {sq, dmul(cq, ca), dmul(-cq, sa)}, {0.0, sa, ca}};
         const double pA[3] = {dmul(arm.a[i], cq), dmul(arm.a[i], sq), arm.d[i]};
@@ -226,7 +255,9 @@ static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const doub
             const double *o = w + 4 * wa.cell_items[it];
             const double dx = dsub(c[0], o[0]), dy = dsub(c[1], o[1]), dz = dsub(c[2], o[2]);
             const double rr = dadd(arm.rs, o[3]);
-            hit = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < dmul(rr, rr);
+            const double t = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), rr2 = dmul(rr, rr);
+            dh_hazard64(dx, dy, dz, t, rr2, wa.hz_dh, hz);
+            hit = t < rr2;
         }
     }
     return __any_sync(0xffffffffu, hit);

@@ -82,15 +82,16 @@ struct Eval
     int nw = 0;
     ChainGuard g{};
     const WorldArgs *wa = nullptr;
+    unsigned long long *hz = nullptr;  // hazard counter of the launch (RunCounters::hazards)
 
     __device__ bool valid64(const SpaceParams &s, const double *q) const
     {
         if constexpr (CK == GBO_CHECK_CIRCLES)
             return circles_valid64(w64, nw, q[0], q[1]);
         else if constexpr (CK == GBO_CHECK_CHAIN_SEGMENTS)
-            return chain_valid64<MAXD>(s, q, w64, nw);
+            return chain_valid64<MAXD>(s, q, w64, nw, wa->hz_pos, hz);
         else if constexpr (CK == GBO_CHECK_DH_SPHERES)
-            return dh_valid64<MAXD>(*arm, q, w64, *wa);
+            return dh_valid64<MAXD>(*arm, q, w64, *wa, hz);
         else
             return true;
     }
@@ -158,6 +159,7 @@ __device__ bool setup_world(const WorldArgs &wa, unsigned char *smem, uint64_t *
     ev.g = wa.guard;
     ev.wa = &wa;
     ev.arm = &wa.arm;
+    ev.hz = ctr ? &ctr->hazards : nullptr;
     unsigned char *p = smem;
     if (PREC == GBO_PRECISION_FP32_GUARDED && (CK == GBO_CHECK_CHAIN_SEGMENTS || CK == GBO_CHECK_DH_SPHERES))
     {
@@ -293,7 +295,7 @@ __device__ __forceinline__ int resolve_warp(const Eval<CK, MAXD> &ev, int r, int
         if (lane == src)
             state_of(wq);
         __syncwarp();
-        const bool hit = dh_valid64_warp(*ev.arm, wq, ev.w64, *ev.wa, wpos, lane);
+        const bool hit = dh_valid64_warp(*ev.arm, wq, ev.w64, *ev.wa, wpos, lane, ev.hz);
         if (lane == src)
         {
             r = hit ? kInvalid : kValid;

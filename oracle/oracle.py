@@ -275,3 +275,47 @@ class Oracle:
         self.lib.ora_radius(C.byref(s), algo, _dp(pts), C.c_long(pts.shape[0]), _dp(q), C.c_long(nq), C.c_double(r),
                             counts.ctypes.data_as(lp), idx.ctypes.data_as(lp), _dp(dist), C.c_long(total))
         return counts, idx[:total], dist[:total]
+
+    # ---- restatement-only entry points (absent from the reference build)
+    def is_valid_brute(self, sp, ck, states):
+        """isValid with every robot sphere tested against every world sphere (no grid)."""
+        st = _rows(states, sp.dim)
+        out = np.empty(st.shape[0], dtype=np.uint8)
+        s, c = sp.c(), ck.c()
+        self.lib.ora_is_valid_brute(C.byref(s), C.byref(c), _dp(st), C.c_long(st.shape[0]),
+                                    out.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        return out
+
+    def sincos_rn(self, x):
+        """Correctly rounded sin and cos (double-double evaluation); returns (sin, cos, undecided)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        s, c = np.empty_like(x), np.empty_like(x)
+        self.lib.ora_sincos_rn.restype = C.c_long
+        hard = self.lib.ora_sincos_rn(_dp(x), C.c_long(x.size), _dp(s), _dp(c))
+        return s, c, int(hard)
+
+    def trig_rounding(self, x):
+        """The C library's sin/cos against the correctly rounded values on x: dict(sin_misrounded,
+        cos_misrounded, undecided, max_ulps)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        counts = np.zeros(4, dtype=np.int64)
+        self.lib.ora_trig_rounding(_dp(x), C.c_long(x.size), counts.ctypes.data_as(C.POINTER(C.c_long)))
+        return dict(sin_misrounded=int(counts[0]), cos_misrounded=int(counts[1]), undecided=int(counts[2]),
+                    max_ulps=int(counts[3]))
+
+    def prm_roadmap(self, sp, ck, seed, n_samples, k=10, edge_cap=None):
+        """PRM roadmap (restatement): dict(sample_index, edge_src, edge_dst, candidates)."""
+        cap = int(edge_cap if edge_cap is not None else n_samples * k)
+        si = np.empty(n_samples, dtype=np.int64)
+        es = np.empty(max(cap, 1), dtype=np.int64)
+        ed = np.empty(max(cap, 1), dtype=np.int64)
+        nm, cand = C.c_long(0), C.c_long(0)
+        s, c = sp.c(), ck.c()
+        lp = C.POINTER(C.c_long)
+        self.lib.ora_prm_roadmap.restype = C.c_long
+        ne = self.lib.ora_prm_roadmap(C.byref(s), C.byref(c), C.c_uint(seed), C.c_long(n_samples), C.c_int(k),
+                                      C.byref(nm), si.ctypes.data_as(lp), es.ctypes.data_as(lp),
+                                      ed.ctypes.data_as(lp), C.c_long(cap), C.byref(cand))
+        if ne > cap:
+            raise RuntimeError(f"edge capacity {cap} < {ne}")
+        return dict(sample_index=si[:nm.value], edge_src=es[:ne], edge_dst=ed[:ne], candidates=int(cand.value))

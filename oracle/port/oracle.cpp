@@ -325,8 +325,136 @@ bool chain_valid(const Space &s, const ora_checker *c, const double *q)
     return true;
 }
 
-bool is_valid(const Space &s, const ora_checker *c, const double *q)
+// Uniform-grid broad phase for the DH sphere checker (a speed-up of this restatement only; the
+// boolean is that of gbompl_oracle::dh_valid, which tests every robot sphere against every world
+// sphere). World sphere o is listed in every cell that its box [o - R, o + R] reaches, with R =
+// r_o + r_robot + 1e-6; cells are found with the monotone map floor((v - x0) / h), so a robot
+// sphere centre inside that box always lands in a listed cell, and a centre outside every box
+// (including outside the grid) is more than r_o + r_robot + 1e-6 from every world centre, where the
+// FP64 narrow phase cannot report a hit. The narrow phase of the listed candidates is
+// dh_valid's expression, evaluated on the same centres.
+struct DhGrid
 {
+    double x0[3] = {0, 0, 0}, inv_h = 1.0;
+    int nc = 0;
+    std::vector<int> start, items;
+
+    int cell_coord(double v, int a) const
+    {
+        double f = std::floor((v - x0[a]) * inv_h);
+        return f < 0.0 ? -1 : (f >= (double)nc ? nc : (int)f);
+    }
+
+    void build(const ora_checker *c)
+    {
+        const long n = c->n_obstacles;
+        if (n <= 0)
+            return;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (long j = 0; j < n; ++j)
+        {
+            const double *o = c->obstacles + 4 * j;
+            const double R = o[3] + c->sphere_radius + 1e-6;
+            for (int a = 0; a < 3; ++a)
+            {
+                lo[a] = std::min(lo[a], o[a] - R);
+                hi[a] = std::max(hi[a], o[a] + R);
+            }
+        }
+        nc = (int)std::min(64.0, std::max(4.0, std::ceil(1.5 * std::cbrt((double)n))));
+        double ext = 0.0;
+        for (int a = 0; a < 3; ++a)
+            ext = std::max(ext, hi[a] - lo[a]);
+        const double h = ext * (1.0 + 1e-9) / nc;
+        inv_h = 1.0 / h;
+        for (int a = 0; a < 3; ++a)
+            x0[a] = lo[a];
+        const size_t cells = (size_t)nc * nc * nc;
+        std::vector<int> count(cells + 1, 0);
+        auto each = [&](long j, auto f) {
+            const double *o = c->obstacles + 4 * j;
+            const double R = o[3] + c->sphere_radius + 1e-6;
+            int l[3], u[3];
+            for (int a = 0; a < 3; ++a)
+            {
+                l[a] = std::max(0, cell_coord(o[a] - R, a));
+                u[a] = std::min(nc - 1, cell_coord(o[a] + R, a));
+            }
+            for (int x = l[0]; x <= u[0]; ++x)
+                for (int y = l[1]; y <= u[1]; ++y)
+                    for (int z = l[2]; z <= u[2]; ++z)
+                        f(((size_t)x * nc + y) * nc + z);
+        };
+        for (long j = 0; j < n; ++j)
+            each(j, [&](size_t cell) { count[cell + 1]++; });
+        start.assign(cells + 1, 0);
+        for (size_t i = 0; i < cells; ++i)
+            start[i + 1] = start[i] + count[i + 1];
+        items.resize((size_t)start[cells]);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (long j = 0; j < n; ++j)
+            each(j, [&](size_t cell) { items[(size_t)fill[cell]++] = (int)j; });
+    }
+
+    bool valid(const ora_checker *c, const double *q) const
+    {
+        const int ns = c->n_joints * c->spheres_per_link;
+        double ctr[3 * 64 * 16];
+        std::vector<double> big;
+        double *cp = ctr;
+        if (ns > 64 * 16)
+        {
+            big.resize(3 * (size_t)ns);
+            cp = big.data();
+        }
+        gbompl_oracle::dh_sphere_centres(c, q, cp);
+        const double rs = c->sphere_radius;
+        for (int s = 0; s < ns; ++s)
+        {
+            const double *p = cp + 3 * s;
+            int ix = cell_coord(p[0], 0), iy = cell_coord(p[1], 1), iz = cell_coord(p[2], 2);
+            if (ix < 0 || iy < 0 || iz < 0 || ix >= nc || iy >= nc || iz >= nc)
+                continue;
+            const size_t cell = ((size_t)ix * nc + iy) * nc + iz;
+            for (int t = start[cell]; t < start[cell + 1]; ++t)
+            {
+                const double *o = c->obstacles + 4 * (size_t)items[(size_t)t];
+                double dx = p[0] - o[0];
+                double dy = p[1] - o[1];
+                double dz = p[2] - o[2];
+                double rr = rs + o[3];
+                if ((dx * dx + dy * dy) + dz * dz < rr * rr)
+                    return false;
+            }
+        }
+        return true;
+    }
+};
+
+// A checker as the batch calls use it: the description plus, for the DH arm, its grid.
+struct Checker
+{
+    const ora_checker *c;
+    DhGrid grid;
+    bool use_grid = false;
+};
+
+Checker make_checker(const ora_checker *c, bool brute = false)
+{
+    Checker k;
+    k.c = c;
+    if (c->kind == ORA_CHECK_DH_SPHERES && !brute && c->n_obstacles > 64 && c->spheres_per_link <= 16 &&
+        c->n_joints <= 64)
+    {
+        k.grid.build(c);
+        k.use_grid = true;
+    }
+    return k;
+}
+
+bool is_valid(const Space &s, const Checker &k, const double *q)
+{
+    const ora_checker *c = k.c;
     switch (c->kind)
     {
         case ORA_CHECK_CIRCLES:
@@ -334,14 +462,14 @@ bool is_valid(const Space &s, const ora_checker *c, const double *q)
         case ORA_CHECK_CHAIN_SEGMENTS:
             return chain_valid(s, c, q);
         case ORA_CHECK_DH_SPHERES:
-            return gbompl_oracle::dh_valid(c, q);
+            return k.use_grid ? k.grid.valid(c, q) : gbompl_oracle::dh_valid(c, q);
         default:
             return true;
     }
 }
 
 // DMV:48-91 (ordered variant). Returns result; fills lastValid.second, nd and the first invalid index.
-bool check_motion_ordered(const Space &s, const ora_checker *c, const double *s1, const double *s2, double &last_t,
+bool check_motion_ordered(const Space &s, const Checker &c, const double *s1, const double *s2, double &last_t,
                           int &nd_out, int &first_j)
 {
     bool result = true;
@@ -374,7 +502,7 @@ bool check_motion_ordered(const Space &s, const ora_checker *c, const double *s1
 }
 
 // DMV:93-145 (bisection variant): s2 first, then FIFO midpoint subdivision of [1, nd-1].
-bool check_motion_bisect(const Space &s, const ora_checker *c, const double *s1, const double *s2)
+bool check_motion_bisect(const Space &s, const Checker &c, const double *s1, const double *s2)
 {
     if (!is_valid(s, c, s2))
         return false;
@@ -423,6 +551,128 @@ void knn_one(const Space &s, const double *pts, long npts, long limit, const dou
         dist[j] = j < kk ? all[j].first : std::numeric_limits<double>::infinity();
     }
 }
+
+// Chain metric with per-row link directions precomputed: KC:105-121 evaluates cos/sin of
+// theta = q_0 + ... + q_i of each argument inside the pair loop; here theta is accumulated in the
+// same order once per row and the pair loop performs the same additions, square roots and final
+// multiplication on the same values, so distances are bitwise those of distance().
+struct ChainTrig
+{
+    int dim = 0;
+    std::vector<double> cs;  // per row: cos(theta_0..theta_{dim-1}), then sin(...)
+    const double *row(long r) const { return cs.data() + (size_t)r * 2 * dim; }
+};
+
+ChainTrig chain_trig(const Space &s, const double *rows, long n)
+{
+    ChainTrig t;
+    t.dim = s.dim;
+    t.cs.resize((size_t)n * 2 * s.dim);
+    parallel_rows(n, [&](long r) {
+        const double *q = rows + (size_t)r * s.dim;
+        double *o = t.cs.data() + (size_t)r * 2 * s.dim;
+        double theta = 0.;
+        for (int i = 0; i < s.dim; ++i)
+        {
+            theta += q[i];
+            o[i] = std::cos(theta);
+            o[s.dim + i] = std::sin(theta);
+        }
+    });
+    return t;
+}
+
+inline double chain_distance_pre(const Space &s, const double *a, const double *b)
+{
+    const int n = s.dim;
+    double dx = 0., dy = 0., dist = 0.;
+    for (int i = 0; i < n; ++i)
+    {
+        dx += a[i] - b[i];
+        dy += a[n + i] - b[n + i];
+        dist += std::sqrt(dx * dx + dy * dy);
+    }
+    return dist * s.link;
+}
+
+// distance(point j, query i) of the batch calls, with the chain's precomputed directions.
+struct PairMetric
+{
+    const Space &s;
+    const double *pts, *q;
+    ChainTrig tp, tq;
+    bool chain;
+    PairMetric(const Space &s_, const double *p, long np, const double *q_, long nq)
+        : s(s_), pts(p), q(q_), chain(s_.kind == ORA_SPACE_KINEMATIC_CHAIN)
+    {
+        if (chain)
+        {
+            tp = chain_trig(s, p, np);
+            tq = chain_trig(s, q_, nq);
+        }
+    }
+    double operator()(long j, long i) const
+    {
+        if (chain)
+            return chain_distance_pre(s, tp.row(j), tq.row(i));
+        return distance(s, pts + (size_t)j * s.dim, q + (size_t)i * s.dim);
+    }
+};
+
+// Exact k nearest by (distance, insertion index) for every query, each query seeing the points
+// [0, limit[i]) (all points when limit is null): tiles of 32 queries scan tiles of 2048 points so that
+// a point tile stays in cache for the whole query tile. Points are visited in increasing index, so a
+// point whose distance equals the current k-th never enters (the earlier index wins the tie), which is
+// the (distance, index) order of knn_one.
+void knn_blocked(const PairMetric &m, long npts, long nq, const long *limit, int k, long *idx, double *dist)
+{
+    const long QT = 32, PT = 2048;
+    const long tiles = (nq + QT - 1) / QT;
+    parallel_rows(tiles, [&](long t) {
+        const long q0 = t * QT, q1 = std::min(nq, q0 + QT);
+        std::vector<double> kd((size_t)(q1 - q0) * k);
+        std::vector<long> ki((size_t)(q1 - q0) * k);
+        std::vector<int> cnt((size_t)(q1 - q0), 0);
+        long lmax = 0;
+        for (long i = q0; i < q1; ++i)
+            lmax = std::max(lmax, limit ? std::min(limit[i], npts) : npts);
+        for (long p0 = 0; p0 < lmax; p0 += PT)
+        {
+            const long p1 = std::min(lmax, p0 + PT);
+            for (long i = q0; i < q1; ++i)
+            {
+                const long lim = std::min(p1, limit ? std::min(limit[i], npts) : npts);
+                double *D = kd.data() + (size_t)(i - q0) * k;
+                long *I = ki.data() + (size_t)(i - q0) * k;
+                int &c = cnt[(size_t)(i - q0)];
+                for (long j = p0; j < lim; ++j)
+                {
+                    const double d = m(j, i);
+                    if (c == k && !(d < D[k - 1]))
+                        continue;
+                    int pos = c < k ? c++ : k - 1;
+                    while (pos > 0 && d < D[pos - 1])
+                    {
+                        D[pos] = D[pos - 1];
+                        I[pos] = I[pos - 1];
+                        --pos;
+                    }
+                    D[pos] = d;
+                    I[pos] = j;
+                }
+            }
+        }
+        for (long i = q0; i < q1; ++i)
+            for (int j = 0; j < k; ++j)
+            {
+                const int c = cnt[(size_t)(i - q0)];
+                idx[(size_t)i * k + j] = j < c ? ki[(size_t)(i - q0) * k + j] : -1;
+                dist[(size_t)i * k + j] =
+                    j < c ? kd[(size_t)(i - q0) * k + j] : std::numeric_limits<double>::infinity();
+            }
+    });
+}
+
 }  // namespace
 
 extern "C" {
@@ -690,7 +940,15 @@ void ora_sample_script(const ora_space *d, unsigned seed, const int *kinds, cons
 void ora_is_valid(const ora_space *d, const ora_checker *c, const double *states, long n, unsigned char *out)
 {
     Space s = make_space(d);
-    parallel_rows(n, [&](long i) { out[i] = is_valid(s, c, states + (size_t)i * s.dim) ? 1 : 0; });
+    Checker k = make_checker(c);
+    parallel_rows(n, [&](long i) { out[i] = is_valid(s, k, states + (size_t)i * s.dim) ? 1 : 0; });
+}
+
+void ora_is_valid_brute(const ora_space *d, const ora_checker *c, const double *states, long n, unsigned char *out)
+{
+    Space s = make_space(d);
+    Checker k = make_checker(c, true);
+    parallel_rows(n, [&](long i) { out[i] = is_valid(s, k, states + (size_t)i * s.dim) ? 1 : 0; });
 }
 
 void ora_check_motion(const ora_space *d, const ora_checker *c, const double *s1, const double *s2, long n,
@@ -698,15 +956,16 @@ void ora_check_motion(const ora_space *d, const ora_checker *c, const double *s1
                       int *first_j)
 {
     Space s = make_space(d);
+    Checker k = make_checker(c);
     parallel_rows(n, [&](long i) {
         const double *a = s1 + (size_t)i * s.dim, *b = s2 + (size_t)i * s.dim;
         double lt = kNaN;
         int ndi = 0, fj = -1;
-        bool r = check_motion_ordered(s, c, a, b, lt, ndi, fj);
+        bool r = check_motion_ordered(s, k, a, b, lt, ndi, fj);
         if (ok)
             ok[i] = r ? 1 : 0;
         if (ok_bisect)
-            ok_bisect[i] = check_motion_bisect(s, c, a, b) ? 1 : 0;
+            ok_bisect[i] = check_motion_bisect(s, k, a, b) ? 1 : 0;
         if (last_t)
             last_t[i] = lt;
         if (nd)
@@ -730,7 +989,8 @@ int ora_check_motion_states(const ora_space *d, const ora_checker *c, const doub
                             long *first_invalid, int *ok_bisect)
 {
     Space s = make_space(d);
-    auto valid = [&](long i) { return is_valid(s, c, states + (size_t)i * s.dim); };
+    Checker k = make_checker(c);
+    auto valid = [&](long i) { return is_valid(s, k, states + (size_t)i * s.dim); };
     if (ok_bisect)
     {
         bool res = true;
@@ -817,18 +1077,16 @@ void ora_knn(const ora_space *d, int algo, const double *pts, long npts, const d
 {
     (void)algo;  // the restatement implements the exact (distance, index) order only
     Space s = make_space(d);
-    parallel_rows(nq, [&](long i) {
-        knn_one(s, pts, npts, npts, q + (size_t)i * s.dim, k, idx + (size_t)i * k, dist + (size_t)i * k);
-    });
+    PairMetric m(s, pts, npts, q, nq);
+    knn_blocked(m, npts, nq, nullptr, k, idx, dist);
 }
 
 void ora_knn_prefix(const ora_space *d, const double *pts, long npts, const double *q, const long *limit, long nq,
                     int k, long *idx, double *dist)
 {
     Space s = make_space(d);
-    parallel_rows(nq, [&](long i) {
-        knn_one(s, pts, npts, limit[i], q + (size_t)i * s.dim, k, idx + (size_t)i * k, dist + (size_t)i * k);
-    });
+    PairMetric m(s, pts, npts, q, nq);
+    knn_blocked(m, npts, nq, limit, k, idx, dist);
 }
 
 // NNL:135-142: keep distance(point, query) <= r, sorted ascending; ties by insertion index.
@@ -837,12 +1095,12 @@ long ora_radius(const ora_space *d, int algo, const double *pts, long npts, cons
 {
     (void)algo;
     Space s = make_space(d);
+    PairMetric m(s, pts, npts, q, nq);
     std::vector<std::vector<std::pair<double, long>>> res(nq);
     parallel_rows(nq, [&](long i) {
-        const double *qq = q + (size_t)i * s.dim;
         for (long j = 0; j < npts; ++j)
         {
-            double dd = distance(s, pts + (size_t)j * s.dim, qq);
+            double dd = m(j, i);
             if (dd <= r)
                 res[i].emplace_back(dd, j);
         }
@@ -863,6 +1121,234 @@ long ora_radius(const ora_space *d, int algo, const double *pts, long npts, cons
         }
     }
     return total;
+}
+
+}  // extern "C"
+
+namespace
+{
+// ------------------------------------------------ correctly rounded sin / cos (double-double)
+// Used to measure how often the C library's sin/cos differ from the correctly rounded value
+// (ora_trig_rounding). Method: Cody and Waite's additive reduction x = k*pi/2 + y with pi/2 split
+// into four doubles (C1, C2: 33 significant bits, so k*C1 and k*C2 are exact for |k| < 2^20; C3, C4:
+// 53 bits; x - k*C1 is exact by Sterbenz's lemma), y carried as a double-double; then the Taylor
+// series sin y = y * sum (-1)^n y^2n/(2n+1)! (n <= 14) and cos y = sum (-1)^n y^2n/(2n)! (n <= 15)
+// evaluated by Horner's rule in double-double (truncation < 1e-33 for |y| <= pi/4); the quadrant
+// k mod 4 picks +-sin y or +-cos y. Constants: pi/2's splits and the coefficients rounded to
+// double-doubles (hi = nearest double, lo = nearest double to the remainder), as derived from their
+// definitions with 400-bit arithmetic. A result whose double-double is within 2^-98 relative of a
+// rounding boundary is reported as undecided (never met on the tested arguments).
+const double kC1 = 0x1.921fb54400000p+0, kC2 = 0x1.0b4611a600000p-34, kC3 = 0x1.3198a2e037073p-69,
+             kC4 = 0x1.129024e088a68p-123, kTwoOverPi = 0x1.45f306dc9c883p-1;
+const DD kSinC[15] = {{0x1.0000000000000p+0, 0.0},
+                      {-0x1.5555555555555p-3, -0x1.5555555555555p-57},
+                      {0x1.1111111111111p-7, 0x1.1111111111111p-63},
+                      {-0x1.a01a01a01a01ap-13, -0x1.a01a01a01a01ap-73},
+                      {0x1.71de3a556c734p-19, -0x1.c154f8ddc6c00p-73},
+                      {-0x1.ae64567f544e4p-26, 0x1.c062e06d1f209p-80},
+                      {0x1.6124613a86d09p-33, 0x1.f28e0cc748ebep-87},
+                      {-0x1.ae7f3e733b81fp-41, -0x1.1d8656b0ee8cbp-97},
+                      {0x1.952c77030ad4ap-49, 0x1.ac981465ddc6cp-103},
+                      {-0x1.2f49b46814157p-57, -0x1.2650f61dbdcb4p-112},
+                      {0x1.71b8ef6dcf572p-66, -0x1.d043ae40c4647p-120},
+                      {-0x1.761b41316381ap-75, 0x1.3423c7d91404fp-130},
+                      {0x1.3f3ccdd165fa9p-84, -0x1.58ddadf344487p-139},
+                      {-0x1.d1ab1c2dccea3p-94, -0x1.054d0c78aea14p-149},
+                      {0x1.259f98b4358adp-103, 0x1.eaf8c39dd9bc5p-157}};
+const DD kCosC[16] = {{0x1.0000000000000p+0, 0.0},
+                      {-0x1.0000000000000p-1, 0.0},
+                      {0x1.5555555555555p-5, 0x1.5555555555555p-59},
+                      {-0x1.6c16c16c16c17p-10, 0x1.f49f49f49f49fp-65},
+                      {0x1.a01a01a01a01ap-16, 0x1.a01a01a01a01ap-76},
+                      {-0x1.27e4fb7789f5cp-22, -0x1.cbbc05b4fa99ap-76},
+                      {0x1.1eed8eff8d898p-29, -0x1.2aec959e14c06p-83},
+                      {-0x1.93974a8c07c9dp-37, -0x1.05d6f8a2efd1fp-92},
+                      {0x1.ae7f3e733b81fp-45, 0x1.1d8656b0ee8cbp-101},
+                      {-0x1.6827863b97d97p-53, -0x1.eec01221a8b0bp-107},
+                      {0x1.e542ba4020225p-62, 0x1.ea72b4afe3c2fp-120},
+                      {-0x1.0ce396db7f853p-70, 0x1.aebcdbd20331cp-124},
+                      {0x1.f2cf01972f578p-80, -0x1.9ada5fcc1ab14p-135},
+                      {-0x1.88e85fc6a4e5ap-89, 0x1.71c37ebd16540p-143},
+                      {0x1.0a18a2635085dp-98, 0x1.b9e2e28e1aa54p-153},
+                      {-0x1.3932c5047d60ep-108, -0x1.832b7b530a627p-162}};
+
+// Rounds a normalized double-double to the nearest double; `hard` is set when the double-double is
+// too close to a rounding boundary for its own error (2^-98 relative) to settle the rounding.
+double dd_round(DD v, bool &hard)
+{
+    const DD r = fast_two_sum(v.hi, v.lo);
+    const double h = r.hi;
+    if (h == 0.0 || !std::isfinite(h))
+        return h;
+    const double up = std::nextafter(h, HUGE_VAL) - h, dn = h - std::nextafter(h, -HUGE_VAL);
+    const double tol = std::fabs(h) * 0x1p-98;
+    if (std::fabs(std::fabs(r.lo) - 0.5 * (r.lo > 0 ? up : dn)) <= tol)
+        hard = true;
+    return h;
+}
+
+// sin and cos of x (|x| < 2^20) as double-doubles.
+void dd_sincos(double x, DD &sn, DD &cs)
+{
+    const double k = std::nearbyint(x * kTwoOverPi);
+    const double r = x - k * kC1;                     // exact
+    DD y = two_sum(r, -(k * kC2));                    // k*C2 exact
+    const double p3 = k * kC3, e3 = std::fma(k, kC3, -p3);
+    y = dd_add(y, {-p3, -e3});
+    y = dd_add(y, {-(k * kC4), 0.0});
+    const DD z = dd_mul(y, y);
+    DD s = kSinC[14];
+    for (int n = 13; n >= 0; --n)
+        s = dd_add(dd_mul(s, z), kSinC[n]);
+    s = dd_mul(s, y);
+    DD c = kCosC[15];
+    for (int n = 14; n >= 0; --n)
+        c = dd_add(dd_mul(c, z), kCosC[n]);
+    const long q = (long)k & 3;
+    const DD ns{-s.hi, -s.lo}, nc{-c.hi, -c.lo};
+    sn = q == 0 ? s : (q == 1 ? c : (q == 2 ? ns : nc));
+    cs = q == 0 ? c : (q == 1 ? ns : (q == 2 ? nc : s));
+}
+}  // namespace
+
+extern "C" {
+
+// Correctly rounded sin/cos (restatement above): out_s/out_c per argument; returns the number of
+// arguments whose rounding the double-double could not settle (their outputs are the nearest
+// double to the double-double).
+long ora_sincos_rn(const double *x, long n, double *out_s, double *out_c)
+{
+    std::atomic<long> hard{0};
+    parallel_rows(n, [&](long i) {
+        DD s, c;
+        dd_sincos(x[i], s, c);
+        bool h = false;
+        out_s[i] = dd_round(s, h);
+        out_c[i] = dd_round(c, h);
+        if (h)
+            hard++;
+    });
+    return hard.load();
+}
+
+// How often the C library's sin and cos differ from the correctly rounded value on x[0..n):
+// counts[0] = sin misrounded, counts[1] = cos misrounded, counts[2] = undecided roundings (skipped),
+// counts[3] = largest difference in units in the last place seen.
+void ora_trig_rounding(const double *x, long n, long *counts)
+{
+    std::atomic<long> ms{0}, mc{0}, hard{0}, worst{0};
+    parallel_rows(n, [&](long i) {
+        DD s, c;
+        dd_sincos(x[i], s, c);
+        bool h = false;
+        const double rs = dd_round(s, h), rc = dd_round(c, h);
+        if (h)
+        {
+            hard++;
+            return;
+        }
+        const double ls = std::sin(x[i]), lc = std::cos(x[i]);
+        auto ulps = [](double a, double b) {
+            long d = 0;
+            while (a != b && d < 1000)
+            {
+                a = std::nextafter(a, b);
+                ++d;
+            }
+            return d;
+        };
+        if (ls != rs)
+        {
+            ms++;
+            long u = ulps(ls, rs);
+            long w = worst.load();
+            while (u > w && !worst.compare_exchange_weak(w, u))
+            {
+            }
+        }
+        if (lc != rc)
+        {
+            mc++;
+            long u = ulps(lc, rc);
+            long w = worst.load();
+            while (u > w && !worst.compare_exchange_weak(w, u))
+            {
+            }
+        }
+    });
+    counts[0] = ms.load();
+    counts[1] = mc.load();
+    counts[2] = hard.load();
+    counts[3] = worst.load();
+}
+
+// PRM roadmap (geometric/planners/prm/src/PRM.cpp:570-604 with KStrategy k, ConnectionStrategy.h:77-81,
+// and the default connection filter): n_samples draws of the space's uniform sampler seeded with
+// `seed` (the sampler of ora_sample_uniform); milestone m = the m-th valid sample; its neighbours are
+// the k nearest among milestones 0..m-1 by (distance, index); every neighbour n is connected when
+// the ordered DiscreteMotionValidator accepts the motion n -> m. Writes the milestones' sample
+// indices (capacity n_samples) and the accepted edges (src = n, dst = m) in attempt order (m
+// ascending, neighbours by increasing distance), at most edge_cap of them; returns the number of
+// accepted edges; *candidates = connection attempts, *n_milestones = milestones.
+long ora_prm_roadmap(const ora_space *d, const ora_checker *c, unsigned seed, long n_samples, int k,
+                     long *n_milestones, long *sample_index, long *edge_src, long *edge_dst, long edge_cap,
+                     long *candidates)
+{
+    Space s = make_space(d);
+    Checker chk = make_checker(c);
+    std::vector<double> samples((size_t)n_samples * s.dim);
+    ora_sample_uniform(d, seed, n_samples, samples.data());
+    std::vector<unsigned char> valid((size_t)n_samples);
+    parallel_rows(n_samples, [&](long i) { valid[(size_t)i] = is_valid(s, chk, samples.data() + (size_t)i * s.dim); });
+    std::vector<double> ms;
+    long m = 0;
+    for (long i = 0; i < n_samples; ++i)
+        if (valid[(size_t)i])
+        {
+            sample_index[m++] = i;
+            ms.insert(ms.end(), samples.begin() + (size_t)i * s.dim, samples.begin() + (size_t)(i + 1) * s.dim);
+        }
+    *n_milestones = m;
+    samples.clear();
+    samples.shrink_to_fit();
+    std::vector<long> limit((size_t)m);
+    for (long i = 0; i < m; ++i)
+        limit[(size_t)i] = i;
+    std::vector<long> nbr((size_t)m * k);
+    std::vector<double> nd((size_t)m * k);
+    PairMetric met(s, ms.data(), m, ms.data(), m);
+    knn_blocked(met, m, m, limit.data(), k, nbr.data(), nd.data());
+    std::vector<long> cs, cd;
+    for (long i = 0; i < m; ++i)
+        for (int j = 0; j < k; ++j)
+            if (nbr[(size_t)i * k + j] >= 0)
+            {
+                cs.push_back(nbr[(size_t)i * k + j]);
+                cd.push_back(i);
+            }
+    const long nc = (long)cs.size();
+    *candidates = nc;
+    std::vector<unsigned char> ok((size_t)nc);
+    parallel_rows(nc, [&](long e) {
+        double lt = kNaN;
+        int ndi = 0, fj = -1;
+        ok[(size_t)e] = check_motion_ordered(s, chk, ms.data() + (size_t)cs[(size_t)e] * s.dim,
+                                             ms.data() + (size_t)cd[(size_t)e] * s.dim, lt, ndi, fj)
+                            ? 1
+                            : 0;
+    });
+    long ne = 0;
+    for (long e = 0; e < nc; ++e)
+        if (ok[(size_t)e])
+        {
+            if (ne < edge_cap)
+            {
+                edge_src[ne] = cs[(size_t)e];
+                edge_dst[ne] = cd[(size_t)e];
+            }
+            ++ne;
+        }
+    return ne;
 }
 
 }  // extern "C"
