@@ -201,8 +201,7 @@ struct gbo_checker
     void *d64 = nullptr, *d32 = nullptr;
     int *cell_start = nullptr, *cell_items = nullptr;
     float *cell_items4 = nullptr;
-    unsigned short *units = nullptr;
-    float *wpair = nullptr;
+    unsigned *test_order = nullptr;
     CounterRing ctr;
     int tuned_schedule = -1;
     std::mutex mu, tune_mu;
@@ -221,10 +220,8 @@ struct gbo_checker
             cudaFree(cell_items);
         if (cell_items4)
             cudaFree(cell_items4);
-        if (units)
-            cudaFree(units);
-        if (wpair)
-            cudaFree(wpair);
+        if (test_order)
+            cudaFree(test_order);
         if (host_stream)
             cudaStreamDestroy(host_stream);
     }
@@ -403,7 +400,6 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
         g.self_den = up(safety * eden + 1e-12);
         g.self_lo = down(flt_eps - e);
         g.self_hi = up(flt_eps + e);
-        g.self_e = up(std::max((double)g.self_hi - flt_eps, flt_eps - (double)g.self_lo));
     }
     segs.resize(n);
     for (int j = 0; j < n; ++j)
@@ -424,7 +420,6 @@ void chain_bounds(const SpaceParams &sp, const double *w, int n, ChainGuard &g, 
         s.e_den = up(safety * eden + 1e-12);
         s.lo = down(flt_eps - e);
         s.hi = up(flt_eps + e);
-        s.e = up(std::max((double)s.hi - flt_eps, flt_eps - (double)s.lo));
         segs[j] = s;
     }
     // workspace distance (segment_count, FP32 form): dx_i accumulates 2i direction errors and i
@@ -473,161 +468,82 @@ float box_knn_eps(const SpaceParams &sp)
 }
 }  // namespace
 
-// World segments of a kinematic-chain checker in pairs for the warp kernels (chain_round.cuh): pair i
-// holds segments 2i and 2i + 1 as {x0, x0'}, {y0, y0'}, {-sx, -sx'}, {sy, sy'}, {e, e'}, {e_den, e_den'},
-// a missing second segment and the closing null pair are null segments (far away, zero vector, e tiny,
-// e_den -1: definitely clear of every link).
-static std::vector<float> chain_world_pairs(const std::vector<ChainSegF32> &segs)
-{
-    const int nw = (int)segs.size(), np = (nw + 1) / 2;
-    std::vector<float> out((size_t)(np + 1) * 12);
-    auto put = [&](int pair, int half, const ChainSegF32 *sgm) {
-        float *r = out.data() + (size_t)pair * 12;
-        r[0 + half] = sgm ? sgm->x0 : kNullCoord;
-        r[2 + half] = sgm ? sgm->y0 : kNullCoord;
-        r[4 + half] = sgm ? -sgm->sx : 0.f;
-        r[6 + half] = sgm ? sgm->sy : 0.f;
-        r[8 + half] = sgm ? sgm->e : kNullE;
-        r[10 + half] = sgm ? sgm->e_den : -1.f;
-    };
-    for (int p = 0; p <= np; ++p)
-        for (int h = 0; h < 2; ++h)
-        {
-            const int j = 2 * p + h;
-            put(p, h, p < np && j < nw ? &segs[j] : nullptr);
-        }
-    return out;
-}
-
-// Round order of a kinematic-chain checker (chain_round.cuh). The validity result does not depend on
-// the order of the segment tests; the warp kernels stop at the first round that holds a definite
-// intersection, so rounds likely to intersect go first: a greedy cover of the definite intersections
-// found (FP32, guarded) in 8192 states drawn uniformly from the joint bounds, repeatedly taking the
-// round that intersects in most states not yet covered. Worlds of more than 32 segments keep their
-// world rounds chunk by chunk (the kernels reload a lane's world pair when the chunk changes).
-static gbo_status order_chain_units(gbo_checker *c)
+// Segment-test order of a kinematic-chain checker. The validity result does not depend on the order in
+// which the segment tests run; the warp-cooperative kernels stop at the first round of 32 tests that
+// holds a definite intersection, so tests that are likely to intersect go first. The order is a greedy
+// cover of the definite intersections found (FP32, guarded) in 8192 states drawn uniformly from the
+// joint bounds: repeatedly take the test that intersects in most states not yet covered.
+static gbo_status order_chain_tests(gbo_checker *c)
 {
     const SpaceParams &sp = c->sp;
     const int n = sp.dim, m = n + 1, nw = c->wa.n;
-    const int n_self = (m - 1) * (m - 2) / 2;
-    const int n_tests = n_self + m * nw;
+    const int n_tests = (m - 1) * (m - 2) / 2 + m * nw;
     const int words = (n_tests + 31) / 32;
-    const int R = (m + 1) / 2, n_chunks = (nw + 31) / 32;
-    int self_pairs = 0;
-    for (int a = 0; a + 2 < m; ++a)
-        self_pairs += (m - a - 1) / 2;
-    const int n_self_units = (self_pairs + 31) / 32;
-    const int n_units = n_self_units + n_chunks * R;
-    if (n_units > 65535)
-        return fail(GBO_ERR_UNSUPPORTED, "segment world too large for the warp kernels");
-    // default test index of self pair (i, j) and of link a vs world segment w (chain_test_entry)
-    auto self_index = [&](int i, int j) {
-        int idx = 0;
-        for (int r = 0; r < i; ++r)
-            idx += m - r - 2;
-        return idx + (j - i - 2);
-    };
-    auto world_index = [&](int a, int w) { return n_self + w * m + a; };
-    std::vector<std::vector<int>> unit_tests(n_units);
+    const int S = 8192;
+    std::mt19937_64 rng(0x9e3779b97f4a7c15ull);
+    std::uniform_real_distribution<double> U(-kPiH, kPiH);
+    std::vector<double> st((size_t)n * S);
+    for (auto &x : st)
+        x = U(rng);
+    double *dst = nullptr;
+    unsigned *dbits = nullptr;
+    CUDA_TRY(cudaMalloc(&dst, st.size() * sizeof(double)));
+    if (cudaMalloc(&dbits, (size_t)S * words * sizeof(unsigned)) != cudaSuccess)
     {
-        int k = 0;
-        for (int a = 0; a + 2 < m; ++a)
-            for (int b = a + 2; b < m; b += 2, ++k)
-            {
-                auto &u = unit_tests[k / 32];
-                u.push_back(self_index(a, b));
-                if (b + 1 < m)
-                    u.push_back(self_index(a, b + 1));
-            }
-        for (int cidx = 0; cidx < n_chunks; ++cidx)
-            for (int lr = 0; lr < R; ++lr)
-            {
-                auto &u = unit_tests[n_self_units + cidx * R + lr];
-                for (int a : {lr, lr + R})
-                    if (a < m)
-                        for (int w = 32 * cidx; w < std::min(nw, 32 * cidx + 32); ++w)
-                            u.push_back(world_index(a, w));
-            }
-    }
-    std::vector<unsigned short> order;
-    if (nw > 0)
-    {
-        const int S = 8192;
-        std::mt19937_64 rng(0x9e3779b97f4a7c15ull);
-        std::uniform_real_distribution<double> U(-kPiH, kPiH);
-        std::vector<double> st((size_t)n * S);
-        for (auto &x : st)
-            x = U(rng);
-        double *dst = nullptr;
-        unsigned *dbits = nullptr;
-        CUDA_TRY(cudaMalloc(&dst, st.size() * sizeof(double)));
-        if (cudaMalloc(&dbits, (size_t)S * words * sizeof(unsigned)) != cudaSuccess)
-        {
-            cudaFree(dst);
-            return fail(GBO_ERR_OUT_OF_MEMORY, "test-order scratch allocation failed");
-        }
-        cudaMemcpy(dst, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice);
-        launch_chain_hits(nullptr, sp, c->wa, dst, S, dbits, words);
-        std::vector<unsigned> bits((size_t)S * words);
-        cudaError_t e = cudaMemcpy(bits.data(), dbits, bits.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
         cudaFree(dst);
-        cudaFree(dbits);
-        if (e != cudaSuccess)
-            return fail(GBO_ERR_CUDA, std::string("round ordering: ") + cudaGetErrorString(e));
-        const int sw = S / 64;
-        std::vector<uint64_t> ub((size_t)n_units * sw, 0);
-        for (int u = 0; u < n_units; ++u)
-            for (int t : unit_tests[u])
-                for (int s2 = 0; s2 < S; ++s2)
-                    if (bits[(size_t)s2 * words + t / 32] >> (t % 32) & 1u)
-                        ub[(size_t)u * sw + s2 / 64] |= 1ull << (s2 % 64);
-        std::vector<uint64_t> covered(sw, 0);
-        std::vector<char> used(n_units, 0);
-        // single-chunk worlds: greedy over all units; otherwise the self units greedily, then the chunks
-        // in order with their rounds greedily within each
-        auto greedy = [&](int lo, int hi) {
-            for (;;)
-            {
-                int best = -1;
-                long best_gain = -1;
-                for (int u = lo; u < hi; ++u)
-                {
-                    if (used[u])
-                        continue;
-                    long g = 0;
-                    for (int w = 0; w < sw; ++w)
-                        g += __builtin_popcountll(ub[(size_t)u * sw + w] & ~covered[w]);
-                    if (g > best_gain)
-                    {
-                        best_gain = g;
-                        best = u;
-                    }
-                }
-                if (best < 0)
-                    break;
-                used[best] = 1;
-                order.push_back((unsigned short)best);
-                for (int w = 0; w < sw; ++w)
-                    covered[w] |= ub[(size_t)best * sw + w];
-            }
-        };
-        if (n_chunks <= 1)
-            greedy(0, n_units);
-        else
-        {
-            greedy(0, n_self_units);
-            for (int cidx = 0; cidx < n_chunks; ++cidx)
-                greedy(n_self_units + cidx * R, n_self_units + (cidx + 1) * R);
-        }
+        return fail(GBO_ERR_OUT_OF_MEMORY, "test-order scratch allocation failed");
     }
-    else
-        for (int u = 0; u < n_units; ++u)
-            order.push_back((unsigned short)u);
-    CUDA_TRY(cudaMalloc(&c->units, order.size() * sizeof(unsigned short)));
-    CUDA_TRY(cudaMemcpy(c->units, order.data(), order.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
-    c->wa.units = c->units;
-    c->wa.n_units = (int)order.size();
-    c->wa.n_self_units = n_self_units;
+    cudaMemcpy(dst, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice);
+    WorldArgs wa = c->wa;
+    wa.test_order = nullptr;
+    launch_chain_hits(nullptr, sp, wa, dst, S, dbits, words);
+    std::vector<unsigned> bits((size_t)S * words);
+    cudaError_t e = cudaMemcpy(bits.data(), dbits, bits.size() * sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(dst);
+    cudaFree(dbits);
+    if (e != cudaSuccess)
+        return fail(GBO_ERR_CUDA, std::string("test ordering: ") + cudaGetErrorString(e));
+    // transpose to per-test state bitsets
+    const int sw = S / 64;
+    std::vector<uint64_t> tb((size_t)n_tests * sw, 0);
+    for (int s = 0; s < S; ++s)
+        for (int t = 0; t < n_tests; ++t)
+            if (bits[(size_t)s * words + t / 32] >> (t % 32) & 1u)
+                tb[(size_t)t * sw + s / 64] |= 1ull << (s % 64);
+    std::vector<uint64_t> covered(sw, 0);
+    std::vector<char> used(n_tests, 0);
+    std::vector<unsigned> order;
+    order.reserve(n_tests);
+    for (int step = 0; step < n_tests; ++step)
+    {
+        int best = -1;
+        long best_gain = -1;
+        for (int t = 0; t < n_tests; ++t)
+        {
+            if (used[t])
+                continue;
+            long g = 0;
+            for (int w = 0; w < sw; ++w)
+                g += __builtin_popcountll(tb[(size_t)t * sw + w] & ~covered[w]);
+            if (g > best_gain)
+            {
+                best_gain = g;
+                best = t;
+            }
+        }
+        if (best_gain <= 0)
+            break;
+        used[best] = 1;
+        order.push_back(chain_test_entry(best, n, nw));
+        for (int w = 0; w < sw; ++w)
+            covered[w] |= tb[(size_t)best * sw + w];
+    }
+    for (int t = 0; t < n_tests; ++t)
+        if (!used[t])
+            order.push_back(chain_test_entry(t, n, nw));
+    CUDA_TRY(cudaMalloc(&c->test_order, order.size() * sizeof(unsigned)));
+    CUDA_TRY(cudaMemcpy(c->test_order, order.data(), order.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+    c->wa.test_order = c->test_order;
     return GBO_OK;
 }
 
@@ -903,13 +819,14 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
     {
         std::vector<ChainSegF32> segs;
         chain_bounds(sp, world, (int)n_world, wa.guard, segs, wa.e_dist);
-        // one-ulp hazard bound of the FP64 form: joint k's position is a sum of k link vectors
-        // cos/sin * L; moving every sine and cosine by one ulp (<= 2^-52) moves each product by at most
-        // L 2^-52 plus its rounding, and each partial sum by its rounding (2^-53 of the reach), with a
-        // safety factor of 2
+        // trig hazard bound of the FP64 forms: joint k's position is a sum of k link vectors cos/sin * L;
+        // the device's sines and cosines (CUDA's FP64 sincos, within 2 ulps, or the correctly rounded
+        // ones) and the C library's (within 1 ulp) differ by at most 4 ulps (<= 4 * 2^-52), which moves
+        // each product by at most 4 L 2^-52 plus its rounding, and each partial sum by its rounding
+        // (2^-53 of the reach); safety factor 2
         {
             const double L = sp.link, reach = sp.dim * std::fabs(L) + 0.001;
-            wa.hz_pos = 2.0 * (sp.dim + 1) * (std::fabs(L) * 0x1p-52 + std::fabs(L) * 0x1p-53 + reach * 0x1p-53);
+            wa.hz_pos = 2.0 * (sp.dim + 1) * (std::fabs(L) * 0x1p-50 + std::fabs(L) * 0x1p-53 + reach * 0x1p-53);
         }
         size_t b32 = pad16(segs.size() * sizeof(ChainSegF32));
         if (b32)
@@ -923,17 +840,9 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         wa.stage32 = b32 > 0 && b32 <= 96 * 1024;
         if (!wa.stage32 && b32)
             return cleanup(fail(GBO_ERR_UNSUPPORTED, "segment world too large for shared memory"));
-        if (sp.dim <= 31)
-        {
-            const std::vector<float> pairs = chain_world_pairs(segs);
-            if (cudaMalloc(&c->wpair, pairs.size() * sizeof(float)) != cudaSuccess)
-                return cleanup(fail(GBO_ERR_OUT_OF_MEMORY, "world allocation failed"));
-            cudaMemcpy(c->wpair, pairs.data(), pairs.size() * sizeof(float), cudaMemcpyHostToDevice);
-            wa.wpair = c->wpair;
-            wa.n_pairs = (int)(segs.size() + 1) / 2;
-            if (auto st = order_chain_units(c))
+        if (b32 && sp.dim <= 31)
+            if (auto st = order_chain_tests(c))
                 return cleanup(st);
-        }
     }
     if (kind == GBO_CHECK_DH_SPHERES)
     {
@@ -992,10 +901,11 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
             dR += 2.0 * eps_t + 16.0 * u;
         }
         const double dc = (dp + 3.0 * u * reach) * std::sqrt(3.0);  // Euclidean centre error
-        // the same propagation for the FP64 form when every sine and cosine moves by one ulp (2^-52):
-        // the one-ulp hazard bound of a sphere centre (safety factor 2)
+        // the same propagation for the FP64 forms when every sine and cosine moves by 4 ulps (4 * 2^-52,
+        // CUDA's FP64 sincos against the C library's): the trig hazard bound of a sphere centre
+        // (safety factor 2)
         {
-            const double u64 = 0x1p-53, et = 0x1p-52;
+            const double u64 = 0x1p-53, et = 0x1p-50;
             double dR64 = 0.0, dp64 = 0.0, reach64 = 0.0;
             for (int i = 0; i < n_joints; ++i)
             {

@@ -133,54 +133,6 @@ __device__ __forceinline__ ff warp_scan_ff(ff v, int lane)
     return v;
 }
 
-// Inclusive float-float scan over lanes [0, 16) when n <= 16 (four steps), else over the whole warp.
-__device__ __forceinline__ ff warp_scan_ff16(ff v, int lane, int n = 16)
-{
-    const int lim = n <= 16 ? 8 : 16;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        if (o > lim)
-            break;
-        const float h = __shfl_up_sync(0xffffffffu, v.hi, o);
-        const float l = __shfl_up_sync(0xffffffffu, v.lo, o);
-        if (lane >= o)
-            v = ff_add(v, {h, l});
-    }
-    return v;
-}
-
-// Inclusive scan / sum over lanes [0, 16) when n <= 16, else over the whole warp.
-__device__ __forceinline__ float warp_scan_f16(float v, int lane, int n)
-{
-    const int lim = n <= 16 ? 8 : 16;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        if (o > lim)
-            break;
-        const float h = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o)
-            v += h;
-    }
-    return v;
-}
-
-__device__ __forceinline__ float warp_sum_f16(float v, int n)
-{
-    if (n <= 16)
-    {
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1)
-            v += __shfl_xor_sync(0xffffffffu, v, o);
-        return __shfl_sync(0xffffffffu, v, 0);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 __device__ __forceinline__ float warp_scan_f(float v, int lane)
 {
 #pragma unroll

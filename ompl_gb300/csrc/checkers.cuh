@@ -216,22 +216,15 @@ __device__ bool chain_valid64(const SpaceParams &s, const double *q, const doubl
 //   lo, hi         : FLT_EPSILON - e and FLT_EPSILON + e rounded outward, e a bound on |fp32 - fp64| of
 //                    s_numer, t_numer, s_numer - denom and t_numer - denom for a link vs this segment
 //   e_den          : bound on |fp32 - fp64| of denom
-//   e              : max(hi - FLT_EPSILON, FLT_EPSILON - lo) rounded up (the warp kernels' margin form)
 struct __align__(16) ChainSegF32
 {
-    float x0, y0, sx, sy, lo, hi, e_den, e;
+    float x0, y0, sx, sy, lo, hi, e_den, pad;
 };
-
-// Null segment of the warp kernels' packed tests (chain_round.cuh): far away with a zero vector, a tiny
-// margin and e_den -1, so that every test against it is definitely clear.
-constexpr float kNullCoord = 1.0e4f;
-constexpr float kNullE = 1.0e-30f;
 
 struct ChainGuard
 {
     float eps_dir;                      // bound on |cos/sin fp32 - fp64| of one link direction
     float self_lo, self_hi, self_den;   // lo, hi, e_den of link-vs-link tests
-    float self_e;                       // max(self_hi - FLT_EPSILON, FLT_EPSILON - self_lo), rounded up
 };
 
 // Guarded segment test: returns kInvalid (definite collision), kValid (definite none) or kAmbiguous.

@@ -77,7 +77,9 @@ constexpr double kFltEps = 1.1920928955078125e-07;
 // distance(a, b) in OMPL's operation order for each space kind.
 //   REAL_VECTOR: RealVectorStateSpace.cpp:230-242; SO2: SO2StateSpace.cpp:114-126;
 //   KINEMATIC_CHAIN: demos/KinematicChain.h:105-121; WRAP_L2: L2 of per-joint wrapped differences.
-template <int MAXD>
+// CR: sines and cosines correctly rounded (sincos_cr); otherwise CUDA's FP64 sincos (within 2 ulp, far
+// cheaper on GB300's FP64 pipe), used by the re-check paths of the FP32 forms.
+template <int MAXD, bool CR = true>
 __device__ double distance64(const SpaceParams &s, const double *a, const double *b)
 {
     const int n = s.dim;
@@ -96,8 +98,16 @@ __device__ double distance64(const SpaceParams &s, const double *a, const double
                 t1 = dadd(t1, a[i]);
                 t2 = dadd(t2, b[i]);
                 double s1, c1, s2, c2;
-                sincos_cr(t1, &s1, &c1);
-                sincos_cr(t2, &s2, &c2);
+                if (CR)
+                {
+                    sincos_cr(t1, &s1, &c1);
+                    sincos_cr(t2, &s2, &c2);
+                }
+                else
+                {
+                    sincos(t1, &s1, &c1);
+                    sincos(t2, &s2, &c2);
+                }
                 dx = dadd(dx, dsub(c1, c2));
                 dy = dadd(dy, dsub(s1, s2));
                 dist = dadd(dist, dsqrt(dadd(dmul(dx, dx), dmul(dy, dy))));

@@ -56,12 +56,7 @@ struct WorldArgs
     // centre (Euclidean) can move when every sine and cosine of the forward kinematics moves by one ulp
     double hz_pos;
     double hz_dh;
-    // kinematic chain, warp kernels (chain_round.cuh): world segment pairs (+ a null pair), 48 bytes
-    // each, and the round order
-    const void *wpair;
-    int n_pairs;
-    const unsigned short *units;
-    int n_units, n_self_units;
+    const unsigned *test_order;  // kinematic chain: segment-test order (likely intersections first)
 };
 
 struct LaunchCfg
@@ -200,11 +195,14 @@ static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const doub
     const int G = wa.grid_n;
     if (lane == 0)
         pos[0][0] = pos[0][1] = pos[0][2] = 0.0;
+    // the joints' sines and cosines, one joint per lane (the FK below is the same in every lane)
+    double cq_l = 1.0, sq_l = 0.0;
+    if (lane < arm.joints)
+        sincos(q[lane], &sq_l, &cq_l);
 #pragma unroll 1
     for (int i = 0; i < arm.joints; ++i)
     {
-        double cq, sq;
-        sincos_cr(q[i], &sq, &cq);
+        const double cq = __shfl_sync(0xffffffffu, cq_l, i), sq = __shfl_sync(0xffffffffu, sq_l, i);
         const double ca = (double)arm.ca[i], sa = (double)arm.sa[i];
         const double A[3][3] = {{cq, dmul(-sq, ca), dmul(sq, sa)}, {sq, dmul(cq, ca), dmul(-cq, sa)}, {0.0, sa, ca}};
         const double pA[3] = {dmul(arm.a[i], cq), dmul(arm.a[i], sq), arm.d[i]};

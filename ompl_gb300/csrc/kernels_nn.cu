@@ -87,7 +87,7 @@ __device__ void knn_exact_query(const NNArgs &nn, const SpaceParams &sp, const d
             continue;
         double x[MAXD];
         load_point<MAXD>(nn.pts64, nn.cap, sp.dim, key, x);
-        const double d = distance64<MAXD>(sp, x, q);
+        const double d = distance64<MAXD, false>(sp, x, q);
         if (d < dk[K - 1])
             topk_insert<K>(dk, ik, d, key);
     }
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(128) knn_finish_kernel(NNArgs nn, SpaceParams 
             break;
         double x[MAXD];
         load_point<MAXD>(nn.pts64, nn.cap, sp.dim, ik[j], x);
-        double cd = distance64<MAXD>(sp, x, q64);
+        double cd = distance64<MAXD, false>(sp, x, q64);
         // measured FP32 metric error (the lists hold distances for the chain, squares otherwise)
         const float d32 = KIND == GBO_SPACE_KINEMATIC_CHAIN ? dk[j] : sqrtf(dk[j]);
         max_err = fmaxf(max_err, fabsf((float)(cd - (double)d32)));
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(256) radius_kernel(NNArgs nn, SpaceParams sp, 
             {
                 double x[MAXD];
                 load_point<MAXD>(nn.pts64, nn.cap, sp.dim, key, x);
-                d = distance64<MAXD>(sp, x, q);
+                d = distance64<MAXD, false>(sp, x, q);
                 hit = d <= r;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
