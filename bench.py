@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve"],
+    p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve", "rrt"],
                    help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
     p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm"],
@@ -972,11 +972,78 @@ def serve_workload(port, n_clients=512, n_req=2000):
         "server": st}
 
 
+def rrt_workload(port, n_clients=64, iterations=100):
+    """RRTConnect-shaped planner clients (ompl_gb300/rrt.py) on the request loop: each client plans
+    between two valid states of its own world (1,024..8,192 spheres, the DH arm), each iteration one
+    nearestK(1) request and one short checkMotion (plus isValid for the goal tree) per growTree, the
+    clients' requests overlapping. Reports growTree rate, request latency percentiles per kind, and that
+    four clients give the same trees alone as in the mix."""
+    import torch
+
+    from ompl_gb300 import base as B
+    from ompl_gb300 import rrt
+    from ompl_gb300 import serve
+    from ompl_gb300 import workloads as W
+    from oracle.oracle import CheckerDesc, SpaceDesc
+    dh = W.dh_arm(np.random.default_rng(2))
+    lo, hi = np.full(7, -math.pi), np.full(7, math.pi)
+    lvs_fraction = 1.0 / 2500.0
+    rng_range = 0.2 * math.sqrt(7 * (2 * math.pi) ** 2)
+    port.set_threads(os.cpu_count() or 1)
+    setups = []
+    for c in range(n_clients):
+        crng = np.random.default_rng(5000 + c)
+        world = W.sphere_world(crng, int(crng.integers(1024, 8193)))
+        cand = crng.uniform(-math.pi, math.pi, size=(400, 7))
+        ok = port.is_valid(SpaceDesc(0, 7, lo, hi, lvs_fraction=lvs_fraction), CheckerDesc(3, world, dh, 8, 0.05),
+                           cand).astype(bool)
+        setups.append((world, cand[ok][0], cand[ok][1]))
+    srv = serve.Server(n_streams=32, arena_bytes=2 << 30)
+    checkers = []
+    for world, _, _ in setups:
+        space = B.RealVectorStateSpace(7, lo, hi)
+        space.setLongestValidSegmentFraction(lvs_fraction)
+        ck = B.DHSphereArmValidityChecker(space, dh, world, 8, 0.05)
+        ck.setPrecision("fp32_guarded")
+        checkers.append(ck)
+
+    def clients(idx):
+        return [rrt.RRTConnectClient(srv, checkers[i], setups[i][1], setups[i][2], 9000 + i, rng_range)
+                for i in idx]
+
+    warm = clients([0])
+    rrt.run_clients(warm, 5, concurrent=False)
+    mix = clients(range(n_clients))
+    t = time.perf_counter()
+    rrt.run_clients(mix, iterations, concurrent=True)
+    wall = time.perf_counter() - t
+    alone = clients(range(4))
+    rrt.run_clients(alone, iterations, concurrent=False)
+    same = sum(len(a.trace) == len(m.trace) and all(
+        x[0] == y[0] and x[1] == y[1] and x[3] == y[3] and ((x[2] is None and y[2] is None) or
+                                                          np.array_equal(x[2], y[2]))
+        for x, y in zip(a.trace, m.trace)) for a, m in zip(alone, mix[:4]))
+    grows = sum(len(c.trace) for c in mix)
+    st = srv.stats()
+    srv.close()
+    torch.cuda.synchronize()
+    return {"workload": f"RRTConnect clients: {n_clients} planners, each in its own world of 1,024..8,192 spheres "
+                        f"with the DH arm, range 0.2 of the extent, up to {iterations} iterations, served "
+                        "concurrently", "clients": n_clients, "wall_s": wall,
+            "solved": sum(c.solution is not None for c in mix), "grow_steps": grows,
+            "grow_steps_per_s": grows / wall, "requests": sum(len(c.log) for c in mix),
+            "requests_per_s": sum(len(c.log) for c in mix) / wall,
+            "latency_ms": {k: rrt.request_percentiles(mix, k) for k in ("knn", "motion", "validity")},
+            "alone_equals_mix": {"clients_checked": 4, "clients_same": int(same)},
+            "server": st}
+
+
 def other_workloads(port):
     import torch
     out = {}
     for name, fn in (("circles2d", circles_workload), ("dh_arm7_4096", arm_workload),
-                     ("prm_dh_arm7_2M", prm_workload), ("serve_512_clients", serve_workload)):
+                     ("prm_dh_arm7_2M", prm_workload), ("serve_512_clients", serve_workload),
+                     ("rrtconnect_64_clients", rrt_workload)):
         t = time.perf_counter()
         out[name] = fn(port)
         out[name]["bench_wall_s"] = time.perf_counter() - t
@@ -993,6 +1060,8 @@ def main():
             r = serve_workload(port, int(os.environ.get("SERVE_CLIENTS", 512)), int(os.environ.get("SERVE_REQUESTS", 2000)))
         elif args.workload == "arm":
             r = arm_workload(port)
+        elif args.workload == "rrt":
+            r = rrt_workload(port)
         else:
             r = prm_workload(port, os.environ.get("PRM_SAMPLES"), os.environ.get("PRM_STAR", "0") == "1")
         print(json.dumps(r))

@@ -61,7 +61,10 @@ enum {
     GBO_CHECK_ALL_VALID = 0,      /* AllValidStateValidityChecker */
     GBO_CHECK_CIRCLES = 1,        /* point robot vs circles; world rows (x, y, r) */
     GBO_CHECK_CHAIN_SEGMENTS = 2, /* KinematicChainValidityChecker; world rows (x0, y0, x1, y1) */
-    GBO_CHECK_DH_SPHERES = 3      /* DH serial arm covered by spheres vs world spheres (x, y, z, r) */
+    GBO_CHECK_DH_SPHERES = 3,     /* DH serial arm covered by spheres vs world spheres (x, y, z, r) */
+    GBO_CHECK_DH_BOXES = 4        /* the same arm vs axis-aligned boxes (cx, cy, cz, hx, hy, hz): centre and
+                                     half extents; no reference counterpart (the reference has no
+                                     collision checker of its own), definition in oracle/dh_arm.h */
 };
 
 /* Arithmetic of validity / motion / kNN evaluation. */
@@ -105,7 +108,8 @@ gbo_status gbo_get_motion_states(const gbo_space *s, const double *s1, const dou
                                  gbo_stream stream);
 
 /* ---- validity checkers ----
- * world: n_world rows of 3 (circles) or 4 (segments, spheres) doubles, host memory, copied to the device.
+ * world: n_world rows of 3 (circles), 4 (segments, spheres) or 6 (boxes) doubles, host memory, copied to
+ * the device.
  * dh: n_joints rows (a, d, alpha_code), alpha_code in {0, +1, -1} = alpha 0, +pi/2, -pi/2 (DH_SPHERES). */
 gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *world, int64_t n_world,
                               const double *dh, int n_joints, int spheres_per_link, double sphere_radius,

@@ -260,6 +260,17 @@ class DHSphereArmValidityChecker(StateValidityChecker):
                          sphere_radius=sphere_radius)
 
 
+class DHBoxArmValidityChecker(StateValidityChecker):
+    """The serial DH arm covered by spheres vs axis-aligned world boxes, rows (cx, cy, cz, hx, hy, hz):
+    a robot sphere hits a box when its centre is closer to the box than its radius (oracle/dh_arm.h
+    states the operation order)."""
+    kind = capi.CHECK_DH_BOXES
+
+    def __init__(self, space, dh, boxes, spheres_per_link=8, sphere_radius=0.05):
+        super().__init__(space, world=np.asarray(boxes).reshape(-1, 6), dh=dh, spheres_per_link=spheres_per_link,
+                         sphere_radius=sphere_radius)
+
+
 class DiscreteMotionValidator:
     """DiscreteMotionValidator (DiscreteMotionValidator.cpp:48-145) over a GPU checker."""
 

@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libgbompl.so")
 OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_NO_DEVICE, ERR_OUT_OF_MEMORY, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
 LAYOUT_SOA, LAYOUT_AOS = 0, 1
 SPACE_REAL_VECTOR, SPACE_SO2, SPACE_KINEMATIC_CHAIN, SPACE_WRAP_L2 = 0, 1, 2, 3
-CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES = 0, 1, 2, 3
+CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES, CHECK_DH_BOXES = 0, 1, 2, 3, 4
 PRECISION_FP64, PRECISION_FP32_GUARDED = 0, 1
 SCHEDULE_PLAIN, SCHEDULE_TILE, SCHEDULE_WARP, SCHEDULE_AUTO = 0, 1, 2, 3
 REQ_VALIDITY, REQ_MOTION, REQ_KNN = 0, 1, 2

@@ -765,8 +765,11 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
 {
     if (!space || !out)
         return fail(GBO_ERR_INVALID_ARGUMENT, "space/out is NULL");
-    if (kind < GBO_CHECK_ALL_VALID || kind > GBO_CHECK_DH_SPHERES)
+    if (kind < GBO_CHECK_ALL_VALID || kind > GBO_CHECK_DH_BOXES)
         return fail(GBO_ERR_INVALID_ARGUMENT, "unknown checker kind");
+    // boxes use the DH sphere-arm kernels with a box narrow phase (WorldArgs::boxes)
+    const bool boxes = kind == GBO_CHECK_DH_BOXES;
+    const int stride = boxes ? 6 : 4;
     if (n_world < 0 || (n_world > 0 && !world) || n_world > (1 << 24))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad world");
     const SpaceParams &sp = space->sp;
@@ -774,7 +777,7 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         return fail(GBO_ERR_INVALID_ARGUMENT, "the circle checker needs a 2-D space");
     if (kind == GBO_CHECK_CHAIN_SEGMENTS && sp.kind != GBO_SPACE_KINEMATIC_CHAIN)
         return fail(GBO_ERR_INVALID_ARGUMENT, "the chain checker needs a kinematic-chain space");
-    if (kind == GBO_CHECK_DH_SPHERES &&
+    if ((kind == GBO_CHECK_DH_SPHERES || boxes) &&
         (!dh || n_joints < 1 || n_joints > 8 || n_joints != sp.dim || spheres_per_link < 1 || sphere_radius < 0))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad DH arm (1..8 joints = space dimension)");
     if (auto st = ensure_device())
@@ -783,7 +786,8 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
     c->sp = sp;
     c->kind = kind;
     WorldArgs &wa = c->wa;
-    wa.kind = kind;
+    wa.kind = boxes ? GBO_CHECK_DH_SPHERES : kind;
+    wa.boxes = boxes ? 1 : 0;
     wa.n = (int)n_world;
     wa.inv_lvs32 = (float)(1.0 / sp.lvs);
     auto cleanup = [&](gbo_status s) {
@@ -803,7 +807,7 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         }
     }
     else if (kind != GBO_CHECK_ALL_VALID)
-        w64.assign(world, world + 4 * n_world);
+        w64.assign(world, world + stride * n_world);
     size_t b64 = pad16(w64.size() * sizeof(double));
     if (b64)
     {
@@ -814,7 +818,7 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
     }
     wa.data64 = c->d64;
     wa.bytes64 = (unsigned)b64;
-    wa.stage64 = (b64 > 0 && b64 <= 96 * 1024 && kind != GBO_CHECK_DH_SPHERES) ? 1 : 0;
+    wa.stage64 = (b64 > 0 && b64 <= 96 * 1024 && wa.kind != GBO_CHECK_DH_SPHERES) ? 1 : 0;
     if (kind == GBO_CHECK_CHAIN_SEGMENTS)
     {
         std::vector<ChainSegF32> segs;
@@ -844,7 +848,7 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
             if (auto st = order_chain_tests(c))
                 return cleanup(st);
     }
-    if (kind == GBO_CHECK_DH_SPHERES)
+    if (wa.kind == GBO_CHECK_DH_SPHERES)
     {
         DHArm &arm = wa.arm;
         arm.joints = n_joints;
@@ -862,13 +866,13 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
             arm.af[i] = (float)arm.a[i];
             arm.dfl[i] = (float)arm.d[i];
         }
-        // FP32 spheres
-        std::vector<float> s32(4 * n_world);
+        // FP32 obstacles (rows as given)
+        std::vector<float> s32(stride * n_world);
         double rmax = 0.0;
-        for (int64_t i = 0; i < 4 * n_world; ++i)
+        for (int64_t i = 0; i < stride * n_world; ++i)
             s32[i] = (float)world[i];
         for (int64_t i = 0; i < n_world; ++i)
-            rmax = std::max(rmax, world[4 * i + 3]);
+            rmax = std::max(rmax, boxes ? 0.0 : world[4 * i + 3]);
         size_t b32 = pad16(s32.size() * sizeof(float));
         if (b32)
         {
@@ -916,22 +920,25 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
             }
             wa.hz_dh = 2.0 * (dp64 + 3.0 * u64 * reach64) * std::sqrt(3.0);
         }
-        // near contact |d| <= 0.2 + rs + rmax: |d^2 - d_ref^2| <= 2|d| dc + dc^2 (+ rounding of d^2, rr^2)
-        const double D = 2.0 * (sphere_radius + rmax);
-        const double E = 2.0 * D * dc + dc * dc + 8.0 * u * D * D + 4.0 * u * (D * D);
-        wa.dh_e = (float)(2.0 * E);
-        // uniform 64^3 grid: a sphere is listed in every cell whose box lies within rs + ro + margin of its
-        // centre (exact sphere-box distance), so the cell holding a robot sphere centre lists every world
-        // sphere that can touch it; cells store the index (FP64 path) and the FP32 sphere itself.
-        const int G = 64;
+        // The grid below lists an obstacle in every cell within rs (+ r) + margin of it, so a listed
+        // obstacle lies within D = rs (+ rmax) + margin + one cell diagonal of the robot sphere centre:
+        // |d^2 - d_ref^2| <= 2|d| dc + dc^2 (+ rounding of d^2, rr^2). Boxes: the distance of a point
+        // from a box is 1-Lipschitz per axis; each axis adds the roundings of |c - centre| - half
+        // extent and of the FP32 box (<= 40u for coordinates below 4).
         const double margin = 1e-3;
+        const int G = 64;
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        // world obstacle i: centre o(i, r), half extent h(i, r) (boxes) or radius (spheres), and the
+        // reach added around it (rs + margin for boxes, rs + r + margin for spheres)
+        auto o_of = [&](int64_t i, int r) { return world[stride * i + r]; };
+        auto half = [&](int64_t i, int r) { return boxes ? world[stride * i + 3 + r] : 0.0; };
+        auto grow = [&](int64_t i) { return (boxes ? 0.0 : world[4 * i + 3]) + sphere_radius + margin; };
         for (int64_t i = 0; i < n_world; ++i)
             for (int r = 0; r < 3; ++r)
             {
-                const double ext = world[4 * i + 3] + sphere_radius + margin;
-                lo[r] = std::min(lo[r], world[4 * i + r] - ext);
-                hi[r] = std::max(hi[r], world[4 * i + r] + ext);
+                const double ext = grow(i) + half(i, r);
+                lo[r] = std::min(lo[r], o_of(i, r) - ext);
+                hi[r] = std::max(hi[r], o_of(i, r) + ext);
             }
         if (n_world == 0)
             for (int r = 0; r < 3; ++r)
@@ -939,11 +946,23 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
                 lo[r] = -1;
                 hi[r] = 1;
             }
-        double inv[3], cell[3];
+        double diag2 = 0.0;
         for (int r = 0; r < 3; ++r)
         {
             lo[r] -= margin;
             hi[r] += margin;
+            diag2 += ((hi[r] - lo[r]) / G) * ((hi[r] - lo[r]) / G);
+        }
+        const double D = 1.01 * (sphere_radius + rmax + margin + std::sqrt(diag2));
+        const double dcx = boxes ? dc + 40.0 * u * std::sqrt(3.0) : dc;
+        const double E = 2.0 * D * dcx + dcx * dcx + 8.0 * u * D * D + 4.0 * u * (D * D);
+        wa.dh_e = (float)(2.0 * E);
+        // uniform 64^3 grid: a sphere is listed in every cell whose box lies within rs + ro + margin of its
+        // centre (exact sphere-box distance), so the cell holding a robot sphere centre lists every world
+        // sphere that can touch it; cells store the index (FP64 path) and the FP32 sphere itself.
+        double inv[3], cell[3];
+        for (int r = 0; r < 3; ++r)
+        {
             inv[r] = G / (hi[r] - lo[r]);
             cell[r] = (hi[r] - lo[r]) / G;
             wa.glo64[r] = lo[r];
@@ -954,12 +973,12 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         const size_t ncell = (size_t)G * G * G;
         std::vector<int> start(ncell + 1, 0);
         auto visit = [&](int64_t i, auto &&emit) {
-            const double ext = world[4 * i + 3] + sphere_radius + margin;
+            const double ext = grow(i);
             int c0[3], c1[3];
             for (int r = 0; r < 3; ++r)
             {
-                c0[r] = std::max(0, (int)std::floor((world[4 * i + r] - ext - lo[r]) * inv[r]) - 1);
-                c1[r] = std::min(G - 1, (int)std::floor((world[4 * i + r] + ext - lo[r]) * inv[r]) + 1);
+                c0[r] = std::max(0, (int)std::floor((o_of(i, r) - half(i, r) - ext - lo[r]) * inv[r]) - 1);
+                c1[r] = std::min(G - 1, (int)std::floor((o_of(i, r) + half(i, r) + ext - lo[r]) * inv[r]) + 1);
             }
             for (int x = c0[0]; x <= c1[0]; ++x)
                 for (int y = c0[1]; y <= c1[1]; ++y)
@@ -970,8 +989,8 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
                         for (int r = 0; r < 3; ++r)
                         {
                             const double b0 = lo[r] + ix[r] * cell[r], b1 = b0 + cell[r];
-                            const double o = world[4 * i + r];
-                            const double g = o < b0 ? b0 - o : (o > b1 ? o - b1 : 0.0);
+                            const double o0 = o_of(i, r) - half(i, r), o1 = o_of(i, r) + half(i, r);
+                            const double g = o1 < b0 ? b0 - o1 : (o0 > b1 ? o0 - b1 : 0.0);
                             d2 += g * g;
                         }
                         if (d2 <= ext * ext * (1.0 + 1e-9))
@@ -983,13 +1002,14 @@ gbo_status gbo_checker_create(const gbo_space *space, int kind, const double *wo
         for (size_t k = 0; k < ncell; ++k)
             start[k + 1] += start[k];
         std::vector<int> fill(start.begin(), start.end() - 1), items(std::max(1, start[ncell]));
-        std::vector<float> items4(4 * items.size(), 0.f);
+        const int per_item = boxes ? 8 : 4;
+        std::vector<float> items4(per_item * items.size(), 0.f);
         for (int64_t i = 0; i < n_world; ++i)
             visit(i, [&](size_t k) {
                 const int pos = fill[k]++;
                 items[pos] = (int)i;
-                for (int r = 0; r < 4; ++r)
-                    items4[4 * (size_t)pos + r] = (float)world[4 * i + r];
+                for (int r = 0; r < stride; ++r)
+                    items4[per_item * (size_t)pos + r] = (float)world[stride * i + r];
             });
         if (cudaMalloc(&c->cell_start, start.size() * sizeof(int)) != cudaSuccess ||
             cudaMalloc(&c->cell_items, items.size() * sizeof(int)) != cudaSuccess ||

@@ -50,7 +50,9 @@ struct WorldArgs
     int grid_n;
     float glo[3], ginv[3];
     double glo64[3], ginv64[3];
-    float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere test near contact
+    float dh_e;           // bound on |d^2 - (rs+ro)^2| error of the FP32 sphere (box) test near contact
+    int boxes;            // DH arm world of axis-aligned boxes: rows (cx, cy, cz, hx, hy, hz), FP32 cell
+                          // items two float4 each, (cx, cy, cz, hx) and (hy, hz, 0, 0)
     float dh_qmax;  // largest |joint angle| the FP32 guard covers (larger: FP64)
     // one-ulp hazard bounds of the FP64 forms (checkers.cuh): how far a chain joint position / a DH sphere
     // centre (Euclidean) can move when every sine and cosine of the forward kinematics moves by one ulp
@@ -111,10 +113,41 @@ __device__ __forceinline__ void dh_hazard64(double dx, double dy, double dz, dou
     }
 }
 
+// FP64 narrow phase of one robot sphere (centre c, radius rs) and one listed world obstacle `o`, with
+// the hazard count: a world sphere (x, y, z, r) is hit iff (dx dx + dy dy) + dz dz < (rs + r)^2; an
+// axis-aligned box (cx, cy, cz, hx, hy, hz) iff (gx gx + gy gy) + gz gz < rs rs with
+// g = max(|c - centre| - half extent, 0) per axis (the squared distance of c from the box).
+__device__ __forceinline__ bool dh_pair64(const double *c, const double *o, double rs, bool boxes, double P,
+                                          unsigned long long *hz)
+{
+    double dx, dy, dz, rr;
+    if (boxes)
+    {
+        dx = dsub(fabs(dsub(c[0], o[0])), o[3]);
+        dy = dsub(fabs(dsub(c[1], o[1])), o[4]);
+        dz = dsub(fabs(dsub(c[2], o[2])), o[5]);
+        dx = dx > 0.0 ? dx : 0.0;
+        dy = dy > 0.0 ? dy : 0.0;
+        dz = dz > 0.0 ? dz : 0.0;
+        rr = rs;
+    }
+    else
+    {
+        dx = dsub(c[0], o[0]);
+        dy = dsub(c[1], o[1]);
+        dz = dsub(c[2], o[2]);
+        rr = dadd(rs, o[3]);
+    }
+    const double t = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), rr2 = dmul(rr, rr);
+    dh_hazard64(dx, dy, dz, t, rr2, P, hz);
+    return t < rr2;
+}
+
 template <int MAXD>
 __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, const WorldArgs &wa,
                            unsigned long long *hz = nullptr)
 {
+    const int stride = wa.boxes ? 6 : 4;
     double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     double p[3] = {0, 0, 0};
     const int G = wa.grid_n;
@@ -157,17 +190,8 @@ __device__ bool dh_valid64(const DHArm &arm, const double *q, const double *w, c
             const int cid = (cell[0] * G + cell[1]) * G + cell[2];
             const int b = wa.cell_start[cid], e = wa.cell_start[cid + 1];
             for (int it = b; it < e; ++it)
-            {
-                const double *o = w + 4 * wa.cell_items[it];
-                double dx = dsub(c[0], o[0]);
-                double dy = dsub(c[1], o[1]);
-                double dz = dsub(c[2], o[2]);
-                double rr = dadd(arm.rs, o[3]);
-                const double t = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), rr2 = dmul(rr, rr);
-                dh_hazard64(dx, dy, dz, t, rr2, wa.hz_dh, hz);
-                if (t < rr2)
+                if (dh_pair64(c, w + stride * wa.cell_items[it], arm.rs, wa.boxes, wa.hz_dh, hz))
                     return false;
-            }
         }
 #pragma unroll
         for (int r = 0; r < 3; ++r)
@@ -248,21 +272,16 @@ static __device__ __noinline__ bool dh_valid64_warp(const DHArm &arm, const doub
             continue;
         const int cid = (cell[0] * G + cell[1]) * G + cell[2];
         const int b = wa.cell_start[cid], e = wa.cell_start[cid + 1];
+        const int stride = wa.boxes ? 6 : 4;
         for (int it = b; it < e && !hit; ++it)
-        {
-            const double *o = w + 4 * wa.cell_items[it];
-            const double dx = dsub(c[0], o[0]), dy = dsub(c[1], o[1]), dz = dsub(c[2], o[2]);
-            const double rr = dadd(arm.rs, o[3]);
-            const double t = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), rr2 = dmul(rr, rr);
-            dh_hazard64(dx, dy, dz, t, rr2, wa.hz_dh, hz);
-            hit = t < rr2;
-        }
+            hit = dh_pair64(c, w + stride * wa.cell_items[it], arm.rs, wa.boxes, wa.hz_dh, hz);
     }
     return __any_sync(0xffffffffu, hit);
 }
 
-// FP32 form: FK, centres and the narrow phase in FP32; a pair whose d^2 - (rs+ro)^2 lies within
-// +-dh_e is ambiguous (dh_e bounds the FP32 error of that difference near contact). q: the joint
+// FP32 form: FK, centres and the narrow phase in FP32; a pair whose d^2 - (rs+ro)^2 (boxes: the squared
+// distance to the box - rs^2) lies within +-dh_e is ambiguous (dh_e bounds the FP32 error of that
+// difference near contact). q: the joint
 // angles as FP32 values within u|q| (+1e-12) of the reference's FP64 angles.
 template <int MAXD>
 __device__ int dh_valid32(const DHArm &arm, const float *q, const float4 *sph, const WorldArgs &wa)
@@ -311,16 +330,28 @@ __device__ int dh_valid32(const DHArm &arm, const float *q, const float4 *sph, c
                 continue;
             const int cid = (cell[0] * G + cell[1]) * G + cell[2];
             const int b = __ldg(wa.cell_start + cid), e = __ldg(wa.cell_start + cid + 1);
-            for (int it = b; it < e; ++it)
-            {
-                const float4 o = __ldg(wa.cell_items4 + it);
-                const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
-                const float rr = rs + o.w;
-                const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
-                if (t < -E)
-                    return kInvalid;
-                amb |= (t <= E);
-            }
+            if (wa.boxes)
+                for (int it = b; it < e; ++it)
+                {
+                    const float4 o = __ldg(wa.cell_items4 + 2 * it), h = __ldg(wa.cell_items4 + 2 * it + 1);
+                    const float dx = fmaxf(fabsf(c[0] - o.x) - o.w, 0.f), dy = fmaxf(fabsf(c[1] - o.y) - h.x, 0.f);
+                    const float dz = fmaxf(fabsf(c[2] - o.z) - h.y, 0.f);
+                    const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rs * rs;
+                    if (t < -E)
+                        return kInvalid;
+                    amb |= (t <= E);
+                }
+            else
+                for (int it = b; it < e; ++it)
+                {
+                    const float4 o = __ldg(wa.cell_items4 + it);
+                    const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
+                    const float rr = rs + o.w;
+                    const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
+                    if (t < -E)
+                        return kInvalid;
+                    amb |= (t <= E);
+                }
         }
 #pragma unroll
         for (int r = 0; r < 3; ++r)

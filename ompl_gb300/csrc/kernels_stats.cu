@@ -220,16 +220,40 @@ __global__ void __launch_bounds__(128) dh_precision_kernel(SpaceParams sp, World
                 const int cid = (cell[0] * G + cell[1]) * G + cell[2];
                 for (int it = wa.cell_start[cid]; it < wa.cell_start[cid + 1]; ++it)
                 {
-                    const float4 o = wa.cell_items4[it];
-                    const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
-                    const float rr = rs + o.w;
-                    const float t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
+                    float t;
+                    if (wa.boxes)
+                    {
+                        const float4 o = wa.cell_items4[2 * it], h = wa.cell_items4[2 * it + 1];
+                        const float dx = fmaxf(fabsf(c[0] - o.x) - o.w, 0.f), dy = fmaxf(fabsf(c[1] - o.y) - h.x, 0.f);
+                        const float dz = fmaxf(fabsf(c[2] - o.z) - h.y, 0.f);
+                        t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rs * rs;
+                    }
+                    else
+                    {
+                        const float4 o = wa.cell_items4[it];
+                        const float dx = c[0] - o.x, dy = c[1] - o.y, dz = c[2] - o.z;
+                        const float rr = rs + o.w;
+                        t = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) - rr * rr;
+                    }
                     face |= t < 0.f;
                     definite |= t < -E;
                     ambiguous |= (t >= -E && t <= E);
-                    const double *o6 = w64 + 4 * wa.cell_items[it];
-                    const double ex = dsub(c6[0], o6[0]), ey = dsub(c6[1], o6[1]), ez = dsub(c6[2], o6[2]);
-                    const double rr6 = dadd(arm.rs, o6[3]);
+                    const double *o6 = w64 + (wa.boxes ? 6 : 4) * wa.cell_items[it];
+                    double ex, ey, ez, rr6;
+                    if (wa.boxes)
+                    {
+                        ex = fmax(dsub(fabs(dsub(c6[0], o6[0])), o6[3]), 0.0);
+                        ey = fmax(dsub(fabs(dsub(c6[1], o6[1])), o6[4]), 0.0);
+                        ez = fmax(dsub(fabs(dsub(c6[2], o6[2])), o6[5]), 0.0);
+                        rr6 = arm.rs;
+                    }
+                    else
+                    {
+                        ex = dsub(c6[0], o6[0]);
+                        ey = dsub(c6[1], o6[1]);
+                        ez = dsub(c6[2], o6[2]);
+                        rr6 = dadd(arm.rs, o6[3]);
+                    }
                     const double t6 = dadd(dadd(dmul(ex, ex), dmul(ey, ey)), dmul(ez, ez)), r2 = dmul(rr6, rr6);
                     hit64 |= t6 < r2;
                     tally_err(mx, (float)((double)t - (t6 - r2)));

@@ -26,7 +26,7 @@ import numpy as np
 PI = np.pi
 
 SPACE_REAL_VECTOR, SPACE_SO2, SPACE_KINEMATIC_CHAIN, SPACE_WRAP_L2 = 0, 1, 2, 3
-CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES = 0, 1, 2, 3
+CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES, CHECK_DH_BOXES = 0, 1, 2, 3, 4
 
 
 @dataclass
@@ -81,6 +81,17 @@ def sphere_world(rng, n, rmin=0.02, rmax=0.1, free_radius=FREE_RADIUS):
         out = np.vstack([out, c[np.linalg.norm(c, axis=1) >= free_radius]])
     r = rng.uniform(rmin, rmax, size=(n, 1))
     return np.ascontiguousarray(np.hstack([out[:n], r]))
+
+
+def box_world(rng, n, hmin=0.02, hmax=0.1, free_radius=FREE_RADIUS):
+    """n axis-aligned boxes, rows (cx, cy, cz, hx, hy, hz): centres uniform in [-1,1]^3 outside a ball of
+    radius `free_radius` around the arm base (as sphere_world), half extents U(hmin, hmax) per axis."""
+    out = np.empty((0, 3))
+    while out.shape[0] < n:
+        c = rng.uniform(-1.0, 1.0, size=(2 * n, 3))
+        out = np.vstack([out, c[np.linalg.norm(c, axis=1) >= free_radius]])
+    h = rng.uniform(hmin, hmax, size=(n, 3))
+    return np.ascontiguousarray(np.hstack([out[:n], h]))
 
 
 def random_pairs(rng, states, n_edges):

@@ -22,7 +22,8 @@ namespace gbompl_oracle
  *   p' = ((R[r][0]*pA[0] + R[r][1]*pA[1]) + R[r][2]*pA[2]) + p[r].
  *   Link i spans p_i -> p_{i+1}; its spheres sit at p_i + f*(p_{i+1} - p_i), f = (k + 0.5)/spheres_per_link.
  *   A robot sphere (centre c, radius rs) hits world sphere (o, ro) iff
- *   (dx*dx + dy*dy) + dz*dz < (rs + ro)*(rs + ro) with d = c - o; the state is valid iff nothing hits. */
+ *   (dx*dx + dy*dy) + dz*dz < (rs + ro)*(rs + ro) with d = c - o (boxes: dh_pair_hits); the state is
+ *   valid iff nothing hits. */
 inline void dh_sphere_centres(const ora_checker *c, const double *q, double *centres /* n_joints*spl*3 */)
 {
     double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
@@ -60,23 +61,41 @@ inline void dh_sphere_centres(const ora_checker *c, const double *q, double *cen
     }
 }
 
+/* Narrow phase of one robot sphere (centre p, radius rs) against world obstacle o.
+ *   sphere (x, y, z, r): hit iff (dx*dx + dy*dy) + dz*dz < (rs + r)*(rs + r), d = p - o;
+ *   box (cx, cy, cz, hx, hy, hz), kind ORA_CHECK_DH_BOXES: per axis g = fabs(p - c) - h, g = 0 when
+ *   g <= 0 (g > 0 ? g : 0), hit iff (gx*gx + gy*gy) + gz*gz < rs*rs (the squared distance of p from
+ *   the box is below rs^2). */
+inline bool dh_pair_hits(const double *p, const double *o, double rs, bool boxes)
+{
+    if (boxes)
+    {
+        double gx = std::fabs(p[0] - o[0]) - o[3];
+        double gy = std::fabs(p[1] - o[1]) - o[4];
+        double gz = std::fabs(p[2] - o[2]) - o[5];
+        gx = gx > 0.0 ? gx : 0.0;
+        gy = gy > 0.0 ? gy : 0.0;
+        gz = gz > 0.0 ? gz : 0.0;
+        return (gx * gx + gy * gy) + gz * gz < rs * rs;
+    }
+    double dx = p[0] - o[0];
+    double dy = p[1] - o[1];
+    double dz = p[2] - o[2];
+    double rr = rs + o[3];
+    return (dx * dx + dy * dy) + dz * dz < rr * rr;
+}
+
 inline bool dh_valid(const ora_checker *c, const double *q)
 {
     const int ns = c->n_joints * c->spheres_per_link;
     std::vector<double> ctr(3 * (size_t)ns);
     dh_sphere_centres(c, q, ctr.data());
-    const double rs = c->sphere_radius;
+    const bool boxes = c->kind == ORA_CHECK_DH_BOXES;
+    const int stride = boxes ? 6 : 4;
     for (int s = 0; s < ns; ++s)
         for (long j = 0; j < c->n_obstacles; ++j)
-        {
-            const double *o = c->obstacles + 4 * j;
-            double dx = ctr[3 * s + 0] - o[0];
-            double dy = ctr[3 * s + 1] - o[1];
-            double dz = ctr[3 * s + 2] - o[2];
-            double rr = rs + o[3];
-            if ((dx * dx + dy * dy) + dz * dz < rr * rr)
+            if (dh_pair_hits(&ctr[3 * s], c->obstacles + stride * j, c->sphere_radius, boxes))
                 return false;
-        }
     return true;
 }
 

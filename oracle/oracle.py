@@ -22,7 +22,7 @@ REF_SO = os.path.join(HERE, "_ref", "libompl_ref.so")
 REF_TREE_DEFAULT = "/root/reference"
 
 SPACE_REAL_VECTOR, SPACE_SO2, SPACE_KINEMATIC_CHAIN, SPACE_WRAP_L2 = 0, 1, 2, 3
-CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES = 0, 1, 2, 3
+CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES, CHECK_DH_BOXES = 0, 1, 2, 3, 4
 NN_EXACT, NN_REF_LINEAR, NN_REF_GNAT, NN_REF_GNAT_NTS, NN_REF_SQRT_APPROX = 0, 1, 2, 3, 4
 
 
@@ -92,6 +92,8 @@ class CheckerDesc:
     def c(self):
         obs = np.ascontiguousarray(self.obstacles if self.obstacles is not None else np.zeros((0, 4)),
                                    dtype=np.float64)
+        if obs.ndim == 1:
+            obs = obs.reshape(1, -1)
         dh = np.ascontiguousarray(self.dh if self.dh is not None else np.zeros((0, 3)), dtype=np.float64)
         self._keep = [obs, dh]
         return _Checker(self.kind, _dp(obs), obs.shape[0], _dp(dh), dh.shape[0], self.spheres_per_link,

@@ -36,7 +36,8 @@ enum {
     ORA_CHECK_ALL_VALID = 0,        /* ompl::base::AllValidStateValidityChecker */
     ORA_CHECK_CIRCLES = 1,          /* point robot vs circles: obstacles are (x, y, r) rows */
     ORA_CHECK_CHAIN_SEGMENTS = 2,   /* KinematicChainValidityChecker: obstacles are (x0, y0, x1, y1) rows */
-    ORA_CHECK_DH_SPHERES = 3        /* serial DH arm covered by spheres vs world spheres (x, y, z, r) rows */
+    ORA_CHECK_DH_SPHERES = 3,       /* serial DH arm covered by spheres vs world spheres (x, y, z, r) rows */
+    ORA_CHECK_DH_BOXES = 4          /* the same arm vs axis-aligned boxes (cx, cy, cz, hx, hy, hz) rows */
 };
 
 /* Nearest-neighbour structures (the reference library honours all; the restatement only EXACT). */

@@ -327,16 +327,18 @@ bool chain_valid(const Space &s, const ora_checker *c, const double *q)
 
 // Uniform-grid broad phase for the DH sphere checker (a speed-up of this restatement only; the
 // boolean is that of gbompl_oracle::dh_valid, which tests every robot sphere against every world
-// sphere). World sphere o is listed in every cell that its box [o - R, o + R] reaches, with R =
-// r_o + r_robot + 1e-6; cells are found with the monotone map floor((v - x0) / h), so a robot
+// obstacle). World sphere o is listed in every cell that its box [o - R, o + R] reaches, with R =
+// r_o + r_robot + 1e-6 (a world box: its half extent + r_robot + 1e-6 per axis); cells are found with the monotone map floor((v - x0) / h), so a robot
 // sphere centre inside that box always lands in a listed cell, and a centre outside every box
-// (including outside the grid) is more than r_o + r_robot + 1e-6 from every world centre, where the
+// (including outside the grid) is more than r_o + r_robot + 1e-6 from every world centre (more than
+// r_robot + 1e-6 from every world box along some axis), where the
 // FP64 narrow phase cannot report a hit. The narrow phase of the listed candidates is
 // dh_valid's expression, evaluated on the same centres.
 struct DhGrid
 {
     double x0[3] = {0, 0, 0}, inv_h = 1.0;
-    int nc = 0;
+    int nc = 0, stride = 4;
+    bool boxes = false;
     std::vector<int> start, items;
 
     int cell_coord(double v, int a) const
@@ -350,15 +352,18 @@ struct DhGrid
         const long n = c->n_obstacles;
         if (n <= 0)
             return;
+        boxes = c->kind == ORA_CHECK_DH_BOXES;
+        stride = boxes ? 6 : 4;
+        // reach of obstacle j along axis a: its radius (or half extent) + the robot sphere radius + 1e-6
+        auto R_of = [&](const double *o, int a) { return (boxes ? o[3 + a] : o[3]) + c->sphere_radius + 1e-6; };
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
         for (long j = 0; j < n; ++j)
         {
-            const double *o = c->obstacles + 4 * j;
-            const double R = o[3] + c->sphere_radius + 1e-6;
+            const double *o = c->obstacles + stride * j;
             for (int a = 0; a < 3; ++a)
             {
-                lo[a] = std::min(lo[a], o[a] - R);
-                hi[a] = std::max(hi[a], o[a] + R);
+                lo[a] = std::min(lo[a], o[a] - R_of(o, a));
+                hi[a] = std::max(hi[a], o[a] + R_of(o, a));
             }
         }
         nc = (int)std::min(64.0, std::max(4.0, std::ceil(1.5 * std::cbrt((double)n))));
@@ -372,13 +377,12 @@ struct DhGrid
         const size_t cells = (size_t)nc * nc * nc;
         std::vector<int> count(cells + 1, 0);
         auto each = [&](long j, auto f) {
-            const double *o = c->obstacles + 4 * j;
-            const double R = o[3] + c->sphere_radius + 1e-6;
+            const double *o = c->obstacles + stride * j;
             int l[3], u[3];
             for (int a = 0; a < 3; ++a)
             {
-                l[a] = std::max(0, cell_coord(o[a] - R, a));
-                u[a] = std::min(nc - 1, cell_coord(o[a] + R, a));
+                l[a] = std::max(0, cell_coord(o[a] - R_of(o, a), a));
+                u[a] = std::min(nc - 1, cell_coord(o[a] + R_of(o, a), a));
             }
             for (int x = l[0]; x <= u[0]; ++x)
                 for (int y = l[1]; y <= u[1]; ++y)
@@ -417,15 +421,8 @@ struct DhGrid
                 continue;
             const size_t cell = ((size_t)ix * nc + iy) * nc + iz;
             for (int t = start[cell]; t < start[cell + 1]; ++t)
-            {
-                const double *o = c->obstacles + 4 * (size_t)items[(size_t)t];
-                double dx = p[0] - o[0];
-                double dy = p[1] - o[1];
-                double dz = p[2] - o[2];
-                double rr = rs + o[3];
-                if ((dx * dx + dy * dy) + dz * dz < rr * rr)
+                if (gbompl_oracle::dh_pair_hits(p, c->obstacles + stride * (size_t)items[(size_t)t], rs, boxes))
                     return false;
-            }
         }
         return true;
     }
@@ -443,7 +440,8 @@ Checker make_checker(const ora_checker *c, bool brute = false)
 {
     Checker k;
     k.c = c;
-    if (c->kind == ORA_CHECK_DH_SPHERES && !brute && c->n_obstacles > 64 && c->spheres_per_link <= 16 &&
+    if ((c->kind == ORA_CHECK_DH_SPHERES || c->kind == ORA_CHECK_DH_BOXES) && !brute && c->n_obstacles > 64 &&
+        c->spheres_per_link <= 16 &&
         c->n_joints <= 64)
     {
         k.grid.build(c);
@@ -462,6 +460,7 @@ bool is_valid(const Space &s, const Checker &k, const double *q)
         case ORA_CHECK_CHAIN_SEGMENTS:
             return chain_valid(s, c, q);
         case ORA_CHECK_DH_SPHERES:
+        case ORA_CHECK_DH_BOXES:
             return k.use_grid ? k.grid.valid(c, q) : gbompl_oracle::dh_valid(c, q);
         default:
             return true;

@@ -218,7 +218,7 @@ std::unique_ptr<Built> build(const ora_space *d, const ora_checker *c)
         inner = std::make_shared<CirclesChecker>(b->si.get(), c);
     else if (kind == ORA_CHECK_CHAIN_SEGMENTS)
         inner = std::make_shared<KinematicChainValidityChecker>(b->si);
-    else if (kind == ORA_CHECK_DH_SPHERES)
+    else if (kind == ORA_CHECK_DH_SPHERES || kind == ORA_CHECK_DH_BOXES)
         inner = std::make_shared<DHChecker>(b->si.get(), c);
     else
         inner = std::make_shared<ob::AllValidStateValidityChecker>(b->si.get());

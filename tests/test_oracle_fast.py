@@ -110,3 +110,23 @@ def test_c_library_trig_rounding_rate(port):
     r = port.trig_rounding(x)
     assert r["undecided"] == 0 and r["max_ulps"] <= 1
     assert (r["sin_misrounded"] + r["cos_misrounded"]) / (2 * len(x)) < 0.01
+
+
+@pytest.mark.parametrize("n_world", [1000, 8000])
+def test_dh_grid_equals_all_pairs_boxes(port, n_world):
+    w = W.config4(n_world=16)
+    boxes = W.box_world(np.random.default_rng(n_world), n_world)
+    sd = SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction)
+    cd = CheckerDesc(W.CHECK_DH_BOXES, boxes, w.dh, 8, 0.05)
+    st = np.random.default_rng(n_world + 1).uniform(-math.pi, math.pi, size=(1500, 7))
+    port.set_threads(8)
+    a = port.is_valid(sd, cd, st)
+    assert 0.05 < a.mean() < 0.95
+    assert np.array_equal(a, port.is_valid_brute(sd, cd, st))
+    s1 = st[a == 1][:40]
+    s2 = np.random.default_rng(3).uniform(-math.pi, math.pi, size=(len(s1), 7))
+    r = port.check_motion(sd, cd, s1, s2, want_state=True, want_bisect=False)
+    bad = r["ok"] == 0
+    near = np.concatenate([r["last_state"][bad], port.interpolate(sd, s1[bad], s2[bad],
+                                                                 r["first_j"][bad] / np.maximum(r["nd"][bad], 1))])
+    assert np.array_equal(port.is_valid(sd, cd, near), port.is_valid_brute(sd, cd, near))
