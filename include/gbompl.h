@@ -224,7 +224,8 @@ gbo_status gbo_nn_error_stats(const gbo_nn *nn, float *max_abs_error, float *bou
  * batches that do not fit are rejected with GBO_ERR_OUT_OF_MEMORY (about 44,000 queries for the
  * kinematic-chain metric, more for box spaces). The first call on a device looks the array up
  * (cudaGetSymbolAddress) and must come before any stream capture; every call shares the array, so
- * calls that overlap on the GPU race. */
+ * calls that overlap on the GPU race. Its re-check counters stay in that array: gbo_nn_stats and
+ * gbo_nn_error_stats do not include no-alloc calls (folding them in would need a host read). */
 gbo_status gbo_nn_nearest_k_noalloc(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, int k,
                                     const int64_t *prefix, int64_t *idx, double *dist, gbo_stream stream);
 
@@ -292,6 +293,12 @@ gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
 /* Correctly rounded FP64 sin and cos (the device routine of the FP64 forms) of n device values, for
  * tests. No reference counterpart (diagnostic). */
 gbo_status gbo_sincos_cr(const double *x, int64_t n, double *sin_out, double *cos_out, gbo_stream stream);
+/* Component tags of a PRM roadmap (replaces boost::disjoint_sets in PRM::addMilestone /
+ * PRM::uniteComponents, src/ompl/geometric/planners/prm/src/PRM.cpp:580-609, read by
+ * PRM::getPlannerData, PRM.cpp:729-756): union_set(src[e], dst[e]) for e = 0..n_edges-1 in order, union
+ * by rank with path compression, then root[v] = find_set(v). Host memory only. */
+gbo_status gbo_prm_component_roots(const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_vertices,
+                                   int64_t *root);
 /* Number of kernels this library launched since load (for launch accounting). */
 uint64_t gbo_launch_count(void);
 /* Self-test of the bounded device waits (no OMPL counterpart): a kernel waits limit_ns nanoseconds

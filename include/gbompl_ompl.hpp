@@ -281,9 +281,23 @@ public:
         ctx_->fromRow(row.data(), state);
         return ok != 0;
     }
-    bool sampleNear(ompl::base::State *, const ompl::base::State *, double) override
+    /* UniformValidStateSampler::sampleNear (UniformValidStateSampler.cpp:59-70): sampleUniformNear on
+     * the same stream, then isValid, until valid or getNrAttempts() draws were made. */
+    bool sampleNear(ompl::base::State *state, const ompl::base::State *near, double distance) override
     {
-        throw ompl::Exception("gbompl: sampleNear is not provided by the GPU valid-state sampler");
+        const unsigned d = ctx_->dim();
+        std::vector<double> c(d), row(d);
+        ctx_->toRow(near, c.data());
+        uint8_t ok = 0;
+        unsigned attempts = 0;
+        do
+        {
+            throwIf(gbo_sample_uniform_near_host(s_, c.data(), distance, 1, row.data()), "sampleNear");
+            throwIf(gbo_is_valid_host(ctx_->checker(), row.data(), 1, &ok), "isValid");
+            ++attempts;
+        } while (!ok && attempts < attempts_);
+        ctx_->fromRow(row.data(), state);
+        return ok != 0;
     }
     /* states.size() consecutive sample() calls; ok[i] is call i's result. */
     void sampleBatch(std::vector<ompl::base::State *> &states, std::vector<bool> &ok)
@@ -303,17 +317,65 @@ private:
     gbo_sampler *s_ = nullptr;
 };
 
+/* The check that a NearestNeighbors distance function (NearestNeighbors.h:58-110) is the state space's
+ * own metric, the only one the GPU index evaluates. From setDistanceFunction on, the function is
+ * compared with StateSpace::distance on up to 8 consecutive pairs of elements: at once on the stored
+ * elements, else on the first elements added afterwards (before they reach the device); a value that
+ * differs throws ompl::Exception. Needs no device. */
+template <typename T>
+class MetricGuard
+{
+public:
+    using DistanceFunction = typename ompl::NearestNeighbors<T>::DistanceFunction;
+    MetricGuard(const ompl::base::StateSpace *space, std::function<const ompl::base::State *(const T &)> stateOf)
+      : space_(space), stateOf_(std::move(stateOf))
+    {
+    }
+    /* setDistanceFunction(df) with the container's elements `stored`. */
+    void set(const DistanceFunction &df, const std::vector<T> &stored)
+    {
+        df_ = df;
+        pending_ = static_cast<bool>(df_);
+        check(stored, {});
+    }
+    /* add(data) with the container's elements `stored`; throws before anything is added. */
+    void check(const std::vector<T> &stored, const std::vector<T> &data)
+    {
+        if (!pending_)
+            return;
+        std::vector<T> run;
+        if (!stored.empty())
+            run.push_back(stored.back());
+        for (size_t i = 0; i < data.size() && run.size() < 9; ++i)
+            run.push_back(data[i]);
+        if (data.empty())
+            run.assign(stored.begin(), stored.begin() + std::min<size_t>(stored.size(), 9));
+        if (run.size() < 2)
+            return;
+        for (size_t i = 0; i + 1 < run.size(); ++i)
+            if (df_(run[i], run[i + 1]) != space_->distance(stateOf_(run[i]), stateOf_(run[i + 1])))
+                throw ompl::Exception("gbompl: GpuNearestNeighbors supports the state space's own metric only");
+        pending_ = false;
+    }
+
+private:
+    const ompl::base::StateSpace *space_;
+    std::function<const ompl::base::State *(const T &)> stateOf_;
+    DistanceFunction df_;
+    bool pending_ = false;
+};
+
 /* NearestNeighbors<T> over a device-resident index of the elements' states. `stateOf` maps an element
  * to its state (e.g. [](Motion *m) { return m->state; }). Results are ordered by (distance, insertion
- * order). The distance function must be the space's own metric: setDistanceFunction checks it on the
- * stored elements and throws otherwise. */
+ * order). The distance function must be the space's own metric (MetricGuard): a different one throws
+ * ompl::Exception from setDistanceFunction or from the first add after it. */
 template <typename T>
 class GpuNearestNeighbors : public ompl::NearestNeighbors<T>
 {
 public:
     GpuNearestNeighbors(GpuContextPtr ctx, std::function<const ompl::base::State *(const T &)> stateOf,
                         int64_t capacity = 1 << 20)
-      : ctx_(std::move(ctx)), stateOf_(std::move(stateOf))
+      : ctx_(std::move(ctx)), stateOf_(std::move(stateOf)), guard_(ctx_->omplSpace().get(), stateOf_)
     {
         throwIf(gbo_nn_create(ctx_->space(), capacity, &nn_), "nearest neighbours");
     }
@@ -321,14 +383,8 @@ public:
 
     void setDistanceFunction(const typename ompl::NearestNeighbors<T>::DistanceFunction &df) override
     {
+        guard_.set(df, elems_);
         ompl::NearestNeighbors<T>::setDistanceFunction(df);
-        for (size_t i = 0; i + 1 < elems_.size() && i < 8; ++i)
-        {
-            const double a = df(elems_[i], elems_[i + 1]);
-            const double b = ctx_->omplSpace()->distance(stateOf_(elems_[i]), stateOf_(elems_[i + 1]));
-            if (a != b)
-                throw ompl::Exception("gbompl: GpuNearestNeighbors supports the state space's own metric only");
-        }
     }
     bool reportsSortedResults() const override { return true; }
     void clear() override
@@ -340,6 +396,7 @@ public:
     void add(const T &data) override { add(std::vector<T>{data}); }
     void add(const std::vector<T> &data) override
     {
+        guard_.check(elems_, data);
         const unsigned d = ctx_->dim();
         std::vector<double> rows(data.size() * d);
         for (size_t i = 0; i < data.size(); ++i)
@@ -412,6 +469,7 @@ public:
 private:
     GpuContextPtr ctx_;
     std::function<const ompl::base::State *(const T &)> stateOf_;
+    MetricGuard<T> guard_;
     gbo_nn *nn_ = nullptr;
     std::vector<T> elems_;
     std::vector<unsigned char> alive_;

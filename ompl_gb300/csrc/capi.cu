@@ -2000,6 +2000,53 @@ gbo_status gbo_sample_gaussian_host(gbo_sampler *s, const double *mean, double s
     return GBO_OK;
 }
 
+// PRM::uniteComponents over a roadmap's edges in the order PRM adds them (PRM.cpp:580-609): boost's
+// disjoint_sets, every vertex first its own set; union_set(n, m) links the two roots by rank (the root of
+// higher rank becomes the parent of the other; on a tie the root of m's set becomes the parent and its
+// rank grows), finds compress paths. root[v] = find_set(v) after the last union: the component tag that
+// PRM::getPlannerData gives each vertex (PRM.cpp:734-754). Host memory, no device work.
+gbo_status gbo_prm_component_roots(const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_vertices,
+                                   int64_t *root)
+{
+    if (n_edges < 0 || n_vertices < 0 || (n_edges && (!src || !dst)) || (n_vertices && !root))
+        return GBO_ERR_INVALID_ARGUMENT;
+    std::vector<int64_t> parent((size_t)n_vertices);
+    std::vector<uint32_t> rank((size_t)n_vertices, 0);
+    for (int64_t v = 0; v < n_vertices; ++v)
+        parent[(size_t)v] = v;
+    auto find = [&](int64_t x) {
+        int64_t r = x;
+        while (parent[(size_t)r] != r)
+            r = parent[(size_t)r];
+        while (parent[(size_t)x] != r)
+        {
+            const int64_t next = parent[(size_t)x];
+            parent[(size_t)x] = r;
+            x = next;
+        }
+        return r;
+    };
+    for (int64_t e = 0; e < n_edges; ++e)
+    {
+        if (src[e] < 0 || src[e] >= n_vertices || dst[e] < 0 || dst[e] >= n_vertices)
+            return GBO_ERR_INVALID_ARGUMENT;
+        const int64_t i = find(src[e]), j = find(dst[e]);
+        if (i == j)
+            continue;
+        if (rank[(size_t)i] > rank[(size_t)j])
+            parent[(size_t)j] = i;
+        else
+        {
+            parent[(size_t)i] = j;
+            if (rank[(size_t)i] == rank[(size_t)j])
+                ++rank[(size_t)j];
+        }
+    }
+    for (int64_t v = 0; v < n_vertices; ++v)
+        root[v] = find(v);
+    return GBO_OK;
+}
+
 gbo_status gbo_measure_fp32_peak(double *flops, gbo_stream stream)
 {
     if (!flops)

@@ -19,7 +19,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libompl_ref.so")
-REF_TREE_DEFAULT = "/root/reference"
 
 SPACE_REAL_VECTOR, SPACE_SO2, SPACE_KINEMATIC_CHAIN, SPACE_WRAP_L2 = 0, 1, 2, 3
 CHECK_ALL_VALID, CHECK_CIRCLES, CHECK_CHAIN_SEGMENTS, CHECK_DH_SPHERES, CHECK_DH_BOXES = 0, 1, 2, 3, 4
@@ -37,9 +36,11 @@ def build_port(verbose: bool = False) -> str:
     return PORT_SO
 
 
-def build_reference(tree: str = REF_TREE_DEFAULT, jobs: int = 8) -> str | None:
-    """Compile OMPL's own sources into oracle/_ref/ when the source tree is present; else None."""
-    if not os.path.isdir(os.path.join(tree, "src", "ompl")):
+def build_reference(tree: str | None = None, jobs: int = 8) -> str | None:
+    """Compile OMPL's own sources from the OMPL source tree `tree` (else $OMPL_SOURCE_TREE) into
+    oracle/_ref/; None when neither names a source tree."""
+    tree = tree or os.environ.get("OMPL_SOURCE_TREE")
+    if not tree or not os.path.isdir(os.path.join(tree, "src", "ompl")):
         return None
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"-j{jobs}", f"REF={tree}"], check=True,
                    capture_output=True)

@@ -112,7 +112,8 @@ int main()
         mism += n1 != n2;
     }
     mism += gnn.size() != lnn.size();
-    // UniformValidStateSampler: same seed, same calls, same results (a few with 2 attempts)
+    // UniformValidStateSampler: same seed, same calls (sample and sampleNear), same results (a few with
+    // 2 attempts)
     space->setStateSamplerAllocator([](const ob::StateSpace *s) { return std::make_shared<SeededSampler>(s, 77); });
     ob::UniformValidStateSampler rvs(si.get());
     gbompl::GpuUniformValidStateSampler gvs(si.get(), ctx, 77);
@@ -121,7 +122,9 @@ int main()
         const unsigned att = i % 50 < 10 ? 2 : 100;
         rvs.setNrAttempts(att);
         gvs.setNrAttempts(att);
-        const bool r1 = rvs.sample(a), r2 = gvs.sample(b);
+        const bool near = i % 7 == 3;  // sampleNear around a stored point, on the same stream
+        const bool r1 = near ? rvs.sampleNear(a, pts[i], 0.1) : rvs.sample(a);
+        const bool r2 = near ? gvs.sampleNear(b, pts[i], 0.1) : gvs.sample(b);
         mism += r1 != r2 || !space->equalStates(a, b);
     }
     std::vector<ob::State *> batch(500);

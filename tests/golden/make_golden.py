@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ by running OMPL's OWN code.
 
-Requires the OMPL source tree (default /root/reference, or argv[1]): the script builds
+Requires the OMPL source tree (argv[1], or $OMPL_SOURCE_TREE): the script builds
 oracle/_ref/libompl_ref.so from those sources (oracle/ref/Makefile) and records inputs and the
 reference's outputs as small .npz files. The CPU restatement (oracle/liboracle.so) is then pinned
 against these files by tests/test_oracle_golden.py on every machine, including ones without the
@@ -231,4 +231,7 @@ def main(tree):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OMPL_SOURCE_TREE")
+    if not tree:
+        sys.exit("usage: make_golden.py <OMPL source tree> (or set OMPL_SOURCE_TREE)")
+    main(tree)

@@ -80,3 +80,30 @@ def test_prm_star_roadmap_matches_sequential_prm(port):
     ok = port.check_motion(sd, cd, M[src], M[dst], want_state=False, want_bisect=False)["ok"].astype(bool)
     assert set(zip(rm.edge_src.cpu().tolist(), rm.edge_dst.cpu().tolist())) == \
         set(zip(src[ok].tolist(), dst[ok].tolist()))
+
+
+def test_prm_planner_data_archive(port, tmp_path):
+    """PRM::getPlannerData of the GPU roadmap equals the oracle replay of PRM's edge sequence (vertex
+    order, tags, out-edge lists), and PlannerDataStorage's archive of it reads back unchanged."""
+    from ompl_gb300 import plannerdata as PD
+    from oracle.planner_data import prm_planner_data
+    n_samples, k = 2500, 10
+    w = W.config4(n_samples=n_samples, n_world=1024)
+    seed = w.extra["sampler_seed"]
+    space = B.WrapL2StateSpace(7)
+    space.setLongestValidSegmentFraction(w.lvs_fraction)
+    checker = B.DHSphereArmValidityChecker(space, w.dh, w.obstacles, 8, 0.05)
+    rm = prm.construct_roadmap(space, checker, seed, n_samples, k=k)
+    pd = PD.planner_data(rm, space)
+    ref = port.prm_roadmap(SpaceDesc(w.space_kind, 7, lvs_fraction=w.lvs_fraction),
+                           CheckerDesc(w.checker_kind, w.obstacles, dh=w.dh, spheres_per_link=8, sphere_radius=0.05),
+                           seed, n_samples, k)
+    vertices, tags, out = prm_planner_data(len(rm.sample_index), list(zip(ref["edge_src"].tolist(),
+                                                                        ref["edge_dst"].tolist())))
+    assert pd.milestone.tolist() == vertices and pd.tags.tolist() == tags
+    assert [pd.targets[pd.offsets[v]:pd.offsets[v + 1]].tolist() for v in range(pd.num_vertices)] == out
+    path = tmp_path / "prm.pdam"
+    PD.store(pd, path)
+    back = PD.load(path, signature=PD.space_signature(space))
+    assert np.array_equal(back.states.view(np.uint64), pd.states.view(np.uint64))
+    assert np.array_equal(back.targets, pd.targets) and np.array_equal(back.tags, pd.tags)
