@@ -43,6 +43,11 @@ N_EDGES = 100_000
 N_BATCHES = 12
 KNN_QUERIES = 20_000
 METRIC = "validated edges/s (DiscreteMotionValidator, 10-link kinematic chain)"
+# measured peaks of this GPU pool (copy bandwidth, bf16 GEMM), when the file is present
+PEAKS = {}
+if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as _f:
+        PEAKS = json.load(_f)
 # algorithmic work of one checked state of the chain predicate: 20 sincos + 50 FMA-chain flops +
 # (55 + 352) segment tests x 21 flops, credited per checked state (states the reference's ordered
 # DiscreteMotionValidator evaluates)
@@ -58,7 +63,7 @@ def parse():
     p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve", "rrt"],
                    help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
-    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm"],
+    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm", "sample"],
                    help="launch one kernel kind twice on the chain workload (for ncu) and exit")
     p.add_argument("--only-headline", action="store_true",
                    help="the chain workload alone (no circles / arm / serving / PRM objects)")
@@ -384,10 +389,15 @@ def ours(args, rank, world, local_rank):
     r0 = run(0, capi.SCHEDULE_AUTO)
     timed0 = {k: r0[k].cpu().numpy() for k in ("ok", "first_j", "nd")}
 
-    # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them
+    # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them. A
+    # sampler of another seed makes a call of the same size first (the jump polynomials of that call
+    # size are prepared once per process, on the host).
     smp = B.StateSampler(space, 5)
     smp.sampleUniform(1000, host=False)
     smp.sampleGaussian(torch.zeros((1000, w.dim), dtype=torch.float64, device=dev), 0.1)
+    warm_smp = B.StateSampler(space, 6)
+    for _ in range(3):
+        warm_smp.sampleUniform(N_STATES, host=False)
     torch.cuda.synchronize()
     s0, s1e, s2e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     s0.record()
@@ -396,9 +406,19 @@ def ours(args, rank, world, local_rank):
     smp.sampleGaussian(means, 0.1)
     s2e.record()
     torch.cuda.synchronize()
+    u_ms = s0.elapsed_time(s1e)
+    sampling_bytes = N_STATES * w.dim * 8
     sampling = {"states": N_STATES, "dim": w.dim,
-                "uniform_states_per_s": N_STATES / (s0.elapsed_time(s1e) * 1e-3),
-                "gaussian_states_per_s": N_STATES / (s1e.elapsed_time(s2e) * 1e-3)}
+                "uniform_states_per_s": N_STATES / (u_ms * 1e-3),
+                "gaussian_states_per_s": N_STATES / (s1e.elapsed_time(s2e) * 1e-3),
+                "uniform_ms": u_ms,
+                "roofline": {"bound": "hbm", "achieved": sampling_bytes / (u_ms * 1e-3) / 1e9,
+                             "peak": PEAKS.get("hbm_gbs"), "unit": "GB/s",
+                             "frac": sampling_bytes / (u_ms * 1e-3) / 1e9 / PEAKS["hbm_gbs"]
+                             if PEAKS.get("hbm_gbs") else None,
+                             "work": f"{sampling_bytes} bytes of coordinates written per call (8 per value)",
+                             "peak_source": "measured copy bandwidth (MEASURED_PEAKS.json)"}}
+    sampled_host = means.cpu().numpy()
     del means
 
     if rank != 0:
@@ -435,6 +455,13 @@ def ours(args, rank, world, local_rank):
     ref_idx, ref_dist = port.knn(sd, w.states, w.states[qi[pq]], 16)
     knn_agree = (ref_idx == knn_idx[pq]).all(axis=1) & \
         np.all(np.abs(ref_dist - knn_dist500) <= 1e-12 * np.maximum(np.abs(ref_dist), np.abs(knn_dist500)), axis=1)
+    # the timed uniform call, every value, against the oracle's sequential stream (same calls before it)
+    ref_s = port.sample_script(sd, 5, [("uniform", 1000), ("gaussian", 1000), ("uniform", N_STATES)],
+                               mean=np.zeros((1000, w.dim)), stddev=0.1)[-N_STATES:]
+    sampling["parity"] = {"values_checked": int(ref_s.size),
+                          "values_agree": int((ref_s.view(np.uint64) == sampled_host.view(np.uint64)).sum()),
+                          "compared": "every coordinate of the timed sampleUniform call, bitwise, against the "
+                                      "oracle's sequential mt19937 stream after the same earlier calls"}
     parity = {"edges_checked": sample, "edges_agree": int(agree.sum()), "knn_checked": len(pq),
               "knn_agree": int(knn_agree.sum()),
               "compared": "ok, first invalid index and segment count of 20,000 edges of timed batch 0; "
@@ -513,6 +540,14 @@ def profile(kind):
     w = workload()
     space = B.KinematicChainSpace(w.dim, w.link_length)
     space.setLongestValidSegmentFraction(w.lvs_fraction)
+    if kind == "sample":
+        # sampleUniform of 1M states of the 10-D chain space, three calls on one stream
+        smp = B.StateSampler(space, 5)
+        for _ in range(3):
+            smp.sampleUniform(N_STATES, soa=True, host=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": kind, "ok": True}))
+        return
     checker = B.KinematicChainValidityChecker(space, w.obstacles)
     checker.setPrecision("fp64" if kind == "motion_plain" else "fp32_guarded")
     if kind == "peaks":

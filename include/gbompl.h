@@ -299,6 +299,13 @@ gbo_status gbo_sincos_cr(const double *x, int64_t n, double *sin_out, double *co
  * by rank with path compression, then root[v] = find_set(v). Host memory only. */
 gbo_status gbo_prm_component_roots(const int64_t *src, const int64_t *dst, int64_t n_edges, int64_t n_vertices,
                                    int64_t *root);
+/* std::mt19937::discard(J) on a host copy of the generator (no OMPL counterpart; RandomNumbers.h:66-76
+ * keeps such a generator): `mt` holds the 624-word block and *pos the index of its next word (1..624,
+ * 624 = used up). Afterwards mt / *pos give the same outputs as the original after J draws. Jumps of
+ * 1,248 words and more use the jump-ahead polynomial x^J mod phi (phi: the characteristic polynomial of
+ * the generator's state transition) instead of stepping; the sampler's large calls use the same jumps
+ * on the device. Host memory only. */
+gbo_status gbo_mt19937_discard(uint32_t *mt, uint32_t *pos, uint64_t J);
 /* Number of kernels this library launched since load (for launch accounting). */
 uint64_t gbo_launch_count(void);
 /* Self-test of the bounded device waits (no OMPL counterpart): a kernel waits limit_ns nanoseconds

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbompl.so")
-SOURCES = ["capi.cu", "kernels_check.cu", "kernels_chain.cu", "kernels_nn.cu", "kernels_sample.cu", "kernels_stats.cu", "noalloc.cu", "server.cu"]
+SOURCES = ["capi.cu", "kernels_check.cu", "kernels_chain.cu", "kernels_nn.cu", "kernels_sample.cu", "kernels_stats.cu", "mt_jump.cu", "noalloc.cu", "server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-O3", "-Xptxas", "-O3"]

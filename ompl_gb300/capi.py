@@ -92,6 +92,7 @@ SIGNATURES = {
     "gbo_checker_precision_stats": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P]),
     "gbo_sincos_cr": (C.c_int, [_P, _I64, _P, _P, _P]),
     "gbo_prm_component_roots": (C.c_int, [_P, _P, _I64, _I64, _P]),
+    "gbo_mt19937_discard": (C.c_int, [_P, _P, C.c_uint64]),
 }
 
 

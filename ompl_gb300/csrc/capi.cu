@@ -1339,19 +1339,46 @@ static gbo_status sampler_words(gbo_sampler *s, int64_t n, gbo_stream stream, in
     return s->words.reserve((size_t)cap * sizeof(unsigned), (cudaStream_t)stream);
 }
 
+// sampleUniform / sampleUniformNear over n states. Calls of at least 2^18 stream words run on segments
+// of the stream generated side by side from jump-ahead windows (segments of L = 2^m words, m >= 15, the
+// smallest m that keeps them at most 160); smaller calls run the recurrence on one CTA.
+static gbo_status sample_uniform_call(gbo_sampler *s, const double *near, StatesView nearv, double distance,
+                                      int64_t n, MutStatesView out, gbo_stream stream)
+{
+    const int64_t values = n * s->sp.dim, W = 2 * values;
+    if (W >= ((int64_t)1 << 18) && values < ((int64_t)1 << 31) && mt_field_ready())
+    {
+        int m = 15;
+        while (m < 24 && W > ((int64_t)160 << m))
+            ++m;
+        const int64_t L = (int64_t)1 << m;
+        const int nseg = (int)((W + L - 1) / L);
+        const uint32_t *polys = nullptr;
+        if (nseg > 1)
+            if (auto st = mt_jump_table((uint64_t)L, nseg - 1, &polys))
+                return fail(st, "jump-ahead polynomials could not be prepared");
+        if (auto st = s->words.reserve((size_t)sample_jump_words(nseg, W) * sizeof(unsigned), (cudaStream_t)stream))
+            return st;
+        launch_sample_uniform_jump(lcfg(stream), s->st, s->sp, near, nearv, distance, n, out, (unsigned *)s->words.p,
+                                   polys, L, nseg);
+        CHECK_LAUNCH();
+        return GBO_OK;
+    }
+    int64_t cap = 0;
+    if (auto st = sampler_words(s, n, stream, cap))
+        return st;
+    launch_sample_uniform(lcfg(stream), s->st, s->sp, near, nearv, distance, n, out, (unsigned *)s->words.p, cap);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
 gbo_status gbo_sample_uniform(gbo_sampler *s, int64_t n, double *out, int64_t ld, int layout, gbo_stream stream)
 {
     Trace trace("gbo_sample_uniform");
     if (!s || n < 0 || (n > 0 && !out) || !valid_layout(layout, n, ld, s->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniform arguments");
     StatesView ov = make_view(out, ld, layout);
-    int64_t cap = 0;
-    if (auto st = sampler_words(s, n, stream, cap))
-        return st;
-    launch_sample_uniform(lcfg(stream), s->st, s->sp, nullptr, StatesView{}, 0.0, n, MutStatesView{out, ov.si, ov.sd},
-                          (unsigned *)s->words.p, cap);
-    CHECK_LAUNCH();
-    return GBO_OK;
+    return sample_uniform_call(s, nullptr, StatesView{}, 0.0, n, MutStatesView{out, ov.si, ov.sd}, stream);
 }
 
 gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double distance, int64_t n, int64_t ld,
@@ -1360,13 +1387,8 @@ gbo_status gbo_sample_uniform_near(gbo_sampler *s, const double *near, double di
     if (!s || n < 0 || (n > 0 && (!out || !near)) || !valid_layout(layout, n, ld, s->sp.dim))
         return fail(GBO_ERR_INVALID_ARGUMENT, "bad sampleUniformNear arguments");
     StatesView ov = make_view(out, ld, layout);
-    int64_t cap = 0;
-    if (auto st = sampler_words(s, n, stream, cap))
-        return st;
-    launch_sample_uniform(lcfg(stream), s->st, s->sp, near, make_view(near, ld, layout), distance, n,
-                          MutStatesView{out, ov.si, ov.sd}, (unsigned *)s->words.p, cap);
-    CHECK_LAUNCH();
-    return GBO_OK;
+    return sample_uniform_call(s, near, make_view(near, ld, layout), distance, n, MutStatesView{out, ov.si, ov.sd},
+                               stream);
 }
 
 // StateSampler::sampleGaussian (StateSampler.h:96-100) for n states, state i drawn around mean row i

@@ -97,6 +97,14 @@ struct GaussChunk
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
                            StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *words,
                            int64_t cap_words);
+// Segmented form of the call (jump-ahead; kernels_sample.cu): nseg segments of L words, windows 1..nseg-1
+// from the jump polynomials `polys` (x^(sL) mod phi, mt_jump.cu); scratch of sample_jump_words(nseg, W).
+void launch_sample_uniform_jump(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
+                                StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *scratch,
+                                const uint32_t *polys, int64_t L, int nseg);
+int64_t sample_jump_words(int64_t nseg, int64_t W);
+bool mt_field_ready();
+gbo_status mt_jump_table(uint64_t L, int K, const uint32_t **out);
 // sampleGaussian values [v_first, M) of a call; st->has_saved says whether value 0 is the cached one.
 // One chunk of at most cap_words / 4 - 156 polar candidates per host round trip; returns the chunks run
 // or -1 on an error. words: scratch of cap_words words; ctl: device GaussChunk; cnt: scratch of

@@ -176,6 +176,372 @@ void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpacePar
     }
 }
 
+// ---------------------------------------------------------------- segmented stream (jump-ahead)
+// Calls of many values cut their stretch of the stream, words [0, W) counted from the sampler's next
+// word T0, into segments of L words (L even, so no value's word pair is split): segment s starts from
+// the generator window at T0 - 1 + s L (position 1 of that window: its word 0 only carries its top
+// bit). Window 0 is the sampler's own state. Window s >= 1 is A^(sL) applied to the window at T0 - 1
+// (mt_jump.cu): with p = x^(sL) mod phi, its word w is the XOR over the set coefficients i of p of
+// u_(i+w), u_t = x_(T0-1+t). One CTA per segment then runs the recurrence over its words and converts
+// them to coordinates, so the call runs at the width of the GPU instead of one CTA's recurrence.
+
+// RN(w1 * 2^32 + w0) / 2^64 (generate_canonical's value) in integer arithmetic: the same double as
+// canonical53, including the largest double below 1 for sums that round up to 2^64.
+__device__ __forceinline__ double canonical53_int(unsigned w0, unsigned w1)
+{
+    const unsigned long long w = ((unsigned long long)w1 << 32) | w0;
+    if (w == 0)
+        return 0.0;
+    const int z = __clzll(w);
+    const unsigned long long m = w << z;  // leading one at bit 63
+    unsigned long long mant = m >> 11;    // 53 bits
+    const unsigned rem = (unsigned)(m & 0x7ffu);
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    unsigned long long e = 1022ull - (unsigned long long)z;  // value in [2^(-1-z), 2^-z)
+    if (mant >> 53)
+    {
+        mant >>= 1;
+        e += 1;
+    }
+    if (e >= 1023ull)
+        return 0.99999999999999988897769753748;  // rounded to 1: nextafter(1, 0)
+    return __longlong_as_double((long long)((e << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// Coordinate d of state i of a call from generate_canonical's U.
+__device__ __forceinline__ void emit_uniform_id(int64_t i, int d, double U, const SpaceParams &sp, const double *span,
+                                                StatesView nearv, int use_near, double distance, MutStatesView out)
+{
+    double x;
+    if (use_near)
+    {
+        const double c = nearv(i, d);
+        double lo, hi;
+        if (sp.kind == GBO_SPACE_SO2)
+        {
+            lo = __dsub_rn(c, distance);
+            hi = __dadd_rn(c, distance);
+        }
+        else
+        {
+            lo = fmax(sp.low[d], __dsub_rn(c, distance));
+            hi = fmin(sp.high[d], __dadd_rn(c, distance));
+        }
+        x = __dadd_rn(__dmul_rn(__dsub_rn(hi, lo), U), lo);
+        if (sp.kind == GBO_SPACE_SO2)
+        {
+            // SO2StateSpace::enforceBounds (SO2StateSpace.cpp:79-87)
+            double y = fmod(x, 2.0 * kPi);
+            if (y < -kPi)
+                y = __dadd_rn(y, 2.0 * kPi);
+            else if (y >= kPi)
+                y = __dsub_rn(y, 2.0 * kPi);
+            x = y;
+        }
+    }
+    else
+        x = __dadd_rn(__dmul_rn(span[d], U), sp.low[d]);
+    out(i, d) = x;
+}
+
+// The next 624 raw words (nxt) after block cur: the recurrence in its three dependency-free chunks,
+// word 623 with the last one. Every thread of the CTA (at least 227) calls it.
+__device__ __forceinline__ void twist_block(const unsigned *cur, unsigned *nxt)
+{
+    const int t = threadIdx.x;
+    if (t < 227)
+        nxt[t] = twist_word(cur[t], cur[t + 1], cur[t + 397]);
+    __syncthreads();
+    if (t < 227)
+        nxt[t + 227] = twist_word(cur[t + 227], cur[t + 228], nxt[t]);
+    __syncthreads();
+    if (t < 169)
+        nxt[t + 454] = twist_word(cur[t + 454], cur[t + 455], nxt[t + 227]);
+    else if (t == 169)
+        nxt[623] = twist_word(cur[623], nxt[0], nxt[396]);
+    __syncthreads();
+}
+
+constexpr int64_t kJumpU = 19968 + 704;  // u words the jumps read (coefficients < 19968, words < 640 + 64)
+
+// u_t = x_(T0-1+t) for t < n (one CTA), and states[0] = the sampler's block and position.
+__global__ void __launch_bounds__(256) mt_window_seq_kernel(const SamplerState *st, int64_t n, unsigned *u,
+                                                            unsigned *state0)
+{
+    __shared__ unsigned buf[2][624];
+    unsigned *cur = buf[0], *nxt = buf[1];
+    const int t = threadIdx.x;
+    for (int i = t; i < 624; i += blockDim.x)
+    {
+        cur[i] = st->mt[i];
+        state0[i] = cur[i];
+    }
+    const int pos = (int)st->pos;  // 1..624
+    if (t == 0)
+        state0[624] = (unsigned)pos;
+    __syncthreads();
+    int64_t w = 625 - pos;  // u_0 .. u_(624-pos) are cur[pos-1 .. 623]
+    for (int i = t; i < w && i < n; i += blockDim.x)
+        u[i] = cur[pos - 1 + i];
+    while (w < n)
+    {
+        twist_block(cur, nxt);
+        for (int i = t; i < 624 && w + i < n; i += blockDim.x)
+            u[w + i] = nxt[i];
+        unsigned *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        w += 624;
+        __syncthreads();
+    }
+}
+
+// Windows 1..K by table lookup ("four Russians"): coefficients are taken 5 at a time (group g covers
+// i = 5g .. 5g + 4), and for each window word w the 32 XOR combinations of u[5g + w .. 5g + w + 4] are
+// tabulated once per group and shared by every window: window k adds the entry its 5 coefficient bits
+// select. A CTA of NW warps covers 8 NW window words and one range of groups for up to 32 NW windows
+// (one thread per window, 8 NW accumulators each). Entry (w, h) sits at word 33 w + h: a reader's
+// address is its h plus a constant per w, and the 32 readers of one column hit 32 banks or the same
+// word; lane (c, q) of warp p builds entries 8q .. 8q + 7 of column 8p + c, and a warp's stores of one
+// step cover 32 banks. Partial results go to states[1..K] by atomicXor (zeroed before).
+constexpr int kJG = 5;                                 // coefficients per lookup
+constexpr int kJGroups = (19937 + kJG - 1) / kJG;      // 3988 groups (bits past 19936 are zero)
+
+// grid: (window-word chunks, ranges of qper groups, window chunks); dynamic shared memory holds the
+// range's u words (5 qper + 8 NW + 5)
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) mt_jump_kernel(const unsigned *u, const unsigned *polys, int K, int qper,
+                                                          unsigned *states)
+{
+    constexpr int TW = 8 * NW, KP = 32 * NW, GB = NW <= 5 ? 4 : 2;  // GB groups tabulated per phase
+    extern __shared__ unsigned us[];
+    __shared__ unsigned tab[2][GB][33 * TW];
+    const int w0 = blockIdx.x * TW;
+    const int g0 = blockIdx.y * qper, g1 = min(g0 + qper, kJGroups);
+    const int k0 = blockIdx.z * KP;
+    const int t = threadIdx.x, nk = min(KP, K - k0);
+    const int sl = kJG * qper + TW + kJG;
+    const int ubase = kJG * g0 + w0;
+    for (int j = t; j < sl; j += blockDim.x)
+        us[j] = ubase + j < kJumpU ? u[ubase + j] : 0u;  // words past kJumpU are never used
+    __syncthreads();
+    const int lane = t & 31, bw = 8 * (t >> 5) + (lane & 7), bq = lane >> 3;
+    // tables of groups ga .. ga + GB - 1 (those below g1) into set (ga / GB) & 1
+    auto build = [&](int ga) {
+#pragma unroll
+        for (int e = 0; e < GB; ++e)
+        {
+            const int g = ga + e;
+            if (g >= g1)
+                break;
+            unsigned *T = tab[((ga - g0) / GB) & 1][e] + 33 * bw + 8 * bq;
+            const unsigned *x = us + kJG * (g - g0) + bw;
+            const unsigned x0 = x[0], x1 = x[1], x2 = x[2];
+            const unsigned base = ((bq & 1) ? x[3] : 0u) ^ ((bq & 2) ? x[4] : 0u);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                T[j] = base ^ ((j & 1) ? x0 : 0u) ^ ((j & 2) ? x1 : 0u) ^ ((j & 4) ? x2 : 0u);
+        }
+    };
+    unsigned acc[TW];
+#pragma unroll
+    for (int w = 0; w < TW; ++w)
+        acc[w] = 0u;
+    // this window's coefficient words qa, qa + 1 (zero past word 623), advanced as the groups move on
+    const unsigned *crow = polys + (size_t)(k0 + min(t, nk - 1)) * 624;
+    int qa = (kJG * g0) >> 5;
+    unsigned c_lo = crow[qa], c_hi = qa + 1 < 624 ? crow[qa + 1] : 0u;
+    if (g0 < g1)
+        build(g0);
+    __syncthreads();
+#pragma unroll 1
+    for (int ga = g0; ga < g1; ga += GB)
+    {
+        if (ga + GB < g1)
+            build(ga + GB);
+        const unsigned(*set)[33 * TW] = tab[((ga - g0) / GB) & 1];
+#pragma unroll
+        for (int e = 0; e < GB; ++e)
+        {
+            const int g = ga + e;
+            if (g >= g1)
+                break;
+            const int b = kJG * g, q = b >> 5, sh = b & 31;
+            if (q != qa)
+            {
+                qa = q;
+                c_lo = c_hi;
+                c_hi = qa + 1 < 624 ? crow[qa + 1] : 0u;
+            }
+            if (t < nk)
+            {
+                unsigned v = c_lo >> sh;
+                if (sh > 32 - kJG)
+                    v |= c_hi << (32 - sh);
+                const unsigned *T = set[e] + (v & 31u);
+#pragma unroll
+                for (int w = 0; w < TW; ++w)
+                    acc[w] ^= T[33 * w];
+            }
+        }
+        __syncthreads();
+    }
+    if (t < nk)
+    {
+        unsigned *o = states + (size_t)(k0 + t + 1) * 625 + w0;
+#pragma unroll
+        for (int w = 0; w < TW; ++w)
+            if (w0 + w < 624)
+                atomicXor(o + w, acc[w]);
+    }
+}
+
+template <int NW>
+static void launch_jump_t(const LaunchCfg &lc, const unsigned *u, const uint32_t *polys, int K, unsigned *states)
+{
+    // two CTAs per SM: the ranges of groups split the rest of the grid over 2 x SM count
+    const int wchunks = (624 + 8 * NW - 1) / (8 * NW), kchunks = (K + 32 * NW - 1) / (32 * NW);
+    const int ranges = std::max(1, std::min(kJGroups, (2 * lc.sm_count + wchunks * kchunks / 2) / (wchunks * kchunks)));
+    const int qper = (kJGroups + ranges - 1) / ranges;
+    const size_t smem = (size_t)(kJG * qper + 8 * NW + kJG) * sizeof(unsigned);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(mt_jump_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    mt_jump_kernel<NW><<<dim3(wchunks, (kJGroups + qper - 1) / qper, kchunks), 32 * NW, smem, lc.stream>>>(
+        u, polys, K, qper, states);
+}
+
+static void launch_jump(const LaunchCfg &lc, const unsigned *u, const uint32_t *polys, int K, unsigned *states)
+{
+    switch (std::min(8, (K + 31) / 32))
+    {
+    case 1: launch_jump_t<1>(lc, u, polys, K, states); break;
+    case 2: launch_jump_t<2>(lc, u, polys, K, states); break;
+    case 3: launch_jump_t<3>(lc, u, polys, K, states); break;
+    case 4: launch_jump_t<4>(lc, u, polys, K, states); break;
+    case 5: launch_jump_t<5>(lc, u, polys, K, states); break;
+    case 6: launch_jump_t<6>(lc, u, polys, K, states); break;
+    case 7: launch_jump_t<7>(lc, u, polys, K, states); break;
+    default: launch_jump_t<8>(lc, u, polys, K, states); break;
+    }
+}
+
+// One CTA per segment s: words [s L, min((s + 1) L, W)) of the call from window s, tempered and stored
+// as the recurrence produces them (word j of the call at words[j]); the last segment leaves its
+// generator in st.
+__global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const unsigned *states, int64_t L,
+                                                         int64_t W, int nseg, unsigned *words)
+{
+    __shared__ unsigned buf[2][624];
+    unsigned *cur = buf[0], *nxt = buf[1];
+    const int t = threadIdx.x, s = blockIdx.x;
+    const unsigned *src = states + (size_t)s * 625;
+    for (int i = t; i < 624; i += blockDim.x)
+        cur[i] = src[i];
+    int pos = s == 0 ? (int)src[624] : 1;
+    const int64_t begin = (int64_t)s * L, len = min(begin + L, W) - begin;
+    unsigned *o = words + begin;
+    __syncthreads();
+    int64_t w = min((int64_t)(624 - pos), len);  // the rest of the first block
+    for (int i = t; i < (int)w; i += blockDim.x)
+        o[i] = temper(cur[pos + i]);
+    pos += (int)w;
+#pragma unroll 1
+    while (w < len)
+    {
+        const int m = (int)min((int64_t)624, len - w);  // words of the new block that belong to the segment
+        unsigned *ob = o + w;
+        if (t < 227)
+        {
+            const unsigned v = twist_word(cur[t], cur[t + 1], cur[t + 397]);
+            nxt[t] = v;
+            if (t < m)
+                ob[t] = temper(v);
+        }
+        __syncthreads();
+        if (t < 227)
+        {
+            const unsigned v = twist_word(cur[t + 227], cur[t + 228], nxt[t]);
+            nxt[t + 227] = v;
+            if (t + 227 < m)
+                ob[t + 227] = temper(v);
+        }
+        __syncthreads();
+        if (t < 170)
+        {
+            const unsigned v = t < 169 ? twist_word(cur[t + 454], cur[t + 455], nxt[t + 227])
+                                       : twist_word(cur[623], nxt[0], nxt[396]);
+            nxt[t + 454] = v;
+            if (t + 454 < m)
+                ob[t + 454] = temper(v);
+        }
+        __syncthreads();
+        unsigned *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        w += m;
+        pos = m;
+    }
+    if (s == nseg - 1)
+    {
+        for (int i = t; i < 624; i += blockDim.x)
+            st->mt[i] = cur[i];
+        if (t == 0)
+            st->pos = (unsigned)pos;
+    }
+}
+
+// Values v0 .. v0 + nv - 1 of the call from the stored word pairs (2m, 2m + 1), m = v - v0:
+// generate_canonical in integer arithmetic, then uniformReal (or the near bounds). state = v / dim by a
+// multiply-high with magic = ceil(2^40 / dim) (exact for v < 2^31 and dim <= 256).
+__global__ void __launch_bounds__(256) pairs_to_states_kernel(const uint2 *pairs, int64_t nv, SpaceParams sp,
+                                                              unsigned long long magic, StatesView nearv,
+                                                              int use_near, double distance, MutStatesView out)
+{
+    __shared__ double span[GBO_MAXD];
+    for (int d = threadIdx.x; d < sp.dim; d += blockDim.x)
+        span[d] = __dsub_rn(sp.high[d], sp.low[d]);
+    __syncthreads();
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < nv; m += (int64_t)gridDim.x * blockDim.x)
+    {
+        const uint2 w = pairs[m];
+        const unsigned long long v = (unsigned long long)m;
+        const int64_t i = (int64_t)__umul64hi(v << 24, magic);
+        emit_uniform_id(i, (int)(v - (unsigned long long)i * sp.dim), canonical53_int(w.x, w.y), sp, span, nearv,
+                        use_near, distance, out);
+    }
+}
+
+int64_t sample_jump_words(int64_t nseg, int64_t W)
+{
+    return kJumpU + nseg * 625 + 4 + W;
+}
+
+void launch_sample_uniform_jump(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
+                                StatesView nearv, double distance, int64_t n, MutStatesView out, unsigned *scratch,
+                                const uint32_t *polys, int64_t L, int nseg)
+{
+    const int64_t values = n * sp.dim, W = 2 * values;
+    unsigned *u = scratch, *states = scratch + kJumpU, *words = states + (size_t)nseg * 625;
+    words += (4 - ((uintptr_t)words / 4) % 4) % 4;  // 16-byte aligned
+    const int K = nseg - 1;
+    if (K > 0)
+        cudaMemsetAsync(states + 625, 0, (size_t)K * 625 * sizeof(unsigned), lc.stream);
+    mt_window_seq_kernel<<<1, 256, 0, lc.stream>>>(st, kJumpU, u, states);
+    note_launch();
+    if (K > 0)
+    {
+        launch_jump(lc, u, (const unsigned *)polys, K, states);
+        note_launch();
+    }
+    mt_segment_kernel<<<nseg, 256, 0, lc.stream>>>(st, states, L, W, nseg, words);
+    const unsigned long long magic = ((1ull << 40) + (unsigned long long)sp.dim - 1) / (unsigned long long)sp.dim;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((values + 255) / 256, (int64_t)lc.sm_count * 16));
+    pairs_to_states_kernel<<<grid, 256, 0, lc.stream>>>((const uint2 *)words, values, sp, magic, nearv, near != nullptr,
+                                                        distance, out);
+    note_launch();
+    note_launch();
+}
+
 // ---------------------------------------------------------------- sampleGaussian
 // RealVectorStateSampler::sampleGaussian (RealVectorStateSpace.cpp:67-82: per coordinate
 // rng_.gaussian(mean, stdDev) clamped to the bounds) and SO2StateSampler::sampleGaussian
