@@ -399,7 +399,8 @@ __global__ void __launch_bounds__(32 * NW) mt_jump_kernel(const unsigned *u, con
 template <int NW>
 static void launch_jump_t(const LaunchCfg &lc, const unsigned *u, const uint32_t *polys, int K, unsigned *states)
 {
-    // two CTAs per SM: the ranges of groups split the rest of the grid over 2 x SM count
+    // two CTAs per SM: the ranges of groups split the rest of the grid over 2 x SM count (four per SM
+    // measured the same: the lookups are bound by shared-memory wavefronts, not by latency)
     const int wchunks = (624 + 8 * NW - 1) / (8 * NW), kchunks = (K + 32 * NW - 1) / (32 * NW);
     const int ranges = std::max(1, std::min(kJGroups, (2 * lc.sm_count + wchunks * kchunks / 2) / (wchunks * kchunks)));
     const int qper = (kJGroups + ranges - 1) / ranges;
