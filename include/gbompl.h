@@ -212,6 +212,18 @@ gbo_status gbo_nn_nearest_r_count(gbo_nn *nn, const double *q, int64_t nq, int64
 gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout, double r,
                                  const int64_t *offsets, int64_t *idx, double *dist, gbo_stream stream);
 gbo_status gbo_nn_stats(const gbo_nn *nn, uint64_t *queries, uint64_t *rechecked, uint64_t *fallbacks);
+/* NearestNeighborsSqrtApprox::nearest (src/ompl/datastructures/NearestNeighborsSqrtApprox.h:91-115) for nq
+ * queries made one after another: query i examines 1 + floor(sqrt(n)) of the n present elements, those
+ * at positions (j * checks + offset_i) % n in insertion order, and returns the first strict minimum of the
+ * FP64 distance (idx[i] = its key, dist[i] = the distance). *offset holds the structure's offset before
+ * the first query and receives it after the last (0 for a new or cleared structure). An empty index
+ * gives GBO_ERR_INVALID_ARGUMENT (OMPL throws). Queries on ld / layout; outputs are device arrays. */
+gbo_status gbo_nn_nearest_sqrt_approx(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout,
+                                      uint64_t *offset, int64_t *idx, double *dist, gbo_stream stream);
+/* The same on host arrays (AoS rows; synchronous). */
+gbo_status gbo_nn_nearest_sqrt_approx_host(gbo_nn *nn, const double *q, int64_t nq, uint64_t *offset, int64_t *idx,
+                                           double *dist);
+
 /* FP32 metric error of the last FP32_GUARDED nearestK call (no OMPL counterpart): the largest
  * |distance_fp32 - distance_fp64| over the candidates it re-checked in FP64, and the bound the guard band
  * assumes for it (the re-check band is twice that bound). */

@@ -466,13 +466,42 @@ public:
                 data.push_back(elems_[i]);
     }
 
-private:
+protected:
     GpuContextPtr ctx_;
     std::function<const ompl::base::State *(const T &)> stateOf_;
     MetricGuard<T> guard_;
     gbo_nn *nn_ = nullptr;
     std::vector<T> elems_;
     std::vector<unsigned char> alive_;
+};
+
+/* NearestNeighborsSqrtApprox<T> (datastructures/NearestNeighborsSqrtApprox.h) over the same device index:
+ * nearest() examines 1 + floor(sqrt(n)) elements chosen round-robin exactly as OMPL's class does (the
+ * offset advances per call and restarts at clear()); the other queries are GpuNearestNeighbors'. */
+template <typename T>
+class GpuNearestNeighborsSqrtApprox : public GpuNearestNeighbors<T>
+{
+public:
+    using GpuNearestNeighbors<T>::GpuNearestNeighbors;
+    void clear() override
+    {
+        GpuNearestNeighbors<T>::clear();
+        offset_ = 0;
+    }
+    T nearest(const T &data) const override
+    {
+        std::vector<double> q(this->ctx_->dim());
+        this->ctx_->toRow(this->stateOf_(data), q.data());
+        int64_t key = -1;
+        double d = 0.0;
+        const gbo_status st = gbo_nn_nearest_sqrt_approx_host(this->nn_, q.data(), 1, &offset_, &key, &d);
+        if (st != GBO_OK || key < 0)
+            throw ompl::Exception("No elements found in nearest neighbors data structure");
+        return this->elems_[key];
+    }
+
+private:
+    mutable uint64_t offset_ = 0;
 };
 
 }  // namespace gbompl

@@ -438,6 +438,7 @@ class NearestNeighborsGPU:
 
     def clear(self):
         check(lib().gbo_nn_clear(self._h))
+        self._sqrt_offset = 0
 
     def size(self):
         s = C.c_int64()
@@ -462,6 +463,21 @@ class NearestNeighborsGPU:
         if isinstance(queries, torch.Tensor):
             return idx, dist
         return _host(idx), (_host(dist) if want_dist else None)
+
+    def nearestSqrtApprox(self, queries, soa=False, stream=None):
+        """NearestNeighborsSqrtApprox::nearest (NearestNeighborsSqrtApprox.h:91-115) for each query in
+        order, over the present elements: (keys, distances). The structure's offset carries across calls
+        and restarts at clear()."""
+        t, n, ld, lay = _batch(queries, self.space.dim, soa)
+        idx = torch.empty(n, dtype=torch.int64, device="cuda")
+        dist = torch.empty(n, dtype=torch.float64, device="cuda")
+        off = C.c_uint64(getattr(self, "_sqrt_offset", 0))
+        check(lib().gbo_nn_nearest_sqrt_approx(self._h, _ptr(t), n, ld, lay, C.byref(off), _ptr(idx), _ptr(dist),
+                                               _stream(stream)))
+        self._sqrt_offset = off.value
+        if isinstance(queries, torch.Tensor):
+            return idx, dist
+        return _host(idx), _host(dist)
 
     def nearestR(self, queries, radius, soa=False, stream=None):
         t, n, ld, lay = _batch(queries, self.space.dim, soa)

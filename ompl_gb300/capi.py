@@ -93,6 +93,8 @@ SIGNATURES = {
     "gbo_sincos_cr": (C.c_int, [_P, _I64, _P, _P, _P]),
     "gbo_prm_component_roots": (C.c_int, [_P, _P, _I64, _I64, _P]),
     "gbo_mt19937_discard": (C.c_int, [_P, _P, C.c_uint64]),
+    "gbo_nn_nearest_sqrt_approx": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P, _P, _P]),
+    "gbo_nn_nearest_sqrt_approx_host": (C.c_int, [_P, _P, _I64, _P, _P, _P]),
 }
 
 

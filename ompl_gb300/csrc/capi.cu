@@ -276,6 +276,7 @@ struct gbo_nn
     NNBoxCells cells;
     NNChainCells ccells;
     DevBuf qfeat, fb_list, part, qorder;
+    DevBuf ranks;  // keys of the present elements in order (approximate nearest after removals)
     CounterRing ctr;
     unsigned long long queries = 0;
     std::mutex mu;
@@ -1813,6 +1814,54 @@ gbo_status gbo_nn_nearest_r_fill(gbo_nn *nn, const double *q, int64_t nq, int64_
     return GBO_OK;
 }
 
+// NearestNeighborsSqrtApprox::nearest (NearestNeighborsSqrtApprox.h:91-115) for nq queries made one after
+// another. checks = 1 + floor(sqrt(n)) for the n present elements; *offset is the structure's offset
+// before the first query and after the last. Positions count the present elements in insertion order
+// (NearestNeighborsLinear's vector, whose remove erases); with removals a table of their keys is built
+// on the host.
+gbo_status gbo_nn_nearest_sqrt_approx(gbo_nn *nn, const double *q, int64_t nq, int64_t ld, int layout,
+                                      uint64_t *offset, int64_t *idx, double *dist, gbo_stream stream)
+{
+    Trace trace("gbo_nn_nearest_sqrt_approx");
+    if (!nn || !offset || nq < 0 || (nq > 0 && (!q || !idx || !dist)) ||
+        !(layout == GBO_LAYOUT_SOA ? ld >= nq : (layout == GBO_LAYOUT_AOS && ld >= nn->sp.dim)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearest arguments");
+    if (nq == 0)
+        return GBO_OK;
+    int64_t n = 0;
+    if (auto st = gbo_nn_size(nn, &n))
+        return st;
+    if (n == 0)
+        return fail(GBO_ERR_INVALID_ARGUMENT, "No elements found in nearest neighbors data structure");
+    const int64_t checks = 1 + (int64_t)std::floor(std::sqrt((double)n));
+    const cudaStream_t s = (cudaStream_t)stream;
+    const int64_t *rank = nullptr;
+    if (n != nn->size)
+    {
+        std::vector<unsigned char> alive((size_t)nn->size);
+        CUDA_TRY(cudaStreamSynchronize(s));
+        CUDA_TRY(cudaMemcpy(alive.data(), nn->alive, (size_t)nn->size, cudaMemcpyDeviceToHost));
+        std::vector<int64_t> keys;
+        keys.reserve((size_t)n);
+        for (int64_t k = 0; k < nn->size; ++k)
+            if (alive[(size_t)k])
+                keys.push_back(k);
+        if ((int64_t)keys.size() != n)
+            return fail(GBO_ERR_INVALID_ARGUMENT, "element count changed during the call");
+        if (auto st = nn->ranks.reserve(keys.size() * sizeof(int64_t), s))
+            return st;
+        CUDA_TRY(cudaMemcpyAsync(nn->ranks.p, keys.data(), keys.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        rank = (const int64_t *)nn->ranks.p;
+    }
+    launch_sqrt_approx(lcfg(stream), nn_args(nn), nn->sp, make_view(q, ld, layout), nq, n, checks,
+                       (unsigned long long)*offset, rank, idx, dist);
+    CHECK_LAUNCH();
+    if (rank)
+        CUDA_TRY(cudaStreamSynchronize(s));  // the key table is host memory's copy
+    *offset = (*offset + (uint64_t)nq) % (uint64_t)checks;
+    return GBO_OK;
+}
+
 gbo_status gbo_nn_error_stats(const gbo_nn *nn, float *max_abs_error, float *bound)
 {
     if (!nn)
@@ -1900,6 +1949,34 @@ gbo_status gbo_nn_nearest_k_host(gbo_nn *nn, const double *q, int64_t nq, int k,
     CUDA_TRY(cudaMemcpyAsync(nn->pin.p, di, bo, cudaMemcpyDeviceToHost, nn->host_stream));
     if (dist)
         CUDA_TRY(cudaMemcpyAsync((char *)nn->pin.p + bo, dd, bo, cudaMemcpyDeviceToHost, nn->host_stream));
+    CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
+    std::memcpy(idx, nn->pin.p, bo);
+    if (dist)
+        std::memcpy(dist, (char *)nn->pin.p + bo, bo);
+    return GBO_OK;
+}
+
+gbo_status gbo_nn_nearest_sqrt_approx_host(gbo_nn *nn, const double *q, int64_t nq, uint64_t *offset, int64_t *idx,
+                                           double *dist)
+{
+    if (!nn || !offset || nq < 0 || (nq > 0 && (!q || !idx)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad nearest arguments");
+    std::lock_guard<std::mutex> lk(nn->mu);
+    const size_t bq = (size_t)nq * nn->sp.dim * sizeof(double), bo = (size_t)nq * 8;
+    if (auto st = nn->pin.reserve(std::max(bq, 2 * bo) + 16))
+        return st;
+    if (auto st = nn->dev.reserve(bq + 2 * bo + 32, nn->host_stream))
+        return st;
+    char *d = (char *)nn->dev.p;
+    std::memcpy(nn->pin.p, q, bq);
+    CUDA_TRY(cudaMemcpyAsync(d, nn->pin.p, bq, cudaMemcpyHostToDevice, nn->host_stream));
+    int64_t *di = (int64_t *)(d + pad16(bq));
+    double *dd = (double *)(d + pad16(bq) + bo);
+    if (auto st = gbo_nn_nearest_sqrt_approx(nn, (const double *)d, nq, nn->sp.dim, GBO_LAYOUT_AOS, offset, di, dd,
+                                             nn->host_stream))
+        return st;
+    CUDA_TRY(cudaMemcpyAsync(nn->pin.p, di, bo, cudaMemcpyDeviceToHost, nn->host_stream));
+    CUDA_TRY(cudaMemcpyAsync((char *)nn->pin.p + bo, dd, bo, cudaMemcpyDeviceToHost, nn->host_stream));
     CUDA_TRY(cudaStreamSynchronize(nn->host_stream));
     std::memcpy(idx, nn->pin.p, bo);
     if (dist)

@@ -584,6 +584,75 @@ void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &
         launch_exact_t<16>(lc, nn, sp, qv, nq, k, prefix, idx, dist, list, list_n, max_items);
 }
 
+// NearestNeighborsSqrtApprox::nearest (NearestNeighborsSqrtApprox.h:91-115) for queries made one after
+// another: query q examines positions (j checks + off_q) % n, j < checks, of the n present elements in
+// insertion order (key rank[pos], or pos when none was removed) and returns the first strict minimum of
+// the FP64 distance (element, query) in j order. One warp per query, lanes over j, then the warp's
+// minimum of (distance, j). off_q is off0 for the first query and (off0 + q) % checks after it, as the
+// structure's offset advances by one (mod checks) per call.
+template <int MAXD>
+__global__ void __launch_bounds__(256) sqrt_approx_kernel(NNArgs nn, SpaceParams sp, StatesView qv, int64_t nq,
+                                                          int64_t n, int64_t checks, unsigned long long off0,
+                                                          const int64_t *rank, int64_t *idx, double *dist)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= nq)
+        return;
+    const unsigned long long un = (unsigned long long)n, uc = (unsigned long long)checks;
+    const unsigned long long off = q == 0 ? off0 : (off0 + (unsigned long long)q) % uc;
+    double qs[MAXD];
+    load_query<MAXD>(qv, q, sp.dim, qs);
+    double best = 0.0;
+    int64_t bj = -1;
+    for (int64_t j = lane; j < checks; j += 32)
+    {
+        const int64_t pos = (int64_t)(((unsigned long long)j * uc + off) % un);
+        const int64_t key = rank ? rank[pos] : pos;
+        double x[MAXD];
+        load_point<MAXD>(nn.pts64, nn.cap, sp.dim, key, x);
+        const double dd = distance64<MAXD>(sp, x, qs);
+        if (bj < 0 || dd < best)
+        {
+            best = dd;
+            bj = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int64_t oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (oj >= 0 && (bj < 0 || ob < best || (ob == best && oj < bj)))
+        {
+            best = ob;
+            bj = oj;
+        }
+    }
+    if (lane == 0)
+    {
+        const int64_t pos = (int64_t)(((unsigned long long)bj * uc + off) % un);
+        idx[q] = rank ? rank[pos] : pos;
+        dist[q] = best;
+    }
+}
+
+void launch_sqrt_approx(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, int64_t nq,
+                        int64_t n, int64_t checks, unsigned long long off0, const int64_t *rank, int64_t *idx,
+                        double *dist)
+{
+    if (nq == 0)
+        return;
+    const int grid = (int)((nq * 32 + 255) / 256);
+    if (sp.dim <= 2)
+        sqrt_approx_kernel<2><<<grid, 256, 0, lc.stream>>>(nn, sp, qv, nq, n, checks, off0, rank, idx, dist);
+    else if (sp.dim <= 8)
+        sqrt_approx_kernel<8><<<grid, 256, 0, lc.stream>>>(nn, sp, qv, nq, n, checks, off0, rank, idx, dist);
+    else
+        sqrt_approx_kernel<16><<<grid, 256, 0, lc.stream>>>(nn, sp, qv, nq, n, checks, off0, rank, idx, dist);
+    note_launch();
+}
+
 template <int KIND, int MAXD, int MAXF, int K_KEEP>
 static void launch_fp32_t(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, const float *qf,
                           int64_t nq, int k, const int64_t *prefix, int64_t *idx, double *dist,

@@ -15,6 +15,9 @@ struct NNArgs
     float eps32;                // bound on |distance_fp32 - distance_fp64|
 };
 
+void launch_sqrt_approx(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, int64_t nq,
+                        int64_t n, int64_t checks, unsigned long long off0, const int64_t *rank, int64_t *idx,
+                        double *dist);
 void launch_knn_exact(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, StatesView qv, int64_t nq, int k,
                       const int64_t *prefix, int64_t *idx, double *dist, const unsigned long long *list,
                       const unsigned long long *list_n, int64_t max_items);

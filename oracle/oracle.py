@@ -254,6 +254,22 @@ class Oracle:
                          idx.ctypes.data_as(C.POINTER(C.c_long)), _dp(dist))
         return idx, dist
 
+    def nn_sqrt_approx(self, sp, pts, queries, remove=()):
+        """NearestNeighborsSqrtApprox::nearest for each query in order, after removing `remove` rows one
+        at a time: (idx, dist, offset after the queries)."""
+        p = _rows(pts, sp.dim)
+        qq = _rows(queries, sp.dim)
+        rem = np.ascontiguousarray(np.asarray(remove, dtype=np.int64))
+        idx = np.empty(qq.shape[0], dtype=np.int64)
+        dist = np.empty(qq.shape[0])
+        s = sp.c()
+        lp = C.POINTER(C.c_long)
+        self.lib.ora_nn_sqrt_approx.restype = C.c_ulong
+        off = self.lib.ora_nn_sqrt_approx(C.byref(s), _dp(p), C.c_long(p.shape[0]), rem.ctypes.data_as(lp),
+                                          C.c_long(rem.size), _dp(qq), C.c_long(qq.shape[0]), idx.ctypes.data_as(lp),
+                                          _dp(dist))
+        return idx, dist, int(off)
+
     def knn_prefix(self, sp, pts, q, limit, k):
         pts, q = _rows(pts, sp.dim), _rows(q, sp.dim)
         limit = np.ascontiguousarray(limit, dtype=np.int64)

@@ -129,6 +129,13 @@ long ora_get_motion_states(const ora_space *s, const double *s1, const double *s
 void ora_knn(const ora_space *s, int algo, const double *pts, long npts, const double *q, long nq, int k,
              long *idx, double *dist);
 
+/* NearestNeighborsSqrtApprox::nearest (NearestNeighborsSqrtApprox.h:91-115) for nq queries made one after
+ * another on a fresh structure holding pts (added in one call), after removing the rows remove[0..nrem)
+ * one at a time: idx[i] = the row returned for query i, dist[i] = its distance to the query. Returns the
+ * structure's offset after the last query. */
+unsigned long ora_nn_sqrt_approx(const ora_space *s, const double *pts, long npts, const long *remove, long nrem,
+                                 const double *q, long nq, long *idx, double *dist);
+
 /* PRM-order prefix nearestK: query i sees only points with row index < limit[i]. */
 void ora_knn_prefix(const ora_space *s, const double *pts, long npts, const double *q, const long *limit, long nq,
                     int k, long *idx, double *dist);

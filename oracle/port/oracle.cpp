@@ -1080,6 +1080,51 @@ void ora_knn(const ora_space *d, int algo, const double *pts, long npts, const d
     knn_blocked(m, npts, nq, nullptr, k, idx, dist);
 }
 
+// NearestNeighborsSqrtApprox.h:91-125: the structure is NearestNeighborsLinear's vector (insertion order,
+// removals erase), checks_ = 1 + floor(sqrt(size)) after every add / remove; nearest() examines
+// positions (j checks_ + offset_) % n for j < checks_, keeps the first strict minimum of
+// distFun_(element, query), then offset_ = (offset_ + 1) % checks_.
+unsigned long ora_nn_sqrt_approx(const ora_space *d, const double *pts, long npts, const long *remove, long nrem,
+                                 const double *q, long nq, long *idx, double *dist)
+{
+    Space s = make_space(d);
+    std::vector<long> data((size_t)npts);
+    for (long i = 0; i < npts; ++i)
+        data[(size_t)i] = i;
+    for (long r = 0; r < nrem; ++r)
+    {
+        auto it = std::find(data.begin(), data.end(), remove[r]);
+        if (it != data.end())
+            data.erase(it);
+    }
+    const size_t n = data.size();
+    const size_t checks = 1 + (size_t)std::floor(std::sqrt((double)n));
+    size_t offset = 0;
+    for (long i = 0; i < nq; ++i)
+    {
+        const double *qi = q + (size_t)i * s.dim;
+        size_t pos = n;
+        double dmin = 0.0;
+        if (n > 0)
+        {
+            for (size_t j = 0; j < checks; ++j)
+            {
+                const size_t p = (j * checks + offset) % n;
+                const double dd = distance(s, pts + (size_t)data[p] * s.dim, qi);
+                if (pos == n || dmin > dd)
+                {
+                    pos = p;
+                    dmin = dd;
+                }
+            }
+            offset = (offset + 1) % checks;
+        }
+        idx[i] = pos == n ? -1 : data[pos];
+        dist[i] = pos == n ? std::numeric_limits<double>::infinity() : dmin;
+    }
+    return n ? (unsigned long)offset : 0;
+}
+
 void ora_knn_prefix(const ora_space *d, const double *pts, long npts, const double *q, const long *limit, long nq,
                     int k, long *idx, double *dist)
 {

@@ -517,6 +517,36 @@ void ora_knn(const ora_space *d, int algo, const double *pts, long npts, const d
     knn_impl(d, algo == ORA_NN_EXACT ? ORA_NN_REF_LINEAR : algo, pts, npts, q, nq, k, idx, dist);
 }
 
+// OMPL's own NearestNeighborsSqrtApprox: add all rows, remove some, then nearest() per query in order
+unsigned long ora_nn_sqrt_approx(const ora_space *d, const double *pts, long npts, const long *remove, long nrem,
+                                 const double *q, long nq, long *idx, double *dist)
+{
+    auto B = build(d, nullptr);
+    StateRows P(*B, pts, npts), Q(*B, q, nq);
+    ompl::NearestNeighborsSqrtApprox<long> nn;
+    nn.setDistanceFunction([&](const long &a, const long &b) {
+        const ob::State *sa = a >= 0 ? P.v[a] : Q.v[-1 - a];
+        const ob::State *sb = b >= 0 ? P.v[b] : Q.v[-1 - b];
+        return B->space->distance(sa, sb);
+    });
+    std::vector<long> all(npts);
+    for (long i = 0; i < npts; ++i)
+        all[i] = i;
+    nn.add(all);
+    for (long r = 0; r < nrem; ++r)
+        nn.remove(remove[r]);
+    for (long i = 0; i < nq; ++i)
+    {
+        const long e = nn.nearest(-1 - i);
+        idx[i] = e;
+        dist[i] = B->space->distance(P.v[e], Q.v[i]);
+    }
+    // the offset after the queries: offset_ is private, so it is recovered as (queries mod checks)
+    const std::size_t n = (std::size_t)(npts - nrem);
+    const std::size_t checks = n ? 1 + (std::size_t)std::floor(std::sqrt((double)n)) : 0;
+    return checks ? (unsigned long)(nq % checks) : 0;
+}
+
 // PRM order (geometric/planners/prm/src/PRM.cpp:570-604): each milestone queries the structure, then
 // is added to it, so query i sees exactly the milestones added before it.
 void ora_knn_prefix(const ora_space *d, const double *pts, long npts, const double *q, const long *limit, long nq,

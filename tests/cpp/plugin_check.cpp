@@ -6,6 +6,7 @@
 #include <ompl/base/samplers/UniformValidStateSampler.h>
 #include <ompl/base/spaces/RealVectorStateSpace.h>
 #include <ompl/datastructures/NearestNeighborsLinear.h>
+#include <ompl/datastructures/NearestNeighborsSqrtApprox.h>
 
 #include <cmath>
 #include <cstdio>
@@ -112,6 +113,18 @@ int main()
         mism += n1 != n2;
     }
     mism += gnn.size() != lnn.size();
+    // NearestNeighborsSqrtApprox: the same round-robin subset, call after call
+    gbompl::GpuNearestNeighborsSqrtApprox<ob::State *> gsq(ctx, [](ob::State *const &s) { return (const ob::State *)s; },
+                                                          4096);
+    ompl::NearestNeighborsSqrtApprox<ob::State *> lsq;
+    gsq.setDistanceFunction(df);
+    lsq.setDistanceFunction(df);
+    gsq.add(pts);
+    lsq.add(pts);
+    gsq.remove(pts[3]);
+    lsq.remove(pts[3]);
+    for (int q = 0; q < 200; ++q)
+        mism += gsq.nearest(pts[(q * 17) % pts.size()]) != lsq.nearest(pts[(q * 17) % pts.size()]);
     // UniformValidStateSampler: same seed, same calls (sample and sampleNear), same results (a few with
     // 2 attempts)
     space->setStateSamplerAllocator([](const ob::StateSpace *s) { return std::make_shared<SeededSampler>(s, 77); });

@@ -149,3 +149,26 @@ def test_real_vector_known_answers(port):
     sp = SpaceDesc(SPACE_REAL_VECTOR, 3, np.zeros(3), np.ones(3))
     assert abs(port.extent(sp) - math.sqrt(3.0)) < 1e-12
     assert np.allclose(port.interpolate(sp, np.zeros(3), np.ones(3), 0.5), 0.5)
+
+
+SQRT_CASES = {"rv2": (0, 2, 0.0), "chain10": (2, 10, 0.1), "wrap7": (3, 7, 0.0)}
+
+
+def sqrt_space(kind, dim, link):
+    from oracle.oracle import SpaceDesc
+    if kind == 0:
+        return SpaceDesc(kind, dim, np.zeros(dim), np.ones(dim))
+    if kind == 2:
+        return SpaceDesc(kind, dim, link_length=link)
+    return SpaceDesc(kind, dim)
+
+
+@pytest.mark.parametrize("name", list(SQRT_CASES))
+def test_sqrt_approx_nearest(port, golden, name):
+    # NearestNeighborsSqrtApprox.h:91-125 after add(all) and removals, queries in order
+    g = golden("sqrt_approx")
+    idx, dist, off = port.nn_sqrt_approx(sqrt_space(*SQRT_CASES[name]), g[f"{name}_pts"], g[f"{name}_q"],
+                                         g[f"{name}_remove"])
+    assert np.array_equal(idx, g[f"{name}_idx"])
+    assert same_bits(dist, g[f"{name}_dist"])
+    assert off == int(g[f"{name}_offset"])
