@@ -379,8 +379,28 @@ def ours(args, rank, world, local_rank):
     knn_idx, _ = nn.nearestK(q, 16, soa=True, want_dist=False)
     k1.record()
     torch.cuda.synchronize()
-    knn_qps = KNN_QUERIES / (k0.elapsed_time(k1) * 1e-3)
+    knn_ms = k0.elapsed_time(k1)
+    knn_qps = KNN_QUERIES / (knn_ms * 1e-3)
     knn_stats = nn.stats()
+    # roofline of the chain cell search: the element-feature and box bytes it read (counted on the
+    # device), over the call's time, against the measured copy bandwidth; DRAM traffic of one launch from
+    # the committed ncu summary (the 80 MB of features stay in L2)
+    knn_dram = None
+    kprof = os.path.join(ROOT, "profiles", "knn_ccell_warp_kernel_chain10.md")
+    if os.path.exists(kprof):
+        for line in open(kprof):
+            if line.startswith("traffic_bytes_per_launch:"):
+                knn_dram = int(line.split(":")[1])
+    knn_gbs = knn_stats["search_bytes"] / (knn_ms * 1e-3) / 1e9
+    knn_roofline = {"bound": "l2 latency (the 80 MB of features stay in L2)", "achieved": knn_gbs,
+                    "peak": PEAKS.get("hbm_gbs"), "unit": "GB/s",
+                    "frac": knn_gbs / PEAKS["hbm_gbs"] if PEAKS.get("hbm_gbs") else None,
+                    "work": f"{knn_stats['search_bytes']} bytes: 48 per visited element (links 4..9; the inner "
+                            "links' 32 bytes, read for candidates only, are not counted) and 160 per cell or "
+                            "chunk box tested",
+                    "note": "peak = measured HBM copy bandwidth, but these bytes are served from L2, so the "
+                            "fraction can exceed 1; traffic = DRAM bytes of one launch from ncu",
+                    "traffic": knn_dram, "feature_array_bytes": N_STATES * 80}
     knn_idx = knn_idx.cpu().numpy()
     pq = np.random.default_rng(12).choice(KNN_QUERIES, 500, replace=False)
     _, knn_dist500 = nn.nearestK(q[:, pq].contiguous(), 16, soa=True)
@@ -503,7 +523,7 @@ def ours(args, rank, world, local_rank):
                               "sin/cos could reverse"},
         "states_per_s": states_per_s,
         "knn_queries_per_s": knn_qps,
-        "knn": {"k": 16, "points": N_STATES, "queries": KNN_QUERIES, **knn_stats},
+        "knn": {**knn_stats, "k": 16, "points": N_STATES, "queries": KNN_QUERIES, "roofline": knn_roofline},
         "sampling": sampling,
         "recheck": stats,
         "clocks": clocks,

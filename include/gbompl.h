@@ -229,6 +229,10 @@ gbo_status gbo_nn_nearest_sqrt_approx_host(gbo_nn *nn, const double *q, int64_t 
  * assumes for it (the re-check band is twice that bound). */
 gbo_status gbo_nn_error_stats(const gbo_nn *nn, float *max_abs_error, float *bound);
 
+/* Bytes of element features and cell / chunk boxes that the last nearestK call's chain cell search read
+ * (no OMPL counterpart; the algorithmic traffic of that search, for its roofline). 0 for other paths. */
+gbo_status gbo_nn_search_bytes(const gbo_nn *nn, uint64_t *bytes);
+
 /* nearestK exactly as gbo_nn_nearest_k, but the call allocates no device memory (no counterpart in
  * OMPL). For callers that cannot allocate once set up: work captured into CUDA graphs, real-time
  * planning loops, processes whose GPU memory belongs to another allocator's pool. Scratch comes from

@@ -450,8 +450,10 @@ class NearestNeighborsGPU:
         check(lib().gbo_nn_stats(self._h, C.byref(q), C.byref(r), C.byref(f)))
         e, b = C.c_float(), C.c_float()
         check(lib().gbo_nn_error_stats(self._h, C.byref(e), C.byref(b)))
+        nb = C.c_uint64()
+        check(lib().gbo_nn_search_bytes(self._h, C.byref(nb)))
         return {"queries": q.value, "rechecked": r.value, "fallbacks": f.value, "max_fp32_error": e.value,
-                "fp32_error_bound": b.value}
+                "fp32_error_bound": b.value, "search_bytes": nb.value}
 
     def nearestK(self, queries, k, prefix=None, soa=False, want_dist=True, stream=None):
         t, n, ld, lay = _batch(queries, self.space.dim, soa)

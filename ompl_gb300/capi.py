@@ -95,6 +95,7 @@ SIGNATURES = {
     "gbo_mt19937_discard": (C.c_int, [_P, _P, C.c_uint64]),
     "gbo_nn_nearest_sqrt_approx": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P, _P, _P]),
     "gbo_nn_nearest_sqrt_approx_host": (C.c_int, [_P, _P, _I64, _P, _P, _P]),
+    "gbo_nn_search_bytes": (C.c_int, [_P, _P]),
 }
 
 

@@ -14,6 +14,7 @@ struct RunCounters
     unsigned long long rechecked;  // states (or segment counts / kNN queries) re-evaluated in FP64
     unsigned long long fallbacks;  // kNN queries answered by the exact FP64 scan
     unsigned long long hazards;    // FP64 decisions a one-ulp change of a sine or cosine could reverse
+    unsigned long long bytes;      // kNN cell search: feature and box bytes read
     unsigned int max_err_bits;     // kNN: largest |FP32 - FP64| distance of a re-checked candidate (float bits)
     unsigned int timeout;          // a bounded wait ran out
     unsigned int error;

@@ -1364,8 +1364,10 @@ bool launch_knn_bcell(const LaunchCfg &lc, const NNArgs &nn, const BoxCellArgs &
 
 // ---------------------------------------------------------------- cell index for the chain metric
 // Elements bucketed by the same key as the query order (the tip and middle-joint points, 8 levels per
-// coordinate: kQueryKeys cells); per cell the elements' features (20 floats, AoS, sorted by cell) and
-// their box (per feature the minimum and maximum). The box bounds the chain distance from below:
+// coordinate: kQueryKeys cells); per cell the elements' features (20 floats in five planes of float4,
+// plane j holding features 4j..4j+3 of every sorted position, so that a warp's 32 elements read 512
+// contiguous bytes per plane and the planes of links 4..9 form the search's hot set) and their box
+// (per feature the minimum and maximum). The box bounds the chain distance from below:
 // L * sum_i |(X_i, Y_i)(q) - box_i| <= L * sum_i |(X_i, Y_i)(q) - (X_i, Y_i)(e)| for every element e
 // of the cell (scaled by 1 - 1e-5 against the rounding of both sides, which see the same features).
 // The search is the warp-per-query one of the box kinds: own cell first (threshold seed), then the
@@ -1384,12 +1386,12 @@ __global__ void ccell_gather_kernel(const int64_t *skey, const int *start, const
             v[f] = f < F ? feat[(int64_t)f * cap + key] : 0.f;
 #pragma unroll
         for (int j = 0; j < 5; ++j)
-            sfeat[5 * p + j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            sfeat[(int64_t)j * n + p] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
     }
 }
 
 // box of cell c: 5 float4 of minima, then 5 of maxima (warp per cell)
-__global__ void ccell_box_kernel(const float4 *sfeat, const int *start, const int *count, float4 *box)
+__global__ void ccell_box_kernel(const float4 *sfeat, int64_t fs, const int *start, const int *count, float4 *box)
 {
     const int lane = threadIdx.x & 31;
     for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < kQueryKeys;
@@ -1407,7 +1409,7 @@ __global__ void ccell_box_kernel(const float4 *sfeat, const int *start, const in
 #pragma unroll
             for (int j = 0; j < 5; ++j)
             {
-                const float4 a = sfeat[5 * (int64_t)p + j];
+                const float4 a = sfeat[(int64_t)j * fs + p];
                 const float v[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
@@ -1441,18 +1443,194 @@ __global__ void ccell_box_kernel(const float4 *sfeat, const int *start, const in
     }
 }
 
+// Inside a cell, elements are ordered by a Morton code of two more joints (levels 0..31 of x and y of joints
+// dim/4 and 3 dim/4, bits interleaved), then by key, so that runs of kChunk consecutive elements
+// ("chunks") are close in those joints and their boxes bound the distance more tightly than the cell's. One
+// CTA per cell sorts (code, key) pairs in shared memory (bitonic sort); cells of more than kSortMax
+// elements keep the scatter's order (still exact, the chunk boxes are only looser).
+constexpr int kSortMax = 16384;
+constexpr int kChunk = 32;  // elements per chunk: one chunk per warp step (16 per chunk, two chunks a step,
+                            // visited fewer elements but took 10% longer)
+
+__device__ __forceinline__ unsigned ccell_code(const SpaceParams &sp, const float *feat, int64_t cap, int64_t key)
+{
+    const int joints[2] = {sp.dim / 4, (3 * sp.dim) / 4};
+    unsigned lv[4];
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+    {
+        const float r = 2.5f * sqrtf(0.5f * (float)(joints[t] + 1));
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+        {
+            const float v = feat[(int64_t)(2 * joints[t] + c) * cap + key];
+            int l = (int)floorf((v + r) * (32.0f / (2.0f * r)));
+            lv[2 * t + c] = (unsigned)(l < 0 ? 0 : (l > 31 ? 31 : l));
+        }
+    }
+    unsigned code = 0;
+#pragma unroll
+    for (int b = 4; b >= 0; --b)
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            code = (code << 1) | ((lv[t] >> b) & 1u);
+    return code;
+}
+
+__global__ void __launch_bounds__(512) ccell_sort_kernel(SpaceParams sp, const float *feat, int64_t cap,
+                                                         const int *start, const int *count, int64_t *skey)
+{
+    extern __shared__ unsigned long long sv[];
+    const int c = blockIdx.x, n = count[c], s0 = start[c];
+    if (n < 2 || n > kSortMax)
+        return;
+    int np = 1;
+    while (np < n)
+        np <<= 1;
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+    {
+        unsigned long long v = ~0ull;
+        if (i < n)
+        {
+            const int64_t key = skey[s0 + i];
+            v = ((unsigned long long)ccell_code(sp, feat, cap, key) << 32) | (unsigned long long)(unsigned)key;
+        }
+        sv[i] = v;
+    }
+    __syncthreads();
+    for (int k = 2; k <= np; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+            for (int i = threadIdx.x; i < np; i += blockDim.x)
+            {
+                const int ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const unsigned long long a = sv[i], b = sv[ixj];
+                    if ((a > b) == ((i & k) == 0))
+                    {
+                        sv[i] = b;
+                        sv[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        skey[s0 + i] = (int64_t)(unsigned)(sv[i] & 0xffffffffull);
+}
+
+// first chunk of each cell: exclusive scan of ceil(count / kChunk) over the 4096 cells (one CTA of 1024)
+__global__ void __launch_bounds__(1024) ccell_chunk_scan_kernel(const int *count, int *cstart)
+{
+    __shared__ int part[1024];
+    const int i0 = threadIdx.x * 4;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+    {
+        v[t] = (count[i0 + t] + kChunk - 1) / kChunk;
+        sum += v[t];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const int x = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    int run = part[threadIdx.x] - sum;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+    {
+        cstart[i0 + t] = run;
+        run += v[t];
+    }
+    if (threadIdx.x == 1023)
+        cstart[kQueryKeys] = part[1023];
+}
+
+// box of each chunk (warp per chunk, lane per element): 5 float4 of minima, then 5 of maxima
+__global__ void ccell_chunk_box_kernel(const float4 *sfeat, int64_t fs, const int *start, const int *count,
+                                       const int *cstart,
+                                       float4 *cbox)
+{
+    const int lane = threadIdx.x & 31;
+    const int nchunks = cstart[kQueryKeys];
+    for (int ch = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); ch < nchunks;
+         ch += (int)((gridDim.x * blockDim.x) >> 5))
+    {
+        // the cell of chunk ch: the last c with cstart[c] <= ch (binary search)
+        int lo = 0, hi = kQueryKeys - 1;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (cstart[mid] <= ch)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int c = lo;
+        const int p0 = start[c] + kChunk * (ch - cstart[c]), p1 = min(p0 + kChunk, start[c] + count[c]);
+        const int p = p0 + lane;
+        float v[20];
+#pragma unroll
+        for (int j = 0; j < 5; ++j)
+        {
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p < p1)
+                a = sfeat[(int64_t)j * fs + p];
+            v[4 * j] = a.x;
+            v[4 * j + 1] = a.y;
+            v[4 * j + 2] = a.z;
+            v[4 * j + 3] = a.w;
+        }
+        float mn[20], mx[20];
+#pragma unroll
+        for (int f = 0; f < 20; ++f)
+        {
+            mn[f] = p < p1 ? v[f] : __int_as_float(0x7f800000);
+            mx[f] = p < p1 ? v[f] : -__int_as_float(0x7f800000);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                mn[f] = fminf(mn[f], __shfl_xor_sync(0xffffffffu, mn[f], o));
+                mx[f] = fmaxf(mx[f], __shfl_xor_sync(0xffffffffu, mx[f], o));
+            }
+        }
+        if (lane < 10)
+        {
+            const float *m = lane < 5 ? mn : mx;
+            const int j = lane < 5 ? lane : lane - 5;
+            float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int jj = 0; jj < 5; ++jj)
+                if (jj == j)
+                    out = make_float4(m[4 * jj], m[4 * jj + 1], m[4 * jj + 2], m[4 * jj + 3]);
+            cbox[10 * (int64_t)ch + lane] = out;
+        }
+    }
+}
+
 void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int *key, int *count,
-                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box)
+                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box, int *cstart, float4 *cbox)
 {
     const int grid = grid_for(lc, nn.size);
     cudaMemsetAsync(count, 0, kQueryKeys * sizeof(int), lc.stream);
     query_key_kernel<<<grid, 256, 0, lc.stream>>>(sp, nn.feat32, nn.cap, nn.size, nn.alive, key, count);
     query_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, start, fill);
     query_scatter_kernel<<<grid, 256, 0, lc.stream>>>(key, nn.size, start, fill, skey);
+    const int smem = kSortMax * (int)sizeof(unsigned long long);
+    cudaFuncSetAttribute(ccell_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    ccell_sort_kernel<<<kQueryKeys, 512, smem, lc.stream>>>(sp, nn.feat32, nn.cap, start, count, skey);
     ccell_gather_kernel<<<grid, 256, 0, lc.stream>>>(skey, start, count, nn.feat32, nn.cap, 2 * sp.dim, nn.size,
                                                      sfeat);
-    ccell_box_kernel<<<(kQueryKeys * 32 + 255) / 256, 256, 0, lc.stream>>>(sfeat, start, count, box);
-    for (int i = 0; i < 5; ++i)
+    ccell_box_kernel<<<(kQueryKeys * 32 + 255) / 256, 256, 0, lc.stream>>>(sfeat, nn.size, start, count, box);
+    ccell_chunk_scan_kernel<<<1, 1024, 0, lc.stream>>>(count, cstart);
+    ccell_chunk_box_kernel<<<lc.sm_count * 8, 256, 0, lc.stream>>>(sfeat, nn.size, start, count, cstart, cbox);
+    for (int i = 0; i < 8; ++i)
         note_launch();
 }
 
@@ -1480,10 +1658,12 @@ __device__ __forceinline__ float ccell_lb(const float4 *b, const float *q, int d
     return s;
 }
 
+// 3 CTAs per SM: 80 registers without spills (the default choice, 64 registers for 4 CTAs, spilled)
 template <int K_KEEP>
-__global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, SpaceParams sp, float eps,
+__global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci, SpaceParams sp, float eps,
                                                              const float *qf, int64_t nq, const int64_t *qorder,
-                                                             const int *qkey, int k, float *part_d, int64_t *part_k)
+                                                             const int *qkey, int k, float *part_d, int64_t *part_k,
+                                                             RunCounters *ctr)
 {
     const int lane = threadIdx.x & 31;
     const int64_t qs = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1498,9 +1678,9 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
     const float link = (float)sp.link;
     WarpList<K_KEEP> L;
     L.init();
-    auto scan_cell = [&](int c, float T) {
-        const int s0 = ci.start[c], s1 = s0 + ci.count[c];
-        for (int p0 = s0; p0 < s1; p0 += 32)
+    unsigned long long nbytes = 0;  // feature and box bytes read for this query (lane 0)
+    // the elements of one chunk (positions p0 .. s1 - 1, at most 32), one lane each
+    auto scan_chunk = [&](int p0, int s1, float T) {
         {
             const int p = p0 + lane;
             float d = __int_as_float(0x7f800000);
@@ -1515,7 +1695,7 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
 #pragma unroll
                 for (int j = 2; j < 5; ++j)
                 {
-                    const float4 a = ci.sfeat[5 * (int64_t)p + j];
+                    const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
                     pf[4 * j] = a.x;
                     pf[4 * j + 1] = a.y;
                     pf[4 * j + 2] = a.z;
@@ -1534,7 +1714,7 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
 #pragma unroll
                     for (int j = 0; j < 2; ++j)
                     {
-                        const float4 a = ci.sfeat[5 * (int64_t)p + j];
+                        const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
                         pf[4 * j] = a.x;
                         pf[4 * j + 1] = a.y;
                         pf[4 * j + 2] = a.z;
@@ -1564,6 +1744,32 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
             }
         }
     };
+    // a cell: its chunks' boxes (lanes over chunks), then the elements of the chunks whose bound is below
+    // min(T, the list's last entry), rechecked against the bound of the moment
+    auto scan_cell = [&](int c, float T) {
+        const int s0 = ci.start[c], s1 = s0 + ci.count[c];
+        const int c0 = ci.cstart[c], c1 = ci.cstart[c + 1];
+        for (int cb = c0; cb < c1; cb += 32)
+        {
+            const int ch = cb + lane;
+            float lb = __int_as_float(0x7f800000);
+            if (ch < c1)
+                lb = ccell_lb(ci.cbox + 10 * (int64_t)ch, qfe, sp.dim) * link * (1.0f - 1e-5f);
+            nbytes += 160ull * (unsigned)min(32, c1 - cb);
+            unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
+            while (m)
+            {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                if (__shfl_sync(0xffffffffu, lb, src) < fminf(T, L.last()))
+                {
+                    const int p0 = s0 + kChunk * (cb + src - c0), p1 = min(p0 + kChunk, s1);
+                    nbytes += 48ull * (unsigned)(p1 - p0);  // links 4.. of each element (inner links not counted)
+                    scan_chunk(p0, p1, T);
+                }
+            }
+        }
+    };
     const int own = qkey[qi];
     scan_cell(own, __int_as_float(0x7f800000));
     float T = __int_as_float(0x7f800000);
@@ -1590,6 +1796,7 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
         float lb = __int_as_float(0x7f800000);
         if (ok && ci.count[c] > 0)
             lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        nbytes += 160ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
         unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
         {
@@ -1624,6 +1831,7 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
         float lb = __int_as_float(0x7f800000);
         if (!near_own(c) && ci.count[c] > 0)
             lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        nbytes += 160ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
         unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
         {
@@ -1643,6 +1851,8 @@ __global__ void __launch_bounds__(256) knn_ccell_warp_kernel(ChainCellArgs ci, S
             part_d[qs * K_KEEP + 32 * s + lane] = L.d[s];
             part_k[qs * K_KEEP + 32 * s + lane] = L.k[s];
         }
+    if (lane == 0 && ctr)
+        atomicAdd(&ctr->bytes, nbytes);
 }
 
 bool launch_knn_ccell(const LaunchCfg &lc, const NNArgs &nn, const ChainCellArgs &ci, const SpaceParams &sp,
@@ -1655,13 +1865,15 @@ bool launch_knn_ccell(const LaunchCfg &lc, const NNArgs &nn, const ChainCellArgs
     const int qb = (int)((nq + 127) / 128), wg = (int)((nq * 32 + 255) / 256);
     if (k <= 12)
     {
-        knn_ccell_warp_kernel<16><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k);
+        knn_ccell_warp_kernel<16><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k,
+                                                             ctr);
         knn_finish_kernel<GBO_SPACE_KINEMATIC_CHAIN, 10, 16><<<qb, 128, 0, lc.stream>>>(
             nn, sp, qv, nq, k, 1, part_d, part_k, idx, dist, fb_list, fb_n, ctr, qorder);
     }
     else
     {
-        knn_ccell_warp_kernel<24><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k);
+        knn_ccell_warp_kernel<24><<<wg, 256, 0, lc.stream>>>(ci, sp, nn.eps32, qf, nq, qorder, qkey, k, part_d, part_k,
+                                                             ctr);
         knn_finish_kernel<GBO_SPACE_KINEMATIC_CHAIN, 10, 24><<<qb, 128, 0, lc.stream>>>(
             nn, sp, qv, nq, k, 1, part_d, part_k, idx, dist, fb_list, fb_n, ctr, qorder);
     }
