@@ -1410,14 +1410,35 @@ gbo_status gbo_sample_gaussian(gbo_sampler *s, const double *mean, double stddev
     const int64_t cap = std::min<int64_t>(((int64_t)1 << 24) + 628,
                                           4 * (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0) + 628);
     cudaStream_t st = (cudaStream_t)stream;
-    if (auto e = s->words.reserve((size_t)cap * sizeof(unsigned), st))
+    // large chunks draw their candidates' words on jump-ahead segments (segment length chosen as for
+    // sampleUniform from the first chunk's words; later chunks are shorter and use fewer segments)
+    const int64_t W0 = 4 * ((cap - 624) / 4);  // the most words a chunk draws (4 per candidate)
+    const uint32_t *polys = nullptr;
+    int64_t L = 0, jump_words = 0;
+    if (W0 >= ((int64_t)1 << 18) && mt_field_ready())
+    {
+        int m = 15;
+        while (m < 24 && W0 > ((int64_t)160 << m))
+            ++m;
+        L = (int64_t)1 << m;
+        const int nseg = (int)((W0 + L - 1) / L);
+        if (nseg > 1)
+            if (auto e = mt_jump_table((uint64_t)L, nseg - 1, &polys))
+                return fail(e, "jump-ahead polynomials could not be prepared");
+        if (nseg == 1)
+            polys = nullptr;
+        jump_words = sample_jump_words(nseg, 0);
+    }
+    const int64_t cap_al = (cap + 3) & ~(int64_t)3;
+    if (auto e = s->words.reserve((size_t)(cap_al + jump_words) * sizeof(unsigned), st))
         return e;
     if (auto e = s->gwork.reserve(sizeof(GaussChunk) + sizeof(long long) * (size_t)(cap / 4096 + 2), st))
         return e;
     const StatesView ov = make_view(out, ld, layout);
     const int64_t chunks = launch_sample_gaussian(
         lcfg(st), s->st, s->has_saved, s->sp, make_view(mean, ld, layout), stddev, n, MutStatesView{out, ov.si, ov.sd},
-        (unsigned *)s->words.p, cap, (GaussChunk *)s->gwork.p, (long long *)((char *)s->gwork.p + sizeof(GaussChunk)));
+        (unsigned *)s->words.p, cap, (GaussChunk *)s->gwork.p, (long long *)((char *)s->gwork.p + sizeof(GaussChunk)),
+        polys ? (unsigned *)s->words.p + cap_al : nullptr, polys, L);
     if (chunks < 0)
         return fail(GBO_ERR_CUDA, std::string("sampleGaussian: ") + cudaGetErrorString(cudaGetLastError()));
     CHECK_LAUNCH();

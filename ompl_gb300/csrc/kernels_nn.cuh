@@ -118,7 +118,8 @@ gbo_status mt_jump_table(uint64_t L, int K, const uint32_t **out);
 // (cap_words / 4096 + 2) long longs.
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
-                               int64_t cap_words, GaussChunk *ctl, long long *cnt);
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt, unsigned *jump_scratch,
+                               const uint32_t *polys, int64_t L);
 double measure_fp32_peak(const LaunchCfg &lc);
 double measure_fp64_peak(const LaunchCfg &lc);
 void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s);

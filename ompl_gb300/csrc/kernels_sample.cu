@@ -428,7 +428,9 @@ static void launch_jump(const LaunchCfg &lc, const unsigned *u, const uint32_t *
 
 // One CTA per segment s: words [s L, min((s + 1) L, W)) of the call from window s, tempered and stored
 // as the recurrence produces them (word j of the call at words[j]); the last segment leaves its
-// generator in st.
+// generator in st. kRaw: the words are stored untempered and st is left unchanged (sampleGaussian's
+// speculative draws, committed afterwards).
+template <bool kRaw>
 __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const unsigned *states, int64_t L,
                                                          int64_t W, int nseg, unsigned *words)
 {
@@ -444,7 +446,7 @@ __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const
     __syncthreads();
     int64_t w = min((int64_t)(624 - pos), len);  // the rest of the first block
     for (int i = t; i < (int)w; i += blockDim.x)
-        o[i] = temper(cur[pos + i]);
+        o[i] = kRaw ? cur[pos + i] : temper(cur[pos + i]);
     pos += (int)w;
 #pragma unroll 1
     while (w < len)
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const
             const unsigned v = twist_word(cur[t], cur[t + 1], cur[t + 397]);
             nxt[t] = v;
             if (t < m)
-                ob[t] = temper(v);
+                ob[t] = kRaw ? v : temper(v);
         }
         __syncthreads();
         if (t < 227)
@@ -464,7 +466,7 @@ __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const
             const unsigned v = twist_word(cur[t + 227], cur[t + 228], nxt[t]);
             nxt[t + 227] = v;
             if (t + 227 < m)
-                ob[t + 227] = temper(v);
+                ob[t + 227] = kRaw ? v : temper(v);
         }
         __syncthreads();
         if (t < 170)
@@ -473,7 +475,7 @@ __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const
                                        : twist_word(cur[623], nxt[0], nxt[396]);
             nxt[t + 454] = v;
             if (t + 454 < m)
-                ob[t + 454] = temper(v);
+                ob[t + 454] = kRaw ? v : temper(v);
         }
         __syncthreads();
         unsigned *tmp = cur;
@@ -482,7 +484,7 @@ __global__ void __launch_bounds__(256) mt_segment_kernel(SamplerState *st, const
         w += m;
         pos = m;
     }
-    if (s == nseg - 1)
+    if (!kRaw && s == nseg - 1)
     {
         for (int i = t; i < 624; i += blockDim.x)
             st->mt[i] = cur[i];
@@ -534,11 +536,32 @@ void launch_sample_uniform_jump(const LaunchCfg &lc, SamplerState *st, const Spa
         launch_jump(lc, u, (const unsigned *)polys, K, states);
         note_launch();
     }
-    mt_segment_kernel<<<nseg, 256, 0, lc.stream>>>(st, states, L, W, nseg, words);
+    mt_segment_kernel<false><<<nseg, 256, 0, lc.stream>>>(st, states, L, W, nseg, words);
     const unsigned long long magic = ((1ull << 40) + (unsigned long long)sp.dim - 1) / (unsigned long long)sp.dim;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((values + 255) / 256, (int64_t)lc.sm_count * 16));
     pairs_to_states_kernel<<<grid, 256, 0, lc.stream>>>((const uint2 *)words, values, sp, magic, nearv, near != nullptr,
                                                         distance, out);
+    note_launch();
+    note_launch();
+}
+
+// The next W raw (untempered) words of the stream after the sampler's next word into raw[0 .. W), the
+// generator unchanged: the segmented generation of sampleUniform without the conversion.
+static void launch_raw_words_jump(const LaunchCfg &lc, const SamplerState *st, int64_t W, unsigned *raw,
+                                  unsigned *scratch, const uint32_t *polys, int64_t L)
+{
+    const int nseg = (int)((W + L - 1) / L);
+    unsigned *u = scratch, *states = scratch + kJumpU;
+    const int K = nseg - 1;
+    if (K > 0)
+        cudaMemsetAsync(states + 625, 0, (size_t)K * 625 * sizeof(unsigned), lc.stream);
+    mt_window_seq_kernel<<<1, 256, 0, lc.stream>>>(st, kJumpU, u, states);
+    if (K > 0)
+    {
+        launch_jump(lc, u, polys, K, states);
+        note_launch();
+    }
+    mt_segment_kernel<true><<<nseg, 256, 0, lc.stream>>>(nullptr, states, L, W, nseg, raw);
     note_launch();
     note_launch();
 }
@@ -764,9 +787,39 @@ __global__ void __launch_bounds__(256) gauss_advance_kernel(SamplerState *st, co
         st->pos = (unsigned)(K - start);
 }
 
+// The same commit when raw holds exactly the words after the sampler's next one (segmented form): the
+// generator after word K is the window of the 624 words before it (position 624), taken from the old
+// block for the part before raw[0].
+__global__ void __launch_bounds__(256) gauss_advance_seg_kernel(SamplerState *st, const unsigned *raw, int64_t W,
+                                                                const GaussChunk *ctl)
+{
+    __shared__ unsigned old[624];
+    const long long c = ctl->consumed;
+    const int64_t K = c >= 0 ? c : W;
+    const int pos = (int)st->pos;
+    for (int i = threadIdx.x; i < 624; i += blockDim.x)
+        old[i] = st->mt[i];
+    __syncthreads();  // every thread has read pos and the block
+    const int64_t r = 624 - pos;
+    if (K <= r)
+    {
+        if (threadIdx.x == 0)
+            st->pos = (unsigned)(pos + K);
+        return;
+    }
+    for (int i = threadIdx.x; i < 624; i += blockDim.x)
+    {
+        const int64_t m = K - 624 + i;  // word m of raw (m < 0: the old block's word pos + m)
+        st->mt[i] = m < 0 ? old[pos + m] : raw[m];
+    }
+    if (threadIdx.x == 0)
+        st->pos = 624u;
+}
+
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
-                               int64_t cap_words, GaussChunk *ctl, long long *cnt)
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt, unsigned *jump_scratch,
+                               const uint32_t *polys, int64_t L)
 {
     const int64_t M = n * sp.dim;
     if (M == 0)
@@ -786,12 +839,20 @@ int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_s
         const double mu = (double)need / 0.7853981633974483;
         const int64_t G = std::max<int64_t>(1, std::min<int64_t>(gmax, (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0)));
         const int nb = (int)((G + kGaussPerCta - 1) / kGaussPerCta);
-        mt_words_kernel<true><<<1, 256, 0, lc.stream>>>(st, 4 * G, words);
+        // segmented (jump-ahead) generation of the candidates' words when the chunk is large
+        const bool seg = polys && 4 * G >= ((int64_t)1 << 18);
+        if (seg)
+            launch_raw_words_jump(lc, st, 4 * G, words, jump_scratch, polys, L);
+        else
+            mt_words_kernel<true><<<1, 256, 0, lc.stream>>>(st, 4 * G, words);
         gauss_count_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt);
         gauss_scan_kernel<<<1, 1024, 0, lc.stream>>>(cnt, nb, ctl);
         GaussArgs a{(const uint4 *)words, G, cnt, need, v, M, stddev, sp, meanv, out, st, ctl};
         gauss_values_kernel<<<nb, 256, 0, lc.stream>>>(a);
-        gauss_advance_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
+        if (seg)
+            gauss_advance_seg_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
+        else
+            gauss_advance_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
         for (int i = 0; i < 5; ++i)
             note_launch();
         GaussChunk h{};

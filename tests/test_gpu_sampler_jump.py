@@ -75,3 +75,26 @@ def test_near_on_segments_so2(port):
     near = rng.uniform(-math.pi, math.pi, size=(2 ** 18, 1))
     got = B.StateSampler(B.SO2StateSpace(), 21).sampleUniformNear(near, 2.5)
     assert same_bits(got, port.sample_uniform_near(d, 21, near, 2.5))
+
+
+def test_gaussian_calls_on_segments_continue_one_stream(port):
+    """sampleGaussian draws a large call's polar candidates on jump-ahead segments and commits exactly the
+    words used: calls below and above the switch, interleaved with uniform calls and with the cached
+    second value crossing calls, against the oracle's polar method (log rounded to nearest)."""
+    d = SpaceDesc(capi.SPACE_REAL_VECTOR, 7, np.full(7, -2.0), np.full(7, 2.0))
+    space = B.RealVectorStateSpace(7, d.low, d.high)
+    rng = np.random.default_rng(8)
+    ops = [("uniform", 300), ("gaussian", 20_001), ("gaussian", 40_000), ("uniform", 5), ("gaussian", 3),
+           ("gaussian", 150_001), ("uniform", 7)]
+    n_mean = sum(c for k, c in ops if k == "gaussian")
+    mean = rng.uniform(-1.5, 1.5, size=(n_mean, 7))
+    smp = B.StateSampler(space, 123)
+    got, mi = [], 0
+    for kind, c in ops:
+        if kind == "uniform":
+            got.append(smp.sampleUniform(c))
+        else:
+            got.append(smp.sampleGaussian(mean[mi:mi + c], 0.4))
+            mi += c
+    want = port.sample_script(d, 123, ops, mean, 0.4, log_mode=1)
+    assert same_bits(np.vstack(got), want)
