@@ -63,7 +63,8 @@ def parse():
     p.add_argument("--workload", default="chain", choices=["chain", "arm", "prm", "serve", "rrt"],
                    help="chain: the headline 10-link chain workload; arm: 7-DoF DH arm, 256k edges of 2..2000 "
                         "steps; prm: PRM roadmap of the DH arm among 16,384 spheres from 2M samples")
-    p.add_argument("--profile", default=None, choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm", "sample"],
+    p.add_argument("--profile", default=None,
+                   choices=["validity", "motion", "motion_plain", "knn", "peaks", "arm", "sample", "gauss"],
                    help="launch one kernel kind twice on the chain workload (for ncu) and exit")
     p.add_argument("--only-headline", action="store_true",
                    help="the chain workload alone (no circles / arm / serving / PRM objects)")
@@ -565,6 +566,15 @@ def profile(kind):
         smp = B.StateSampler(space, 5)
         for _ in range(3):
             smp.sampleUniform(N_STATES, soa=True, host=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": kind, "ok": True}))
+        return
+    if kind == "gauss":
+        # sampleGaussian of 1M states of the 10-D chain space around uniform means, three calls
+        smp = B.StateSampler(space, 5)
+        means = smp.sampleUniform(N_STATES, host=False)
+        for _ in range(3):
+            smp.sampleGaussian(means, 0.1)
         torch.cuda.synchronize()
         print(json.dumps({"profile": kind, "ok": True}))
         return

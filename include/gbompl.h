@@ -309,6 +309,9 @@ gbo_status gbo_measure_fp64_peak(double *flops, gbo_stream stream);
 /* Correctly rounded FP64 sin and cos (the device routine of the FP64 forms) of n device values, for
  * tests. No reference counterpart (diagnostic). */
 gbo_status gbo_sincos_cr(const double *x, int64_t n, double *sin_out, double *cos_out, gbo_stream stream);
+/* FP64 natural log rounded to nearest (the device routine of sampleGaussian's polar method) of n positive
+ * normal device values, for tests. No reference counterpart (diagnostic). */
+gbo_status gbo_log_rn(const double *x, int64_t n, double *out, gbo_stream stream);
 /* Component tags of a PRM roadmap (replaces boost::disjoint_sets in PRM::addMilestone /
  * PRM::uniteComponents, src/ompl/geometric/planners/prm/src/PRM.cpp:580-609, read by
  * PRM::getPlannerData, PRM.cpp:729-756): union_set(src[e], dst[e]) for e = 0..n_edges-1 in order, union

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gbo_checker_counters": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "gbo_checker_precision_stats": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P]),
     "gbo_sincos_cr": (C.c_int, [_P, _I64, _P, _P, _P]),
+    "gbo_log_rn": (C.c_int, [_P, _I64, _P, _P]),
     "gbo_prm_component_roots": (C.c_int, [_P, _P, _I64, _I64, _P]),
     "gbo_mt19937_discard": (C.c_int, [_P, _P, C.c_uint64]),
     "gbo_nn_nearest_sqrt_approx": (C.c_int, [_P, _P, _I64, _I64, C.c_int, _P, _P, _P, _P]),

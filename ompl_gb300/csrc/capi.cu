@@ -2203,6 +2203,17 @@ gbo_status gbo_sincos32(const double *theta, int64_t n, float *cos_out, float *s
     return GBO_OK;
 }
 
+gbo_status gbo_log_rn(const double *x, int64_t n, double *out, gbo_stream stream)
+{
+    if (n < 0 || n > (int64_t)INT32_MAX * 256 || (n > 0 && (!x || !out)))
+        return fail(GBO_ERR_INVALID_ARGUMENT, "bad log_rn arguments");
+    if (auto st = ensure_device())
+        return st;
+    launch_log_rn(lcfg(stream), x, n, out);
+    CHECK_LAUNCH();
+    return GBO_OK;
+}
+
 gbo_status gbo_sincos_cr(const double *x, int64_t n, double *sin_out, double *cos_out, gbo_stream stream)
 {
     if (n < 0 || (n > 0 && (!x || !sin_out || !cos_out)))

@@ -120,6 +120,8 @@ int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_s
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
                                int64_t cap_words, GaussChunk *ctl, long long *cnt, unsigned *jump_scratch,
                                const uint32_t *polys, int64_t L);
+// log_rn (the sampleGaussian log, rounded to nearest) of n device values, for tests.
+void launch_log_rn(const LaunchCfg &lc, const double *x, int64_t n, double *out);
 double measure_fp32_peak(const LaunchCfg &lc);
 double measure_fp64_peak(const LaunchCfg &lc);
 void launch_sincos32(const LaunchCfg &lc, const double *theta, int64_t n, float *c, float *s);

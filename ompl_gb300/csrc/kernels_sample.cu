@@ -574,7 +574,7 @@ static void launch_raw_words_jump(const LaunchCfg &lc, const SamplerState *st, i
 // a candidate takes two uniform01 draws (4 stream words), x = 2U - 1, y = 2V - 1, r2 = x^2 + y^2, and is
 // rejected while r2 > 1 or r2 == 0; an accepted one gives mult = sqrt(-2 log(r2) / r2) and the values
 // y * mult (returned) then x * mult (cached for the next draw of the same RNG, across calls).
-// Every operation is the same IEEE double operation except log, which is log_cr (crlog.cuh, rounded
+// Every operation is the same IEEE double operation except log, which is log_rn (crlog.cuh, rounded
 // to nearest); glibc's log differs from the correctly rounded value in the last bit for a small
 // fraction of arguments, and only the values of those pairs differ (by an ulp or two).
 //
@@ -708,59 +708,101 @@ struct GaussArgs
     GaussChunk *ctl;
 };
 
+// Pair j from candidate (x, y) with r2 = x^2 + y^2 and lg = log(r2).
+__device__ __forceinline__ void gauss_pair(const GaussArgs &a, int64_t j, double x, double y, double r2, double lg)
+{
+    const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lg), r2));
+    const double g1 = __dmul_rn(y, mult), g2 = __dmul_rn(x, mult);
+    const int64_t v = a.v0 + 2 * j;
+    gauss_emit(a.sp, a.mean, a.stddev, a.out, v, g1);
+    if (v + 1 < a.M)
+        gauss_emit(a.sp, a.mean, a.stddev, a.out, v + 1, g2);
+    else
+    {
+        a.st->saved = g2;
+        a.st->has_saved = 1;
+    }
+}
+
 // Accepted candidate j of the chunk (in stream order) becomes pair j: values v0 + 2j and v0 + 2j + 1.
+// A CTA ranks its candidates' acceptances and stores the accepted (x, y) compacted in stream order, so
+// that its threads then evaluate consecutive pairs with no lane idle on a rejected candidate (and store
+// consecutive values). The pairs whose log the plain-FP64 evaluation cannot round (about 6 %) are queued
+// and finished after the others by consecutive threads, so that the double-double evaluation runs in a
+// few dense warps instead of in most warps for one lane each.
 __global__ void __launch_bounds__(256) gauss_values_kernel(const __grid_constant__ GaussArgs a)
 {
+    __shared__ double2 sxy[kGaussPerCta];          // accepted (x, y) by local pair index
+    __shared__ unsigned short slow[kGaussPerCta];  // local pair indices left to log_cr
     __shared__ int wcnt[4][8];
+    __shared__ int nslow;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const long long rank0 = a.off[blockIdx.x];
+    if (rank0 >= a.need)
+        return;  // the call's pairs all come from earlier candidates
+    if (t == 0)
+        nslow = 0;
     const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
+    double xs[4], ys[4];
     unsigned bal[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
     {
         const int64_t k = base + r * 256 + t;
         bool acc = false;
+        xs[r] = ys[r] = 0.0;
         if (k < a.G)
         {
-            double x, y, r2;
-            acc = polar_candidate(a.cand[k], x, y, r2);
+            double r2;
+            acc = polar_candidate(a.cand[k], xs[r], ys[r], r2);
         }
         bal[r] = __ballot_sync(0xffffffffu, acc);
         if (lane == 0)
             wcnt[r][warp] = __popc(bal[r]);
     }
     __syncthreads();
-    long long rank = a.off[blockIdx.x];
-#pragma unroll 1
+    int rank = 0;  // accepted candidates of this CTA in earlier rounds
+#pragma unroll
     for (int r = 0; r < 4; ++r)
     {
         int before = 0, all = 0;
+#pragma unroll
         for (int w = 0; w < 8; ++w)
         {
             before += w < warp ? wcnt[r][w] : 0;
             all += wcnt[r][w];
         }
-        const bool acc = (bal[r] >> lane) & 1u;
-        const long long j = rank + before + __popc(bal[r] & ((1u << lane) - 1u));
-        rank += all;
-        if (!acc || j >= a.need)
-            continue;
-        const int64_t k = base + r * 256 + t;
-        double x, y, r2;
-        polar_candidate(a.cand[k], x, y, r2);
-        const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log_cr(r2)), r2));
-        const double g1 = __dmul_rn(y, mult), g2 = __dmul_rn(x, mult);
-        const int64_t v = a.v0 + 2 * j;
-        gauss_emit(a.sp, a.mean, a.stddev, a.out, v, g1);
-        if (v + 1 < a.M)
-            gauss_emit(a.sp, a.mean, a.stddev, a.out, v + 1, g2);
-        else
+        if ((bal[r] >> lane) & 1u)
         {
-            a.st->saved = g2;
-            a.st->has_saved = 1;
+            const int q = rank + before + __popc(bal[r] & ((1u << lane) - 1u));
+            sxy[q] = make_double2(xs[r], ys[r]);
+            if (rank0 + q == a.need - 1)
+                a.ctl->consumed = 4 * (base + r * 256 + t + 1);
         }
-        if (j == a.need - 1)
-            a.ctl->consumed = 4 * (k + 1);
+        rank += all;
+    }
+    __syncthreads();
+    const int np = (int)min((long long)rank, a.need - rank0);
+#pragma unroll 1
+    for (int q = t; q < np; q += 256)
+    {
+        const double2 p = sxy[q];
+        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        double lg;
+        if (log_fast(r2, lg))
+            gauss_pair(a, rank0 + q, p.x, p.y, r2, lg);
+        else
+            slow[atomicAdd(&nslow, 1)] = (unsigned short)q;
+    }
+    __syncthreads();
+    const int ns = nslow;
+#pragma unroll 1
+    for (int i = t; i < ns; i += 256)
+    {
+        const int q = slow[i];
+        const double2 p = sxy[q];
+        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        gauss_pair(a, rank0 + q, p.x, p.y, r2, log_cr(r2));
     }
 }
 
@@ -983,6 +1025,21 @@ double measure_fp32_peak(const LaunchCfg &lc)
     cudaEventDestroy(e1);
     cudaFree(sink);
     return best;
+}
+
+__global__ void log_rn_kernel(const double *x, int64_t n, double *out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = log_rn(x[i]);
+}
+
+void launch_log_rn(const LaunchCfg &lc, const double *x, int64_t n, double *out)
+{
+    if (n == 0)
+        return;
+    log_rn_kernel<<<(int)((n + 255) / 256), 256, 0, lc.stream>>>(x, n, out);
+    note_launch();
 }
 
 }  // namespace gbo

@@ -32,6 +32,28 @@ def test_sincos_cr_matches_double_double_oracle(port):
     assert np.array_equal(c.cpu().numpy().view(np.uint64), rc.view(np.uint64))
 
 
+def test_log_rn_matches_oracle(port):
+    """The sampleGaussian log (a plain-FP64 evaluation with a rounding test, the double-double one when
+    that cannot decide) against the oracle's double-double log, which the CPU suite pins against a 200-bit
+    evaluation: bitwise on the polar method's arguments x^2 + y^2, arguments within 2^-53..2^-110 of 1,
+    next to powers of two, and over the whole exponent range."""
+    rng = np.random.default_rng(12)
+    u = rng.random((3_000_000, 2)) * 2 - 1
+    r2 = (u * u).sum(axis=1)
+    r2 = r2[(r2 > 0) & (r2 <= 1)]
+    k = rng.integers(1, 1 << 52, size=200_000).astype(np.float64)
+    sh = rng.integers(53, 110, size=200_000)
+    x = np.concatenate([r2, 1.0 - np.ldexp(k, -sh), 1.0 + np.ldexp(k, -sh),
+                        np.ldexp(1.0 + rng.uniform(-0.3, 0.4, 200_000), -rng.integers(0, 1000, 200_000)),
+                        np.exp(rng.uniform(-700, 700, 200_000)),
+                        [1.0, 0.5, 0.25, 2.0, np.nextafter(1.0, 0.0), np.nextafter(1.0, 2.0), 2.0 ** -1022]])
+    t = torch.as_tensor(x, device="cuda")
+    out = torch.empty_like(t)
+    capi.check(capi.lib().gbo_log_rn(B._ptr(t), len(x), B._ptr(out), B._stream(None)))
+    want = port.log_rn(x)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want.view(np.uint64))
+
+
 def test_glibc_trig_rounding_on_this_host(port):
     """Recorded on the GPU machine's C library (aarch64): how often sin/cos differ from the correctly
     rounded values; always by at most one ulp."""
