@@ -115,11 +115,15 @@ gbo_status mt_jump_table(uint64_t L, int K, const uint32_t **out);
 // sampleGaussian values [v_first, M) of a call; st->has_saved says whether value 0 is the cached one.
 // One chunk of at most cap_words / 4 - 156 polar candidates per host round trip; returns the chunks run
 // or -1 on an error. words: scratch of cap_words words; ctl: device GaussChunk; cnt: scratch of
-// (cap_words / 4096 + 2) long longs.
+// (cap_words / 4096 + 2) long longs; pair / kidx: scratch of gauss_pair_slots(cap_words) entries.
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
-                               int64_t cap_words, GaussChunk *ctl, long long *cnt, unsigned *jump_scratch,
-                               const uint32_t *polys, int64_t L);
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt, double2 *pair,
+                               unsigned short *kidx, unsigned *jump_scratch, const uint32_t *polys, int64_t L);
+inline int64_t gauss_pair_slots(int64_t cap_words)
+{
+    return 1024 * (cap_words / 4096 + 1);
+}
 // log_rn (the sampleGaussian log, rounded to nearest) of n device values, for tests.
 void launch_log_rn(const LaunchCfg &lc, const double *x, int64_t n, double *out);
 double measure_fp32_peak(const LaunchCfg &lc);

@@ -626,24 +626,90 @@ __global__ void gauss_saved_kernel(SamplerState *st, SpaceParams sp, StatesView 
     }
 }
 
-__global__ void __launch_bounds__(256) gauss_count_kernel(const uint4 *cand, int64_t G, long long *cnt)
+// The pairs of CTA b's 1,024 candidates (k = 1024 b .. 1024 b + 1023): its threads rank the accepted
+// candidates in stream order with ballots and keep their (x, y) compacted in shared memory, then
+// evaluate consecutive pairs with no lane idle on a rejected candidate: accepted candidate q of the CTA
+// gives pair[1024 b + q] = (y mult, x mult), mult = sqrt(-2 log(r2) / r2), and kidx[1024 b + q] = its
+// candidate index within the CTA; cnt[b] = the CTA's accepted count. The pairs whose log the plain-FP64
+// evaluation cannot round (about 6 %) are queued and finished after the others by consecutive threads,
+// so that the double-double evaluation runs in a few dense warps instead of in most warps for one
+// lane each. Every candidate's FP64 work is done here once; gauss_emit_kernel places the pairs.
+__global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int64_t G, long long *cnt,
+                                                          double2 *pair, unsigned short *kidx)
 {
+    __shared__ double2 sxy[kGaussPerCta];          // accepted (x, y) by local pair index
+    __shared__ unsigned short slow[kGaussPerCta];  // local pair indices left to log_cr
+    __shared__ int wcnt[4][8];
+    __shared__ int nslow;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0)
+        nslow = 0;
     const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
-    int c = 0;
-#pragma unroll 1
+    double xs[4], ys[4];
+    unsigned bal[4];
+#pragma unroll
     for (int r = 0; r < 4; ++r)
     {
-        const int64_t k = base + r * 256 + threadIdx.x;
-        bool a = false;
+        const int64_t k = base + r * 256 + t;
+        bool acc = false;
+        xs[r] = ys[r] = 0.0;
         if (k < G)
         {
-            double x, y, r2;
-            a = polar_candidate(cand[k], x, y, r2);
+            double r2;
+            acc = polar_candidate(cand[k], xs[r], ys[r], r2);
         }
-        c += __syncthreads_count(a);
+        bal[r] = __ballot_sync(0xffffffffu, acc);
+        if (lane == 0)
+            wcnt[r][warp] = __popc(bal[r]);
     }
-    if (threadIdx.x == 0)
-        cnt[blockIdx.x] = c;
+    __syncthreads();
+    int np = 0;  // accepted candidates of this CTA in earlier rounds
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+    {
+        int before = 0, all = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w)
+        {
+            before += w < warp ? wcnt[r][w] : 0;
+            all += wcnt[r][w];
+        }
+        if ((bal[r] >> lane) & 1u)
+        {
+            const int q = np + before + __popc(bal[r] & ((1u << lane) - 1u));
+            sxy[q] = make_double2(xs[r], ys[r]);
+            kidx[base + q] = (unsigned short)(r * 256 + t);
+        }
+        np += all;
+    }
+    if (t == 0)
+        cnt[blockIdx.x] = np;
+    __syncthreads();
+#pragma unroll 1
+    for (int q = t; q < np; q += 256)
+    {
+        const double2 p = sxy[q];
+        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        double lg;
+        if (log_fast(r2, lg))
+        {
+            const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lg), r2));
+            pair[base + q] = make_double2(__dmul_rn(p.y, mult), __dmul_rn(p.x, mult));
+        }
+        else
+            slow[atomicAdd(&nslow, 1)] = (unsigned short)q;
+    }
+    __syncthreads();
+    const int ns = nslow;
+#pragma unroll 1
+    for (int i = t; i < ns; i += 256)
+    {
+        const int q = slow[i];
+        const double2 p = sxy[q];
+        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log_cr(r2)), r2));
+        pair[base + q] = make_double2(__dmul_rn(p.y, mult), __dmul_rn(p.x, mult));
+    }
 }
 
 // Exclusive scan of the per-CTA counts in place (one CTA of 1024 threads); the total goes to ctl.
@@ -694,12 +760,13 @@ __global__ void __launch_bounds__(1024) gauss_scan_kernel(long long *cnt, int nb
 
 struct GaussArgs
 {
-    const uint4 *cand;      // candidate k = raw words 4k .. 4k+3
-    int64_t G;              // candidates of the chunk
-    const long long *off;   // accepted candidates before each CTA
-    int64_t need;           // pairs the call still needs
-    int64_t v0;             // value index of the chunk's first pair
-    int64_t M;              // values of the call
+    const double2 *pair;         // pairs of each CTA's accepted candidates (gauss_pairs_kernel)
+    const unsigned short *kidx;  // their candidate indices within the CTA
+    const long long *off;        // accepted candidates before each CTA
+    int nb;                      // CTAs of the chunk
+    int64_t need;                // pairs the call still needs
+    int64_t v0;                  // value index of the chunk's first pair
+    int64_t M;                   // values of the call
     double stddev;
     SpaceParams sp;
     StatesView mean;
@@ -708,101 +775,33 @@ struct GaussArgs
     GaussChunk *ctl;
 };
 
-// Pair j from candidate (x, y) with r2 = x^2 + y^2 and lg = log(r2).
-__device__ __forceinline__ void gauss_pair(const GaussArgs &a, int64_t j, double x, double y, double r2, double lg)
+// Accepted candidate j of the chunk (in stream order) becomes pair j: values v0 + 2j and v0 + 2j + 1;
+// the value past the call's end is cached. The words through the last needed candidate are the
+// chunk's consumption.
+__global__ void __launch_bounds__(256) gauss_emit_kernel(const __grid_constant__ GaussArgs a)
 {
-    const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lg), r2));
-    const double g1 = __dmul_rn(y, mult), g2 = __dmul_rn(x, mult);
-    const int64_t v = a.v0 + 2 * j;
-    gauss_emit(a.sp, a.mean, a.stddev, a.out, v, g1);
-    if (v + 1 < a.M)
-        gauss_emit(a.sp, a.mean, a.stddev, a.out, v + 1, g2);
-    else
-    {
-        a.st->saved = g2;
-        a.st->has_saved = 1;
-    }
-}
-
-// Accepted candidate j of the chunk (in stream order) becomes pair j: values v0 + 2j and v0 + 2j + 1.
-// A CTA ranks its candidates' acceptances and stores the accepted (x, y) compacted in stream order, so
-// that its threads then evaluate consecutive pairs with no lane idle on a rejected candidate (and store
-// consecutive values). The pairs whose log the plain-FP64 evaluation cannot round (about 6 %) are queued
-// and finished after the others by consecutive threads, so that the double-double evaluation runs in a
-// few dense warps instead of in most warps for one lane each.
-__global__ void __launch_bounds__(256) gauss_values_kernel(const __grid_constant__ GaussArgs a)
-{
-    __shared__ double2 sxy[kGaussPerCta];          // accepted (x, y) by local pair index
-    __shared__ unsigned short slow[kGaussPerCta];  // local pair indices left to log_cr
-    __shared__ int wcnt[4][8];
-    __shared__ int nslow;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const long long rank0 = a.off[blockIdx.x];
+    const int b = blockIdx.x;
+    const long long rank0 = a.off[b];
     if (rank0 >= a.need)
         return;  // the call's pairs all come from earlier candidates
-    if (t == 0)
-        nslow = 0;
-    const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
-    double xs[4], ys[4];
-    unsigned bal[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-    {
-        const int64_t k = base + r * 256 + t;
-        bool acc = false;
-        xs[r] = ys[r] = 0.0;
-        if (k < a.G)
-        {
-            double r2;
-            acc = polar_candidate(a.cand[k], xs[r], ys[r], r2);
-        }
-        bal[r] = __ballot_sync(0xffffffffu, acc);
-        if (lane == 0)
-            wcnt[r][warp] = __popc(bal[r]);
-    }
-    __syncthreads();
-    int rank = 0;  // accepted candidates of this CTA in earlier rounds
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-    {
-        int before = 0, all = 0;
-#pragma unroll
-        for (int w = 0; w < 8; ++w)
-        {
-            before += w < warp ? wcnt[r][w] : 0;
-            all += wcnt[r][w];
-        }
-        if ((bal[r] >> lane) & 1u)
-        {
-            const int q = rank + before + __popc(bal[r] & ((1u << lane) - 1u));
-            sxy[q] = make_double2(xs[r], ys[r]);
-            if (rank0 + q == a.need - 1)
-                a.ctl->consumed = 4 * (base + r * 256 + t + 1);
-        }
-        rank += all;
-    }
-    __syncthreads();
-    const int np = (int)min((long long)rank, a.need - rank0);
+    const long long next = b + 1 < a.nb ? a.off[b + 1] : a.ctl->accepted;
+    const int np = (int)(min(next, (long long)a.need) - rank0);  // at most 1,024
+    const int64_t base = (int64_t)b * kGaussPerCta;
 #pragma unroll 1
-    for (int q = t; q < np; q += 256)
+    for (int q = threadIdx.x; q < np; q += 256)
     {
-        const double2 p = sxy[q];
-        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
-        double lg;
-        if (log_fast(r2, lg))
-            gauss_pair(a, rank0 + q, p.x, p.y, r2, lg);
+        const double2 g = a.pair[base + q];
+        const int64_t j = rank0 + q, v = a.v0 + 2 * j;
+        gauss_emit(a.sp, a.mean, a.stddev, a.out, v, g.x);
+        if (v + 1 < a.M)
+            gauss_emit(a.sp, a.mean, a.stddev, a.out, v + 1, g.y);
         else
-            slow[atomicAdd(&nslow, 1)] = (unsigned short)q;
-    }
-    __syncthreads();
-    const int ns = nslow;
-#pragma unroll 1
-    for (int i = t; i < ns; i += 256)
-    {
-        const int q = slow[i];
-        const double2 p = sxy[q];
-        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
-        gauss_pair(a, rank0 + q, p.x, p.y, r2, log_cr(r2));
+        {
+            a.st->saved = g.y;
+            a.st->has_saved = 1;
+        }
+        if (j == a.need - 1)
+            a.ctl->consumed = 4 * (base + a.kidx[base + q] + 1);
     }
 }
 
@@ -860,8 +859,8 @@ __global__ void __launch_bounds__(256) gauss_advance_seg_kernel(SamplerState *st
 
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
-                               int64_t cap_words, GaussChunk *ctl, long long *cnt, unsigned *jump_scratch,
-                               const uint32_t *polys, int64_t L)
+                               int64_t cap_words, GaussChunk *ctl, long long *cnt, double2 *pair,
+                               unsigned short *kidx, unsigned *jump_scratch, const uint32_t *polys, int64_t L)
 {
     const int64_t M = n * sp.dim;
     if (M == 0)
@@ -887,10 +886,10 @@ int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_s
             launch_raw_words_jump(lc, st, 4 * G, words, jump_scratch, polys, L);
         else
             mt_words_kernel<true><<<1, 256, 0, lc.stream>>>(st, 4 * G, words);
-        gauss_count_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt);
+        gauss_pairs_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt, pair, kidx);
         gauss_scan_kernel<<<1, 1024, 0, lc.stream>>>(cnt, nb, ctl);
-        GaussArgs a{(const uint4 *)words, G, cnt, need, v, M, stddev, sp, meanv, out, st, ctl};
-        gauss_values_kernel<<<nb, 256, 0, lc.stream>>>(a);
+        GaussArgs a{pair, kidx, cnt, nb, need, v, M, stddev, sp, meanv, out, st, ctl};
+        gauss_emit_kernel<<<nb, 256, 0, lc.stream>>>(a);
         if (seg)
             gauss_advance_seg_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
         else
