@@ -410,12 +410,14 @@ def ours(args, rank, world, local_rank):
     r0 = run(0, capi.SCHEDULE_AUTO)
     timed0 = {k: r0[k].cpu().numpy() for k in ("ok", "first_j", "nd")}
 
-    # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them; two
-    # calls of the same size come first (the jump polynomials of a call size are prepared once per
-    # process on the host, and the sampler's scratch grows once)
+    # sampling on one sampler's stream: 1M uniform states, then 1M Gaussian states around them; calls
+    # of the same sizes come first (the jump polynomials of a call size are prepared once per process
+    # on the host, and the sampler's scratch grows once)
     smp = B.StateSampler(space, 5)
     for _ in range(2):
-        smp.sampleUniform(N_STATES, host=False)
+        warm_means = smp.sampleUniform(N_STATES, host=False)
+    smp.sampleGaussian(warm_means, 0.1)
+    del warm_means
     smp.sampleUniform(1000, host=False)
     smp.sampleGaussian(torch.zeros((1000, w.dim), dtype=torch.float64, device=dev), 0.1)
     torch.cuda.synchronize()

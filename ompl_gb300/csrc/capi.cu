@@ -1407,7 +1407,7 @@ gbo_status gbo_sample_gaussian(gbo_sampler *s, const double *mean, double stddev
     // raw words for the expected candidates plus a margin and one whole block (capped; larger calls
     // run in several chunks)
     const double mu = (double)((M + 1) / 2) / 0.7853981633974483;
-    const int64_t cap = std::min<int64_t>(((int64_t)1 << 24) + 628,
+    const int64_t cap = std::min<int64_t>(((int64_t)1 << 25) + 628,
                                           4 * (int64_t)std::ceil(mu + 8.0 * std::sqrt(mu) + 64.0) + 628);
     cudaStream_t st = (cudaStream_t)stream;
     // large chunks draw their candidates' words on jump-ahead segments (segment length chosen as for

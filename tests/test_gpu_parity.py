@@ -141,12 +141,12 @@ def test_sampler_gaussian_vs_ompl(golden, port, name):
 
 
 def test_sampler_gaussian_across_chunks_vs_oracle(port):
-    """One sampleGaussian call of 7M values (more polar candidates than one chunk of the word scratch
-    holds, so two host rounds), then a uniform call: bitwise against the oracle's polar method with
-    the log rounded to nearest, and the stream position after the call is OMPL's."""
+    """One sampleGaussian call of 14M values (more polar candidates than one chunk of the word scratch,
+    2^25 words, holds, so two host rounds), then a uniform call: bitwise against the oracle's polar
+    method with the log rounded to nearest, and the stream position after the call is OMPL's."""
     d = SpaceDesc(capi.SPACE_REAL_VECTOR, 7, np.full(7, -2.0), np.full(7, 2.0))
     s = gpu_space(d)
-    n = 1_000_001
+    n = 2_000_001
     rng = np.random.default_rng(5)
     mean = rng.uniform(-1.5, 1.5, size=(n + 3, 7))
     ops = [("gaussian", 2), ("gaussian", n), ("gaussian", 1), ("uniform", 9)]
