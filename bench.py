@@ -397,7 +397,7 @@ def ours(args, rank, world, local_rank):
                     "peak": PEAKS.get("hbm_gbs"), "unit": "GB/s",
                     "frac": knn_gbs / PEAKS["hbm_gbs"] if PEAKS.get("hbm_gbs") else None,
                     "work": f"{knn_stats['search_bytes']} bytes: 48 per visited element (links 4..9; the inner "
-                            "links' 32 bytes, read for candidates only, are not counted) and 160 per cell or "
+                            "links' 32 bytes, read for candidates only, are not counted) and 80 per cell or "
                             "chunk box tested",
                     "note": "peak = measured HBM copy bandwidth, but these bytes are served from L2, so the "
                             "fraction can exceed 1; traffic = DRAM bytes of one launch from ncu",

@@ -1697,14 +1697,14 @@ static gbo_status ensure_chain_cells(gbo_nn *nn, const LaunchCfg &lc)
     for (auto r : {c.key.reserve((size_t)n * sizeof(int), s), c.count.reserve(kQueryKeys * sizeof(int), s),
                    c.start.reserve(kQueryKeys * sizeof(int), s), c.fill.reserve(kQueryKeys * sizeof(int), s),
                    c.skey.reserve((size_t)n * sizeof(int64_t), s), c.sfeat.reserve((size_t)n * 5 * sizeof(float4), s),
-                   c.box.reserve((size_t)kQueryKeys * 10 * sizeof(float4), s),
+                   c.box.reserve((size_t)kQueryKeys * 5 * sizeof(uint4), s),
                    c.cstart.reserve((size_t)(kQueryKeys + 1) * sizeof(int), s),
-                   c.cbox.reserve((size_t)(n / 32 + kQueryKeys) * 10 * sizeof(float4), s)})
+                   c.cbox.reserve((size_t)(n / 32 + kQueryKeys) * 5 * sizeof(uint4), s)})
         if (r)
             return r;
     launch_ccell_build(lc, nn_args(nn), nn->sp, (int *)c.key.p, (int *)c.count.p, (int *)c.start.p, (int *)c.fill.p,
-                       (int64_t *)c.skey.p, (float4 *)c.sfeat.p, (float4 *)c.box.p, (int *)c.cstart.p,
-                       (float4 *)c.cbox.p);
+                       (int64_t *)c.skey.p, (float4 *)c.sfeat.p, (uint4 *)c.box.p, (int *)c.cstart.p,
+                       (uint4 *)c.cbox.p);
     CHECK_LAUNCH();
     c.valid = true;
     return GBO_OK;
@@ -1793,8 +1793,8 @@ gbo_status gbo_nn_nearest_k(gbo_nn *nn, const double *q, int64_t nq, int64_t ld,
                     return st;
                 NNChainCells &c = nn->ccells;
                 const ChainCellArgs ci{(const int *)c.start.p,  (const int *)c.count.p, (const int64_t *)c.skey.p,
-                                       (const float4 *)c.sfeat.p, nn->size,  (const float4 *)c.box.p,
-                                       (const int *)c.cstart.p,   (const float4 *)c.cbox.p};
+                                       (const float4 *)c.sfeat.p, nn->size,  (const uint4 *)c.box.p,
+                                       (const int *)c.cstart.p,   (const uint4 *)c.cbox.p};
                 if (launch_knn_ccell(lc, a, ci, nn->sp, qv, (const float *)nn->qfeat.p, nq, ord,
                                      work + 3 * kQueryKeys, k, idx, dist, (unsigned long long *)nn->fb_list.p, fb_n,
                                      ctr, part_d, part_k))

@@ -20,6 +20,8 @@
 //   radius kernels    FP64 count / fill (CSR), sorted by (distance, key).
 #include <climits>
 
+#include <cuda_fp16.h>
+
 #include "kernels_nn.cuh"
 
 namespace gbo
@@ -1390,8 +1392,21 @@ __global__ void ccell_gather_kernel(const int64_t *skey, const int *start, const
     }
 }
 
-// box of cell c: 5 float4 of minima, then 5 of maxima (warp per cell)
-__global__ void ccell_box_kernel(const float4 *sfeat, int64_t fs, const int *start, const int *count, float4 *box)
+// A chain box in 80 bytes: feature f's (minimum, maximum) as a half2 rounded outward (minimum down,
+// maximum up, so that the half box contains the float one and every distance bound computed from it
+// is still a lower bound; values beyond the half range become the largest finite half or infinity on
+// the safe side), features 4j .. 4j+3 in uint4 j.
+__device__ __forceinline__ uint4 pack_box4(float4 lo, float4 hi)
+{
+    auto pk = [](float l, float h) {
+        const __half2 v = __halves2half2(__float2half_rd(l), __float2half_ru(h));
+        return *(const unsigned *)&v;
+    };
+    return make_uint4(pk(lo.x, hi.x), pk(lo.y, hi.y), pk(lo.z, hi.z), pk(lo.w, hi.w));
+}
+
+// box of cell c: five uint4 (pack_box4) (warp per cell)
+__global__ void ccell_box_kernel(const float4 *sfeat, int64_t fs, const int *start, const int *count, uint4 *box)
 {
     const int lane = threadIdx.x & 31;
     for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < kQueryKeys;
@@ -1437,8 +1452,7 @@ __global__ void ccell_box_kernel(const float4 *sfeat, int64_t fs, const int *sta
                     lo = make_float4(m0[4 * j], m0[4 * j + 1], m0[4 * j + 2], m0[4 * j + 3]);
                     hi = make_float4(m1[4 * j], m1[4 * j + 1], m1[4 * j + 2], m1[4 * j + 3]);
                 }
-            box[10 * (int64_t)c + lane] = lo;
-            box[10 * (int64_t)c + 5 + lane] = hi;
+            box[5 * (int64_t)c + lane] = pack_box4(lo, hi);
         }
     }
 }
@@ -1552,10 +1566,9 @@ __global__ void __launch_bounds__(1024) ccell_chunk_scan_kernel(const int *count
         cstart[kQueryKeys] = part[1023];
 }
 
-// box of each chunk (warp per chunk, lane per element): 5 float4 of minima, then 5 of maxima
+// box of each chunk (warp per chunk, lane per element): five uint4 (pack_box4)
 __global__ void ccell_chunk_box_kernel(const float4 *sfeat, int64_t fs, const int *start, const int *count,
-                                       const int *cstart,
-                                       float4 *cbox)
+                                       const int *cstart, uint4 *cbox)
 {
     const int lane = threadIdx.x & 31;
     const int nchunks = cstart[kQueryKeys];
@@ -1600,22 +1613,23 @@ __global__ void ccell_chunk_box_kernel(const float4 *sfeat, int64_t fs, const in
                 mx[f] = fmaxf(mx[f], __shfl_xor_sync(0xffffffffu, mx[f], o));
             }
         }
-        if (lane < 10)
+        if (lane < 5)
         {
-            const float *m = lane < 5 ? mn : mx;
-            const int j = lane < 5 ? lane : lane - 5;
-            float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
 #pragma unroll
-            for (int jj = 0; jj < 5; ++jj)
-                if (jj == j)
-                    out = make_float4(m[4 * jj], m[4 * jj + 1], m[4 * jj + 2], m[4 * jj + 3]);
-            cbox[10 * (int64_t)ch + lane] = out;
+            for (int j = 0; j < 5; ++j)
+                if (j == lane)
+                {
+                    lo = make_float4(mn[4 * j], mn[4 * j + 1], mn[4 * j + 2], mn[4 * j + 3]);
+                    hi = make_float4(mx[4 * j], mx[4 * j + 1], mx[4 * j + 2], mx[4 * j + 3]);
+                }
+            cbox[5 * (int64_t)ch + lane] = pack_box4(lo, hi);
         }
     }
 }
 
 void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int *key, int *count,
-                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box, int *cstart, float4 *cbox)
+                        int *start, int *fill, int64_t *skey, float4 *sfeat, uint4 *box, int *cstart, uint4 *cbox)
 {
     const int grid = grid_for(lc, nn.size);
     cudaMemsetAsync(count, 0, kQueryKeys * sizeof(int), lc.stream);
@@ -1634,23 +1648,26 @@ void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams
         note_launch();
 }
 
-// chain distance from query features q to the box of a cell (before the scale by the link length)
-__device__ __forceinline__ float ccell_lb(const float4 *b, const float *q, int dim)
+// chain distance from query features q to a cell's or chunk's box (pack_box4 layout), before the scale by
+// the link length
+__device__ __forceinline__ float ccell_lb(const uint4 *b, const float *q, int dim)
 {
     float s = 0.f;
 #pragma unroll
     for (int j = 0; j < 5; ++j)
     {
-        const float4 lo = b[j], hi = b[5 + j];
-        const float l[4] = {lo.x, lo.y, lo.z, lo.w}, h[4] = {hi.x, hi.y, hi.z, hi.w};
+        const uint4 w = b[j];
+        const unsigned u[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
         for (int t = 0; t < 4; t += 2)
         {
             const int i = (4 * j + t) / 2;  // link
             if (i < dim)
             {
-                const float dx = fmaxf(fmaxf(l[t] - q[4 * j + t], q[4 * j + t] - h[t]), 0.f);
-                const float dy = fmaxf(fmaxf(l[t + 1] - q[4 * j + t + 1], q[4 * j + t + 1] - h[t + 1]), 0.f);
+                const float2 bx = __half22float2(*(const __half2 *)&u[t]);      // (min, max) of x
+                const float2 by = __half22float2(*(const __half2 *)&u[t + 1]);  // (min, max) of y
+                const float dx = fmaxf(fmaxf(bx.x - q[4 * j + t], q[4 * j + t] - bx.y), 0.f);
+                const float dy = fmaxf(fmaxf(by.x - q[4 * j + t + 1], q[4 * j + t + 1] - by.y), 0.f);
                 s += sqrt_approx(fmaf(dx, dx, dy * dy));
             }
         }
@@ -1754,8 +1771,8 @@ __global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci
             const int ch = cb + lane;
             float lb = __int_as_float(0x7f800000);
             if (ch < c1)
-                lb = ccell_lb(ci.cbox + 10 * (int64_t)ch, qfe, sp.dim) * link * (1.0f - 1e-5f);
-            nbytes += 160ull * (unsigned)min(32, c1 - cb);
+                lb = ccell_lb(ci.cbox + 5 * (int64_t)ch, qfe, sp.dim) * link * (1.0f - 1e-5f);
+            nbytes += 80ull * (unsigned)min(32, c1 - cb);
             unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
             while (m)
             {
@@ -1795,8 +1812,8 @@ __global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci
     auto visit = [&](int c, bool ok) {
         float lb = __int_as_float(0x7f800000);
         if (ok && ci.count[c] > 0)
-            lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
-        nbytes += 160ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
+            lb = ccell_lb(ci.box + 5 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        nbytes += 80ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
         unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
         {
@@ -1830,8 +1847,8 @@ __global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci
         const int c = cb + lane;
         float lb = __int_as_float(0x7f800000);
         if (!near_own(c) && ci.count[c] > 0)
-            lb = ccell_lb(ci.box + 10 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
-        nbytes += 160ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
+            lb = ccell_lb(ci.box + 5 * (int64_t)c, qfe, sp.dim) * link * (1.0f - 1e-5f);
+        nbytes += 80ull * __popc(__ballot_sync(0xffffffffu, lb < __int_as_float(0x7f800000)));
         unsigned m = __ballot_sync(0xffffffffu, lb < fminf(T, L.last()));
         while (m)
         {

@@ -59,14 +59,14 @@ struct ChainCellArgs
     const int64_t *skey;   // element key at each sorted position
     const float4 *sfeat;   // five planes of float4 (features 4j..4j+3 of each sorted position in plane j)
     int64_t fs;            // plane stride (float4 units)
-    const float4 *box;     // ten float4 per cell: 20 minima, then 20 maxima
+    const uint4 *box;      // five uint4 per cell: feature f's (minimum, maximum) as a half2 rounded outward
     const int *cstart;     // [kQueryKeys + 1] first chunk of each cell (chunks of 32 sorted positions)
-    const float4 *cbox;    // ten float4 per chunk, as box
+    const uint4 *cbox;     // five uint4 per chunk, as box
 };
-// key: [size] ints; count / start / fill: [kQueryKeys] ints; skey: [size]; sfeat: 5 planes of [size]; box: [10 * kQueryKeys];
-// cstart: [kQueryKeys + 1]; cbox: [10 * (size / 32 + kQueryKeys)]
+// key: [size] ints; count / start / fill: [kQueryKeys] ints; skey: [size]; sfeat: 5 planes of [size]; box: [5 * kQueryKeys];
+// cstart: [kQueryKeys + 1]; cbox: [5 * (size / 32 + kQueryKeys)]
 void launch_ccell_build(const LaunchCfg &lc, const NNArgs &nn, const SpaceParams &sp, int *key, int *count,
-                        int *start, int *fill, int64_t *skey, float4 *sfeat, float4 *box, int *cstart, float4 *cbox);
+                        int *start, int *fill, int64_t *skey, float4 *sfeat, uint4 *box, int *cstart, uint4 *cbox);
 // qorder / qkey: the query order and each query's key (launch_query_order's order and key arrays).
 // Returns true when launched (lists for every query, P = 1, and the finish kernel).
 bool launch_knn_ccell(const LaunchCfg &lc, const NNArgs &nn, const ChainCellArgs &ci, const SpaceParams &sp,
