@@ -583,12 +583,23 @@ static void launch_raw_words_jump(const LaunchCfg &lc, const SamplerState *st, i
 // the ones the call needs and then commits exactly the words used (gauss_advance_kernel).
 constexpr int kGaussPerCta = 1024;  // candidates per CTA: 256 threads x 4
 
+// 2U - 1 rounded to nearest for a generate_canonical value U in [0, 1): 2U by the exponent (exact; U is
+// 0 or at least 2^-64), then one FP64 subtraction.
+__device__ __forceinline__ double two_u_minus_1(double U)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(U);
+    return __dsub_rn(__longlong_as_double((long long)(b ? b + (1ull << 52) : 0ull)), 1.0);
+}
+
+// The polar method's candidate from four stream words: generate_canonical in integer arithmetic (the
+// same doubles as canonical53), and the rejection test r2 > 1 || r2 == 0 on the bits (r2 >= +0).
 __device__ __forceinline__ bool polar_candidate(uint4 w, double &x, double &y, double &r2)
 {
-    x = __dsub_rn(__dmul_rn(2.0, canonical53(temper(w.x), temper(w.y))), 1.0);
-    y = __dsub_rn(__dmul_rn(2.0, canonical53(temper(w.z), temper(w.w))), 1.0);
+    x = two_u_minus_1(canonical53_int(temper(w.x), temper(w.y)));
+    y = two_u_minus_1(canonical53_int(temper(w.z), temper(w.w)));
     r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
-    return !(r2 > 1.0 || r2 == 0.0);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(r2);
+    return rb != 0ull && rb <= 0x3FF0000000000000ull;
 }
 
 // Value v of the call (coordinate v % dim of state v / dim) from a standard normal value g:
@@ -638,6 +649,7 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
                                                           double2 *pair, unsigned short *kidx)
 {
     __shared__ double2 sxy[kGaussPerCta];          // accepted (x, y) by local pair index
+    __shared__ double sr2[kGaussPerCta];           // and their x^2 + y^2
     __shared__ unsigned short slow[kGaussPerCta];  // local pair indices left to log_cr
     __shared__ int wcnt[4][8];
     __shared__ int nslow;
@@ -645,19 +657,16 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
     if (t == 0)
         nslow = 0;
     const int64_t base = (int64_t)blockIdx.x * kGaussPerCta;
-    double xs[4], ys[4];
+    double xs[4], ys[4], rs[4];
     unsigned bal[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
     {
         const int64_t k = base + r * 256 + t;
         bool acc = false;
-        xs[r] = ys[r] = 0.0;
+        xs[r] = ys[r] = rs[r] = 0.0;
         if (k < G)
-        {
-            double r2;
-            acc = polar_candidate(cand[k], xs[r], ys[r], r2);
-        }
+            acc = polar_candidate(cand[k], xs[r], ys[r], rs[r]);
         bal[r] = __ballot_sync(0xffffffffu, acc);
         if (lane == 0)
             wcnt[r][warp] = __popc(bal[r]);
@@ -678,6 +687,7 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
         {
             const int q = np + before + __popc(bal[r] & ((1u << lane) - 1u));
             sxy[q] = make_double2(xs[r], ys[r]);
+            sr2[q] = rs[r];
             kidx[base + q] = (unsigned short)(r * 256 + t);
         }
         np += all;
@@ -689,7 +699,7 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
     for (int q = t; q < np; q += 256)
     {
         const double2 p = sxy[q];
-        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        const double r2 = sr2[q];
         double lg;
         if (log_fast(r2, lg))
         {
@@ -706,7 +716,7 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
     {
         const int q = slow[i];
         const double2 p = sxy[q];
-        const double r2 = __dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y));
+        const double r2 = sr2[q];
         const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log_cr(r2)), r2));
         pair[base + q] = make_double2(__dmul_rn(p.y, mult), __dmul_rn(p.x, mult));
     }
