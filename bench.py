@@ -477,10 +477,11 @@ def ours(args, rank, world, local_rank):
     ref_idx, ref_dist = port.knn(sd, w.states, w.states[qi[pq]], 16)
     knn_agree = (ref_idx == knn_idx[pq]).all(axis=1) & \
         np.all(np.abs(ref_dist - knn_dist500) <= 1e-12 * np.maximum(np.abs(ref_dist), np.abs(knn_dist500)), axis=1)
-    # the timed uniform call, every value, against the oracle's sequential stream (same calls before it)
-    ref_s = port.sample_script(sd, 5, [("uniform", N_STATES), ("uniform", N_STATES), ("uniform", 1000),
-                                       ("gaussian", 1000), ("uniform", N_STATES)],
-                               mean=np.zeros((1000, w.dim)), stddev=0.1)[-N_STATES:]
+    # the timed uniform call, every value, against the oracle's sequential stream (same calls before it;
+    # the Gaussian calls' stream consumption does not depend on their means)
+    ref_s = port.sample_script(sd, 5, [("uniform", N_STATES), ("uniform", N_STATES), ("gaussian", N_STATES),
+                                       ("uniform", 1000), ("gaussian", 1000), ("uniform", N_STATES)],
+                               mean=np.zeros((N_STATES + 1000, w.dim)), stddev=0.1)[-N_STATES:]
     sampling["parity"] = {"values_checked": int(ref_s.size),
                           "values_agree": int((ref_s.view(np.uint64) == sampled_host.view(np.uint64)).sum()),
                           "compared": "every coordinate of the timed sampleUniform call, bitwise, against the "
@@ -535,7 +536,28 @@ def ours(args, rank, world, local_rank):
         del dev_batches, pin_in, states_soa, nn
         torch.cuda.empty_cache()
         out["workloads"] = other_workloads(port)
+    bad = parity_shortfalls(out)
+    if bad:
+        print("bench: parity shortfall in " + ", ".join(bad), file=sys.stderr)
     print(json.dumps(out))
+
+
+def parity_shortfalls(obj, path=""):
+    """Paths of the parity objects in the bench line whose agreement count is below their checked count."""
+    bad = []
+    if isinstance(obj, dict):
+        for key, val in obj.items():
+            sub = f"{path}/{key}"
+            if isinstance(val, dict) and key in ("parity", "alone_equals_mix"):
+                for ck, cv in val.items():
+                    if ck.endswith("_checked"):
+                        agree = val.get(ck[: -len("_checked")] + "_agree", val.get(ck[: -len("_checked")] + "_same"))
+                        if agree is not None and agree < cv:
+                            bad.append(f"{sub}/{ck}")
+                if val.get("digest_match") is False:
+                    bad.append(f"{sub}/digest_match")
+            bad += parity_shortfalls(val, sub)
+    return bad
 
 
 def profile(kind):
