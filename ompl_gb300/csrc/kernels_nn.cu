@@ -1696,70 +1696,100 @@ __global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci
     WarpList<K_KEEP> L;
     L.init();
     unsigned long long nbytes = 0;  // feature and box bytes read for this query (lane 0)
-    // the elements of one chunk (positions p0 .. s1 - 1, at most 32), one lane each
-    auto scan_chunk = [&](int p0, int s1, float T) {
+    // Elements whose outer-link partial passes wait in a per-warp ring of 64 (position and partial) until
+    // 32 are queued (or the cell ends); their inner links are then read and summed one element per lane,
+    // so that this stage runs with full warps instead of for the few passing lanes of every chunk. A
+    // queued element is tested again against the list and T of the moment, which only lie lower.
+    __shared__ int wq_pos[8][64];
+    __shared__ float wq_outer[8][64];
+    int *qp = wq_pos[threadIdx.x >> 5];
+    float *qo = wq_outer[threadIdx.x >> 5];
+    int qhead = 0, qn = 0;  // warp-uniform
+    auto flush = [&](int cnt, float T) {
+        __syncwarp();  // the queued entries are written
+        const int slot = (qhead + lane) & 63;
+        const int p = lane < cnt ? qp[slot] : 0;
+        const float outer = lane < cnt ? qo[slot] : 0.f;
+        __syncwarp();  // and read before later chunks reuse their slots
+        qhead += cnt;
+        qn -= cnt;
+        float d = __int_as_float(0x7f800000);
+        int key = -1;
+        const float last = L.last();
+        if (lane < cnt && outer * link < last && outer * link <= T)
         {
-            const int p = p0 + lane;
-            float d = __int_as_float(0x7f800000);
-            int key = -1;
-            const float last = L.last();
-            if (p < s1)
+            float pf[8];
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
             {
-                // links 4.. first (features 8-19): their terms are the largest; the rest (features 0-7)
-                // is read only when the element can still enter the list. Terms are non-negative and
-                // FP32 addition is monotone, so the full sum is at least the partial one.
-                float pf[20];
-#pragma unroll
-                for (int j = 2; j < 5; ++j)
-                {
-                    const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
-                    pf[4 * j] = a.x;
-                    pf[4 * j + 1] = a.y;
-                    pf[4 * j + 2] = a.z;
-                    pf[4 * j + 3] = a.w;
-                }
-                float outer = 0.f;
-#pragma unroll
-                for (int i = 4; i < 10; ++i)
-                    if (i < sp.dim)
-                    {
-                        const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
-                        outer += sqrt_approx(fmaf(dx, dx, dy * dy));
-                    }
-                if (outer * link < last && outer * link <= T)
-                {
-#pragma unroll
-                    for (int j = 0; j < 2; ++j)
-                    {
-                        const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
-                        pf[4 * j] = a.x;
-                        pf[4 * j + 1] = a.y;
-                        pf[4 * j + 2] = a.z;
-                        pf[4 * j + 3] = a.w;
-                    }
-                    float inner = 0.f;
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        if (i < sp.dim)
-                        {
-                            const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
-                            inner += sqrt_approx(fmaf(dx, dx, dy * dy));
-                        }
-                    d = (inner + outer) * link;
-                    key = (int)ci.skey[p];
-                }
+                const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
+                pf[4 * j] = a.x;
+                pf[4 * j + 1] = a.y;
+                pf[4 * j + 2] = a.z;
+                pf[4 * j + 3] = a.w;
             }
-            unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
-            while (m)
-            {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const float dc = __shfl_sync(0xffffffffu, d, src);
-                const int kc = __shfl_sync(0xffffffffu, key, src);
-                if (dc < L.last())
-                    L.insert(dc, kc, lane);
-            }
+            float inner = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i < sp.dim)
+                {
+                    const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
+                    inner += sqrt_approx(fmaf(dx, dx, dy * dy));
+                }
+            d = (inner + outer) * link;
+            key = (int)ci.skey[p];
         }
+        unsigned m = __ballot_sync(0xffffffffu, d < last && d <= T);
+        while (m)
+        {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const float dc = __shfl_sync(0xffffffffu, d, src);
+            const int kc = __shfl_sync(0xffffffffu, key, src);
+            if (dc < L.last())
+                L.insert(dc, kc, lane);
+        }
+    };
+    // the elements of one chunk (positions p0 .. s1 - 1, at most 32), one lane each: links 4.. first
+    // (features 8-19), whose terms are the largest; the rest (features 0-7) is read only when the element
+    // can still enter the list (flush). Terms are non-negative and FP32 addition is monotone, so the full
+    // sum is at least the partial one.
+    auto scan_chunk = [&](int p0, int s1, float T) {
+        const int p = p0 + lane;
+        const float last = L.last();
+        float outer = 0.f;
+        bool pass = false;
+        if (p < s1)
+        {
+            float pf[20];
+#pragma unroll
+            for (int j = 2; j < 5; ++j)
+            {
+                const float4 a = ci.sfeat[(int64_t)j * ci.fs + p];
+                pf[4 * j] = a.x;
+                pf[4 * j + 1] = a.y;
+                pf[4 * j + 2] = a.z;
+                pf[4 * j + 3] = a.w;
+            }
+#pragma unroll
+            for (int i = 4; i < 10; ++i)
+                if (i < sp.dim)
+                {
+                    const float dx = pf[2 * i] - qfe[2 * i], dy = pf[2 * i + 1] - qfe[2 * i + 1];
+                    outer += sqrt_approx(fmaf(dx, dx, dy * dy));
+                }
+            pass = outer * link < last && outer * link <= T;
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, pass);
+        if (pass)
+        {
+            const int slot = (qhead + qn + __popc(pm & ((1u << lane) - 1u))) & 63;
+            qp[slot] = p;
+            qo[slot] = outer;
+        }
+        qn += __popc(pm);
+        if (qn >= 32)
+            flush(32, T);
     };
     // a cell: its chunks' boxes (lanes over chunks), then the elements of the chunks whose bound is below
     // min(T, the list's last entry), rechecked against the bound of the moment
@@ -1786,6 +1816,8 @@ __global__ void __launch_bounds__(256, 3) knn_ccell_warp_kernel(ChainCellArgs ci
                 }
             }
         }
+        if (qn > 0)
+            flush(qn, T);
     };
     const int own = qkey[qi];
     scan_cell(own, __int_as_float(0x7f800000));
