@@ -4,9 +4,11 @@
 // The stream is OMPL's RNG (RandomNumbers.h:66-76): std::mt19937 -> libstdc++
 // generate_canonical<double, 53> (two 32-bit draws w0, w1: (w0 + w1 * 2^32) / 2^64, values >= 1
 // replaced by the largest double below 1) -> uniformReal(lo, hi) = (hi - lo) * U + lo.
-// mt19937 (Matsumoto & Nishimura 1998) is sequential across 624-word blocks, so one CTA produces a
-// sampler's word stream (mt_words_kernel) and the whole GPU converts word pairs into coordinates
-// (words_to_states_kernel); large calls alternate the two over chunks of the stream.
+// mt19937 (Matsumoto & Nishimura 1998) is sequential across 624-word blocks. Calls of fewer than 2^18
+// stream words run on one CTA that produces the sampler's word stream (mt_words_kernel) while the
+// whole GPU converts word pairs into coordinates (words_to_states_kernel); larger calls cut their
+// stretch of the stream into segments that start from jump-ahead windows and run side by side (below).
+// sampleGaussian (further below) draws its polar candidates' words the same two ways.
 #include <algorithm>
 #include <cmath>
 
@@ -579,8 +581,9 @@ static void launch_raw_words_jump(const LaunchCfg &lc, const SamplerState *st, i
 // fraction of arguments, and only the values of those pairs differ (by an ulp or two).
 //
 // Stream consumption is data dependent, so a chunk draws a bounded surplus of candidates
-// speculatively (raw words, generator unchanged), ranks the accepted ones across the GPU, converts
-// the ones the call needs and then commits exactly the words used (gauss_advance_kernel).
+// speculatively (raw words, generator unchanged), evaluates every accepted candidate's pair once
+// (gauss_pairs_kernel), ranks the CTAs' counts (gauss_scan_kernel), places the pairs the call needs
+// (gauss_emit_kernel) and then commits exactly the words used (gauss_advance[_seg]_kernel).
 constexpr int kGaussPerCta = 1024;  // candidates per CTA: 256 threads x 4
 
 // 2U - 1 rounded to nearest for a generate_canonical value U in [0, 1): 2U by the exponent (exact; U is
