@@ -645,7 +645,7 @@ __global__ void gauss_saved_kernel(SamplerState *st, SpaceParams sp, StatesView 
 // evaluate consecutive pairs with no lane idle on a rejected candidate: accepted candidate q of the CTA
 // gives pair[1024 b + q] = (y mult, x mult), mult = sqrt(-2 log(r2) / r2), and kidx[1024 b + q] = its
 // candidate index within the CTA; cnt[b] = the CTA's accepted count. The pairs whose log the plain-FP64
-// evaluation cannot round (about 6 %) are queued and finished after the others by consecutive threads,
+// evaluation cannot round (about 3 %) are queued and finished after the others by consecutive threads,
 // so that the double-double evaluation runs in a few dense warps instead of in most warps for one
 // lane each. Every candidate's FP64 work is done here once; gauss_emit_kernel places the pairs.
 __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int64_t G, long long *cnt,
