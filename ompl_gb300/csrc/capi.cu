@@ -1434,14 +1434,16 @@ gbo_status gbo_sample_gaussian(gbo_sampler *s, const double *mean, double stddev
         return e;
     const size_t cnt_bytes = pad16(sizeof(GaussChunk) + sizeof(long long) * (size_t)(cap / 4096 + 2));
     const size_t slots = (size_t)gauss_pair_slots(cap);
-    if (auto e = s->gwork.reserve(cnt_bytes + slots * (sizeof(double2) + sizeof(unsigned short)), st))
+    if (auto e = s->gwork.reserve(cnt_bytes + slots * (sizeof(double2) + sizeof(unsigned short) + 2 * sizeof(unsigned)),
+                                  st))
         return e;
     double2 *pair = (double2 *)((char *)s->gwork.p + cnt_bytes);
     const StatesView ov = make_view(out, ld, layout);
     const int64_t chunks = launch_sample_gaussian(
         lcfg(st), s->st, s->has_saved, s->sp, make_view(mean, ld, layout), stddev, n, MutStatesView{out, ov.si, ov.sd},
         (unsigned *)s->words.p, cap, (GaussChunk *)s->gwork.p, (long long *)((char *)s->gwork.p + sizeof(GaussChunk)),
-        pair, (unsigned short *)(pair + slots), polys ? (unsigned *)s->words.p + cap_al : nullptr, polys, L);
+        pair, (unsigned short *)(pair + slots), (unsigned *)((unsigned short *)(pair + slots) + slots),
+        polys ? (unsigned *)s->words.p + cap_al : nullptr, polys, L);
     if (chunks < 0)
         return fail(GBO_ERR_CUDA, std::string("sampleGaussian: ") + cudaGetErrorString(cudaGetLastError()));
     CHECK_LAUNCH();

@@ -99,6 +99,8 @@ struct GaussChunk
 {
     long long accepted;  // accepted candidates of the chunk
     long long consumed;  // stream words used: through the last needed accepted candidate, else all
+    long long slow;      // pairs log_fast leaves (gauss_slow_kernel)
+    long long slow_cr;   // pairs log_med leaves too (gauss_cr_kernel)
 };
 // words: scratch of cap_words (even, >= 2) 32-bit words; calls above cap_words / 2 values run in chunks
 void launch_sample_uniform(const LaunchCfg &lc, SamplerState *st, const SpaceParams &sp, const double *near,
@@ -115,11 +117,13 @@ gbo_status mt_jump_table(uint64_t L, int K, const uint32_t **out);
 // sampleGaussian values [v_first, M) of a call; st->has_saved says whether value 0 is the cached one.
 // One chunk of at most cap_words / 4 - 156 polar candidates per host round trip; returns the chunks run
 // or -1 on an error. words: scratch of cap_words words; ctl: device GaussChunk; cnt: scratch of
-// (cap_words / 4096 + 2) long longs; pair / kidx: scratch of gauss_pair_slots(cap_words) entries.
+// (cap_words / 4096 + 2) long longs; pair / kidx: scratch of gauss_pair_slots(cap_words) entries; slowlist:
+// twice that (the pairs log_fast leaves, then those log_med leaves).
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
                                int64_t cap_words, GaussChunk *ctl, long long *cnt, double2 *pair,
-                               unsigned short *kidx, unsigned *jump_scratch, const uint32_t *polys, int64_t L);
+                               unsigned short *kidx, unsigned *slowlist, unsigned *jump_scratch,
+                               const uint32_t *polys, int64_t L);
 inline int64_t gauss_pair_slots(int64_t cap_words)
 {
     return 1024 * (cap_words / 4096 + 1);

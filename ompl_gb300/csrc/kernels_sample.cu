@@ -645,17 +645,20 @@ __global__ void gauss_saved_kernel(SamplerState *st, SpaceParams sp, StatesView 
 // evaluate consecutive pairs with no lane idle on a rejected candidate: accepted candidate q of the CTA
 // gives pair[1024 b + q] = (y mult, x mult), mult = sqrt(-2 log(r2) / r2), and kidx[1024 b + q] = its
 // candidate index within the CTA; cnt[b] = the CTA's accepted count. The pairs whose log the plain-FP64
-// evaluation cannot round (about 3 %) are queued and finished after the others by consecutive threads,
-// so that the double-double evaluation runs in a few dense warps instead of in most warps for one
-// lane each. Every candidate's FP64 work is done here once; gauss_emit_kernel places the pairs.
+// evaluation cannot round (about 3 %) are listed (b << 10 | q, one global atomic per CTA) for
+// gauss_slow_kernel, which runs the double-double evaluation for all of them across the GPU; done here
+// at the end of each CTA, it held the CTA's other warps in a long serial tail. gauss_emit_kernel places
+// the pairs.
 __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int64_t G, long long *cnt,
-                                                          double2 *pair, unsigned short *kidx)
+                                                          double2 *pair, unsigned short *kidx, unsigned *slowlist,
+                                                          GaussChunk *ctl)
 {
     __shared__ double2 sxy[kGaussPerCta];          // accepted (x, y) by local pair index
     __shared__ double sr2[kGaussPerCta];           // and their x^2 + y^2
     __shared__ unsigned short slow[kGaussPerCta];  // local pair indices left to log_cr
     __shared__ int wcnt[4][8];
     __shared__ int nslow;
+    __shared__ long long slow0;  // this CTA's first entry in slowlist
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0)
         nslow = 0;
@@ -714,15 +717,58 @@ __global__ void __launch_bounds__(256) gauss_pairs_kernel(const uint4 *cand, int
     }
     __syncthreads();
     const int ns = nslow;
-#pragma unroll 1
+    if (ns == 0)
+        return;
+    if (t == 0)
+        slow0 = atomicAdd((unsigned long long *)&ctl->slow, (unsigned long long)ns);
+    __syncthreads();
     for (int i = t; i < ns; i += 256)
+        slowlist[slow0 + i] = (unsigned)blockIdx.x << 10 | slow[i];
+}
+
+// Pair v = b << 10 | q of the chunk from its candidate (formed again from its words) and lg = log(r2).
+__device__ __forceinline__ void gauss_listed_pair(const uint4 *cand, const unsigned short *kidx, double2 *pair,
+                                                  unsigned v, bool cr, unsigned *crlist, GaussChunk *ctl)
+{
+    const int64_t base = (int64_t)(v >> 10) * kGaussPerCta;
+    const int q = (int)(v & 1023u);
+    double x, y, r2, lg;
+    polar_candidate(cand[base + kidx[base + q]], x, y, r2);
+    if (cr)
+        lg = log_cr(r2);
+    else if (!log_med(r2, lg))
     {
-        const int q = slow[i];
-        const double2 p = sxy[q];
-        const double r2 = sr2[q];
-        const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log_cr(r2)), r2));
-        pair[base + q] = make_double2(__dmul_rn(p.y, mult), __dmul_rn(p.x, mult));
+        // left to gauss_cr_kernel (about 2 % of the list): one atomic per warp
+        const unsigned act = __activemask(), lane = threadIdx.x & 31u;
+        const unsigned lead = __ffs(act) - 1;
+        unsigned long long at = 0;
+        if (lane == lead)
+            at = atomicAdd((unsigned long long *)&ctl->slow_cr, (unsigned long long)__popc(act));
+        at = __shfl_sync(act, at, lead);
+        crlist[at + __popc(act & ((1u << lane) - 1u))] = v;
+        return;
     }
+    const double mult = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, lg), r2));
+    pair[base + q] = make_double2(__dmul_rn(y, mult), __dmul_rn(x, mult));
+}
+
+// The pairs gauss_pairs_kernel listed, with log_med; those it cannot round go to crlist.
+__global__ void __launch_bounds__(256) gauss_slow_kernel(const uint4 *cand, const unsigned short *kidx,
+                                                         const unsigned *slowlist, unsigned *crlist,
+                                                         GaussChunk *ctl, double2 *pair)
+{
+    const long long n = ctl->slow;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        gauss_listed_pair(cand, kidx, pair, slowlist[e], false, crlist, ctl);
+}
+
+// The pairs gauss_slow_kernel left, with log_cr.
+__global__ void __launch_bounds__(256) gauss_cr_kernel(const uint4 *cand, const unsigned short *kidx,
+                                                       const unsigned *crlist, GaussChunk *ctl, double2 *pair)
+{
+    const long long n = ctl->slow_cr;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        gauss_listed_pair(cand, kidx, pair, crlist[e], true, nullptr, ctl);
 }
 
 // Exclusive scan of the per-CTA counts in place (one CTA of 1024 threads); the total goes to ctl.
@@ -873,7 +919,8 @@ __global__ void __launch_bounds__(256) gauss_advance_seg_kernel(SamplerState *st
 int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_saved, const SpaceParams &sp,
                                StatesView meanv, double stddev, int64_t n, MutStatesView out, unsigned *words,
                                int64_t cap_words, GaussChunk *ctl, long long *cnt, double2 *pair,
-                               unsigned short *kidx, unsigned *jump_scratch, const uint32_t *polys, int64_t L)
+                               unsigned short *kidx, unsigned *slowlist, unsigned *jump_scratch,
+                               const uint32_t *polys, int64_t L)
 {
     const int64_t M = n * sp.dim;
     if (M == 0)
@@ -899,7 +946,12 @@ int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_s
             launch_raw_words_jump(lc, st, 4 * G, words, jump_scratch, polys, L);
         else
             mt_words_kernel<true><<<1, 256, 0, lc.stream>>>(st, 4 * G, words);
-        gauss_pairs_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt, pair, kidx);
+        cudaMemsetAsync(&ctl->slow, 0, 2 * sizeof(long long), lc.stream);  // slow and slow_cr
+        unsigned *crlist = slowlist + gauss_pair_slots(cap_words);
+        gauss_pairs_kernel<<<nb, 256, 0, lc.stream>>>((const uint4 *)words, G, cnt, pair, kidx, slowlist, ctl);
+        gauss_slow_kernel<<<lc.sm_count * 8, 256, 0, lc.stream>>>((const uint4 *)words, kidx, slowlist, crlist, ctl,
+                                                                  pair);
+        gauss_cr_kernel<<<lc.sm_count, 256, 0, lc.stream>>>((const uint4 *)words, kidx, crlist, ctl, pair);
         gauss_scan_kernel<<<1, 1024, 0, lc.stream>>>(cnt, nb, ctl);
         GaussArgs a{pair, kidx, cnt, nb, need, v, M, stddev, sp, meanv, out, st, ctl};
         gauss_emit_kernel<<<nb, 256, 0, lc.stream>>>(a);
@@ -907,7 +959,7 @@ int64_t launch_sample_gaussian(const LaunchCfg &lc, SamplerState *st, bool has_s
             gauss_advance_seg_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
         else
             gauss_advance_kernel<<<1, 256, 0, lc.stream>>>(st, words, 4 * G, ctl);
-        for (int i = 0; i < 5; ++i)
+        for (int i = 0; i < 7; ++i)
             note_launch();
         GaussChunk h{};
         if (cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, lc.stream) != cudaSuccess ||
