@@ -605,14 +605,28 @@ __device__ __forceinline__ bool polar_candidate(uint4 w, double &x, double &y, d
     return rb != 0ull && rb <= 0x3FF0000000000000ull;
 }
 
+// a < b for doubles as IEEE compares them, on the integer pipe (the FP64 pipe is this kernel's bound):
+// false when either is NaN or both are zeros, else the order of the sign-magnitude bit patterns.
+__device__ __forceinline__ bool dlt_bits(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const unsigned long long ma = (unsigned long long)ia & 0x7fffffffffffffffull;
+    const unsigned long long mb = (unsigned long long)ib & 0x7fffffffffffffffull;
+    if (ma > 0x7ff0000000000000ull || mb > 0x7ff0000000000000ull || (ma | mb) == 0ull)
+        return false;
+    return (ia ^ ((ia >> 63) & 0x7fffffffffffffffll)) < (ib ^ ((ib >> 63) & 0x7fffffffffffffffll));
+}
+
 // Value v of the call (coordinate v % dim of state v / dim) from a standard normal value g:
-// normal_distribution's g * 1 + 0 (which turns -0 into +0), then * stdDev + mean and the bounds.
+// normal_distribution's g * 1 + 0 (which only turns -0 into +0: done on the bits), then * stdDev + mean
+// and the bounds.
 __device__ __forceinline__ void gauss_emit(const SpaceParams &sp, StatesView mean, double stddev, MutStatesView out,
                                            int64_t v, double g)
 {
     const int64_t i = v / sp.dim;
     const int d = (int)(v - i * sp.dim);
-    double z = __dadd_rn(__dmul_rn(__dadd_rn(g, 0.0), stddev), mean(i, d));
+    const double g0 = __double_as_longlong(g) == (long long)0x8000000000000000ull ? 0.0 : g;
+    double z = __dadd_rn(__dmul_rn(g0, stddev), mean(i, d));
     if (sp.kind == GBO_SPACE_SO2)
     {
         // SO2StateSpace::enforceBounds (SO2StateSpace.cpp:79-87)
@@ -623,9 +637,9 @@ __device__ __forceinline__ void gauss_emit(const SpaceParams &sp, StatesView mea
             r = __dsub_rn(r, 2.0 * kPi);
         z = r;
     }
-    else if (z < sp.low[d])
+    else if (dlt_bits(z, sp.low[d]))
         z = sp.low[d];
-    else if (z > sp.high[d])
+    else if (dlt_bits(sp.high[d], z))
         z = sp.high[d];
     out(i, d) = z;
 }
